@@ -1,0 +1,319 @@
+"""Benchmark: Gcell-updates/s of the GB300 stepper on a benchmark workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload visco2d|elastic2d|visco3d]
+    python bench.py --impl reference ...     # the CPU implementation of the same path
+
+One bench "step" is one complete simulation of the workload (all its time
+steps, e.g. 4000 steps of the 1024x1024 viscoelastic grid) from a zero state,
+with every input resident in HBM.  K steps are timed with CUDA events on the
+stream the kernels run on, bracketed by a barrier and synchronisations; L2 is
+flushed (a 256 MiB write) after every simulation, inside the timed region.
+Under torchrun each rank runs its own replica (the path shards over shots;
+a single-shot workload has no exchange), and the time is the max over ranks.
+
+The JSON line adds:
+  roofline     - HBM roofline of the dominant kernel (stress update),
+                 algorithmic bytes per launch / mean launch time (CUDA events
+                 around single launches), against the measured HBM peak;
+  cpu_baseline - the CPU restatement of the reference kernels (all host
+                 cores) on a bounded sample of the same workload;
+  e2e          - the same metric through the public C-ABI call sequence with
+                 host buffers: ts_create (uploads) + ts_run + ts_read of the
+                 traces and final field + ts_destroy, wall clock;
+  clocks       - SM clocks and throttle reasons sampled during the timing.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from taichi_sim_gb300 import workloads  # noqa: E402
+
+# Per-cell bytes each kernel must move at least once per step (float32):
+# stress: v read (2D 8, 3D 12), stresses r/w, memory variables r/w, moduli,
+# per-cell Q scale; velocity: stresses read, v r/w, dt/rho.  CPML strip
+# memories are added per strip cell.
+KERNEL_BYTES = {
+    "visco2d": {"stress": 8 + 24 + 72 + 12 + 8, "velocity": 12 + 16 + 8, "psi_stress": 8 * 2, "psi_vel": 8 * 2},
+    "elastic2d": {"stress": 8 + 24 + 12, "velocity": 12 + 16 + 8, "psi_stress": 8 * 2, "psi_vel": 8 * 2},
+    "visco3d": {"stress": 12 + 48 + 144 + 20 + 8, "velocity": 24 + 24 + 8, "psi_stress": 8 * 3, "psi_vel": 8 * 3},
+}
+FAMILY = {"elastic2d": "TAICHI2D", "visco2d": "WGSL2D", "visco3d": "WGSL3D"}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def build_model(name, time_steps=None):
+    from taichi_sim_gb300.sim_support.simulator import Simulator
+    from taichi_sim_gb300.sim_support.Simulator3D import Simulator3D
+    cfg = workloads.WORKLOADS[name]() if time_steps is None else workloads.WORKLOADS[name](n_steps=time_steps)
+    return (Simulator3D if name == "visco3d" else Simulator)(cfg)
+
+
+def strip_fraction(sim):
+    """Fraction of cells inside the CPML strips, per axis (a cell-weighted mean)."""
+    frac = []
+    for ax, n in zip("xyz", sim.grid_shape()):
+        a = getattr(sim, f"_a_{ax}").flatten()
+        b = getattr(sim, f"_b_{ax}").flatten()
+        nonid = (a != 0) | (b != 1)
+        frac.append(float(nonid.sum() + 2 * (sim._coefs.shape[0] - 1)) / n if nonid.any() else 0.0)
+    return frac
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons while timing."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        self.out.flush()
+        self.out.seek(0)
+        rows = [l.strip().split(", ") for l in self.out.read().splitlines() if l.strip()]
+        os.unlink(self.out.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        smax = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, name in enumerate(names):
+                if len(r) > 4 + k and r[4 + k].strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_baseline(sim, name, target_s=12.0):
+    """The CPU restatement of the reference kernels, all host cores, on a
+    bounded number of time steps of the same grid."""
+    from oracle import oracle
+    fam = {"elastic2d": oracle.TAICHI2D, "visco2d": oracle.WGSL2D, "visco3d": oracle.WGSL3D}[name]
+    cores = len(os.sched_getaffinity(0))
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    cells = int(np.prod(sim.grid_shape()))
+    t = time.time()
+    oracle.run(sim, fam, n_steps=4)
+    probe = max(time.time() - t, 1e-3) / 4
+    n = int(max(8, min(sim._n_steps, target_s / probe)))
+    t = time.time()
+    oracle.run(sim, fam, n_steps=n)
+    dt = time.time() - t
+    return {"value": cells * n / dt / 1e9, "unit": "Gcell/s", "cores": cores, "kind": "port",
+            "sample": f"{n} of {sim._n_steps} time steps of the full {'x'.join(map(str, sim.grid_shape()))} grid "
+                      f"(C restatement of the reference kernels, OpenMP, {dt:.1f} s)"}
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU path (the oracle port: the
+    reference's own kernels need Taichi/wgpu, absent here) on the same metric."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    name = args.workload
+    sim = build_model(name, args.time_steps)
+    from oracle import oracle
+    fam = {"elastic2d": oracle.TAICHI2D, "visco2d": oracle.WGSL2D, "visco3d": oracle.WGSL3D}[name]
+    cores = len(os.sched_getaffinity(0))
+    cells = int(np.prod(sim.grid_shape()))
+    sample = args.ref_sample_steps
+    for _ in range(args.warmup):
+        oracle.run(sim, fam, n_steps=max(2, sample // 10))
+    t = time.time()
+    for _ in range(args.steps):
+        oracle.run(sim, fam, n_steps=sample)
+    dt = time.time() - t
+    value = cells * sample * args.steps / dt / 1e9
+    line = {"impl": "reference", "metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": name, "grid": list(sim.grid_shape()), "time_steps_per_step": sample},
+            "cpu_baseline": {"value": value, "unit": "Gcell/s", "cores": cores, "kind": "port",
+                             "sample": f"{sample} time steps of the full grid per step"},
+            "e2e": {"value": value, "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="visco2d", choices=sorted(workloads.WORKLOADS))
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ref-sample-steps", type=int, default=200)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--profile-steps", type=int, default=200)
+    ap.add_argument("--time-steps", type=int, default=None,
+                    help="override the workload's time steps (small runs for profiler captures)")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        print("bench: at least 3 warm-up steps are required; using 3", file=sys.stderr)
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    from taichi_sim_gb300 import engine
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    name = args.workload
+    sim = build_model(name, args.time_steps)
+    n_t = int(sim._n_steps)
+    cells = int(np.prod(sim.grid_shape()))
+    fam = getattr(engine, FAMILY[name])
+    st = engine.Stepper(sim, family=fam)
+    stream = torch.cuda.Stream()
+    h = stream.cuda_stream
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def one_simulation():
+        st.reset(stream=h, wait=False)
+        st.run(n_t, stream=h)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    for _ in range(args.warmup):
+        one_simulation()
+    torch.cuda.synchronize()
+    _, _, bad = st.status()
+    if bad >= 0:
+        raise RuntimeError(f"workload unstable at step {bad}")
+    launches0 = st.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        start.record(stream)
+        for _ in range(args.steps):
+            one_simulation()
+        end.record(stream)
+        torch.cuda.synchronize()
+    launches = st.launch_count() - launches0
+    ms = start.elapsed_time(end)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = cells * n_t * args.steps * world / (ms / 1e3) / 1e9
+    clocks = clk.summary()
+
+    # ---- roofline of the dominant kernel (single launches between events) ----
+    st.reset()
+    k_ms = st.profile_steps(min(args.profile_steps, n_t), stream=h)
+    kb = KERNEL_BYTES[name]
+    frac = strip_fraction(sim)
+    strip_share = sum(frac) / len(frac)
+    bytes_stress = cells * (kb["stress"] + kb["psi_stress"] * 2 * strip_share)
+    bytes_vel = cells * (kb["velocity"] + kb["psi_vel"] * 2 * strip_share)
+    peak, peak_kind = peaks()
+    dom = 0 if k_ms[0] >= k_ms[1] else 1
+    dom_bytes = [bytes_stress, bytes_vel][dom]
+    achieved = dom_bytes / (k_ms[dom] / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", f"traffic_{name}.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(["stress", "velocity"][dom])
+    roofline = {"kernel": ["stress", "velocity"][dom], "bound": "hbm", "achieved": round(achieved, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                "peak_kind": peak_kind, "bytes_per_launch": int(dom_bytes),
+                "kernel_ms": {"stress": round(k_ms[0], 5), "velocity": round(k_ms[1], 5)}}
+    b_alg = workloads.B_ALG[name]
+    step_roofline = {"b_alg_per_cell_update": b_alg, "achieved": round(value * b_alg, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(value * b_alg / peak, 4),
+                     "note": "whole time step (both kernels) at the benchmark's algorithmic bytes per cell-update"}
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e_times, h2d, d2h = [], 0, 0
+    st.close()
+    for _ in range(args.e2e_steps):
+        torch.cuda.synchronize()
+        t0 = time.time()
+        with engine.Stepper(sim, family=fam) as s2:
+            s2.run(n_t)
+            tr = s2.read("traces")
+            fld = s2.read("szz" if sim._dims == 3 else "syy")
+            h2d, _ = s2.transfer_bytes()
+        torch.cuda.synchronize()
+        e2e_times.append(time.time() - t0)
+        d2h = tr.nbytes + fld.nbytes
+    e2e_s = float(np.mean(e2e_times))
+    e2e = {"value": cells * n_t * world / e2e_s / 1e9, "unit": "Gcell/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "seconds_per_step": round(e2e_s, 4),
+           "path": "ts_create + ts_run + ts_read(traces, field) + ts_destroy"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(sim, name)
+
+    if rank == 0:
+        line = {"metric": "Gcell-updates/s", "value": round(value, 3), "unit": "Gcell/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded numpy default_rng(0); no public dataset exists)",
+                "config": {"workload": name, "grid": list(sim.grid_shape()), "time_steps_per_step": n_t,
+                           "family": FAMILY[name], "receivers": int(sim._n_rec),
+                           "zener": "L=3 fitted 2-8 MHz, per-cell Q" if name != "elastic2d" else None,
+                           "l2": "256 MiB flush written after every simulation (inside the timed region)",
+                           "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+                "roofline": roofline, "step_roofline": step_roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": int(launches), "clocks": clocks}
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,175 @@
+/*
+ * taichi_sim_gb300 - C ABI of the GB300 (sm_103a) staggered-grid
+ * (visco)elastic time stepper.
+ *
+ * The reference project has no C interface: each backend's
+ * ``implementation()`` uploads the host model's tables to a device runtime,
+ * runs the per-step kernel loop and reads the results back.  This ABI is
+ * that boundary made explicit, with plain pointers and sizes:
+ *
+ *   ts_create        replaces the buffer uploads of
+ *                    sim_taichi_elastic.py:40-132,
+ *                    sim_webgpu_viscoelastic.py:57-191 and
+ *                    sim_webgpu_3D_viscoelastic.py:62-244
+ *   ts_run           replaces the time loops (kernel launches per step)
+ *                    sim_taichi_elastic.py:311-335,
+ *                    sim_webgpu_viscoelastic.py:469-537,
+ *                    sim_webgpu_3D_viscoelastic.py:628-695
+ *   ts_status        replaces the per-step velocity-norm read and the
+ *                    STABILITY_THRESHOLD test (sim_taichi_elastic.py:320-333,
+ *                    sim_webgpu_viscoelastic.py:518-535)
+ *   ts_read          replaces the final readbacks
+ *                    (sim_taichi_elastic.py:338-339,
+ *                    sim_webgpu_viscoelastic.py:540-543,
+ *                    sim_webgpu_3D_viscoelastic.py:698-701)
+ *   ts_set_sources   replaces the per-shot re-upload of the source term after
+ *                    ``set_t0`` (sim_support/simulator.py:329-337)
+ *   ts_reset         zeroes the wavefield for the next shot
+ *   ts_destroy       releases everything ts_create allocated
+ *
+ * Every input is a host pointer to the reference's own table, in the
+ * reference's layout (C order, last axis fastest); ts_create copies what it
+ * needs.  Calls on one handle must not overlap; different handles are
+ * independent.  All functions return TS_OK (0) or a positive TS_E* code;
+ * ts_strerror gives its text and ts_last_error the detail of the last
+ * failure on this thread.
+ */
+#ifndef TAICHI_SIM_GB300_H
+#define TAICHI_SIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TS_ABI_VERSION 1
+
+/* status codes */
+#define TS_OK 0
+#define TS_E_ARG 1        /* invalid argument or descriptor */
+#define TS_E_CUDA 2       /* CUDA runtime error (device lost, launch failure) */
+#define TS_E_NOMEM 3      /* device allocation failed */
+#define TS_E_NODEV 4      /* no usable sm_103 device */
+#define TS_E_STATE 5      /* call not valid in the handle's state */
+
+/* kernel families: which reference backend's semantics to follow */
+#define TS_TAICHI2D 0     /* sim_taichi_elastic.py:138-309 (2D elastic) */
+#define TS_WGSL2D 1       /* shader_webgpu_viscoelastic.wgsl:829-1141 */
+#define TS_WGSL3D 2       /* shader_webgpu_3D_viscoelastic.wgsl:1341-1850 */
+
+/* ts_read targets */
+#define TS_VX 0
+#define TS_VY 1
+#define TS_VZ 2
+#define TS_SXX 3
+#define TS_SYY 4
+#define TS_SZZ 5
+#define TS_SXY 6
+#define TS_SXZ 7
+#define TS_SYZ 8
+#define TS_TRACES 9       /* receiver traces, float [n_steps][n_rec] */
+
+typedef struct ts_sim ts_sim;
+
+typedef struct ts_desc {
+    int32_t abi_version;       /* TS_ABI_VERSION */
+    int32_t family;            /* TS_TAICHI2D / TS_WGSL2D / TS_WGSL3D */
+    int32_t nx, ny, nz;        /* full grid incl. CPML and pad; nz = 1 in 2D */
+    int32_t n_steps;           /* rows of the source term and of the traces */
+    int32_t ord;               /* number of staggered FD coefficients, 1..6 */
+    const float *coefs;        /* [ord]  (Simulator._coefs) */
+    float dx, dy, dz, dt;      /* grid steps (mm) and time step (us) */
+    /* CPML vectors, each of length n_axis - 2 (ord - 1): full-grid a/b/k and
+     * half-grid ah/bh/kh per axis (Simulator._a_x, _a_x_half, ...); the z
+     * set is unused in 2D and may be NULL. */
+    const float *a_x, *b_x, *k_x, *a_xh, *b_xh, *k_xh;
+    const float *a_y, *b_y, *k_y, *a_yh, *b_yh, *k_yh;
+    const float *a_z, *b_z, *k_z, *a_zh, *b_zh, *k_zh;
+    /* material grids [nx][ny][nz]: density as the host model leaves it (the
+     * reference averages it in place), P and S velocities */
+    const float *rho, *cp, *cs;
+    /* attenuation: visco = 0 is the elastic update */
+    int32_t visco;
+    int32_t n_sls;             /* Zener mechanisms, 1..8 */
+    const float *tau;          /* [4][n_sls]: tau_eps_p, tau_sigma_p, tau_eps_s, tau_sigma_s */
+    const float *sum_alpha;    /* [2]: sum tau_eps/tau_sigma for P and S */
+    /* optional per-cell quality factor (not in the reference): when g_p is
+     * non-NULL the memory-variable weight of mechanism l at a cell is
+     * zc[l] * g_p[cell] (P) or zc[l] * g_s[cell] (S), with relaxation
+     * constants zh[l] = dt / (2 tau_sigma_l) and zm[l] = 1 / (1 + zh[l]). */
+    const float *g_p, *g_s;    /* grids, or NULL */
+    const float *zc, *zh, *zm; /* [n_sls], or NULL */
+    /* sources: the reference's source term and source map */
+    const float *source_term;  /* [src_rows][src_cols] (a 1D term is src_cols = 1) */
+    int32_t src_rows, src_cols;
+    int32_t n_src_el;          /* Simulator._n_src (the WGSL backends' stride) */
+    const int32_t *pos_sources;/* grid, column index or -1 */
+    /* receivers */
+    int32_t n_rec, n_rec_pt;
+    const int32_t *pos_sensors;    /* grid, receiver index or -1 (Taichi family) */
+    const int32_t *info_rec_pt;    /* [n_rec_pt][dims+1]: grid indices, receiver (WGSL families) */
+    const int32_t *offset_sensors; /* [n_rec] first point of each receiver */
+    const int32_t *delay_rec;      /* [n_rec] first recorded step */
+} ts_desc;
+
+/* Allocate device state for one simulation on the current CUDA device and
+ * upload the tables.  The wavefield starts at zero. */
+int ts_create(const ts_desc *desc, ts_sim **out);
+
+/* Enqueue n_steps time steps on `stream` (a cudaStream_t, or NULL for the
+ * handle's own stream).  Asynchronous; steps past desc->n_steps are
+ * rejected with TS_E_ARG. */
+int ts_run(ts_sim *sim, int32_t n_steps, void *stream);
+
+/* Wait for queued steps; report the steps done, the largest squared
+ * velocity norm seen so far and the first step (0-based) whose norm broke
+ * the family's stability threshold (-1 if none).  Any pointer may be NULL. */
+int ts_status(ts_sim *sim, int32_t *steps_done, float *max_v2, int32_t *first_unstable_step);
+
+/* Wait for queued steps and copy one field ([nx][ny][nz] floats) or the
+ * traces ([n_steps][n_rec] floats) to host memory of `bytes` bytes. */
+int ts_read(ts_sim *sim, int32_t what, void *host_dst, size_t bytes);
+
+/* Replace the source term (same shape as at creation), e.g. for a new
+ * focal law. */
+int ts_set_sources(ts_sim *sim, const float *source_term);
+
+/* Zero the wavefield, memory variables, traces and the step counter. */
+int ts_reset(ts_sim *sim);
+
+/* As ts_reset, but enqueued on `stream` (NULL: the handle's own stream)
+ * without waiting; later ts_run calls on the same stream see the zeroed
+ * state. */
+int ts_reset_async(ts_sim *sim, void *stream);
+
+/* Run n_steps steps launching each kernel between CUDA events on `stream`
+ * and return the mean device time per launch of each kernel of a step, in
+ * milliseconds (ms_per_kernel[ts_launches_per_step]).  Advances the
+ * simulation like ts_run. */
+int ts_profile_steps(ts_sim *sim, int32_t n_steps, void *stream, float *ms_per_kernel);
+
+/* Total kernel launches this handle has issued (graph replays count every
+ * kernel node). */
+int ts_launch_count(const ts_sim *sim, int64_t *launches);
+
+/* Bytes this handle has copied host->device and device->host so far. */
+int ts_transfer_bytes(const ts_sim *sim, int64_t *h2d, int64_t *d2h);
+
+/* Device pointer and size of a field or of the traces, for zero-copy use
+ * by a caller on the same device. */
+int ts_device_buffer(ts_sim *sim, int32_t what, void **dev_ptr, size_t *pitch_bytes);
+
+/* Number of kernel launches one time step issues (for launch accounting). */
+int ts_launches_per_step(const ts_sim *sim, int32_t *launches);
+
+void ts_destroy(ts_sim *sim);
+
+const char *ts_strerror(int code);
+const char *ts_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,780 @@
+// C ABI of the GB300 stepper (include/taichi_sim_gb300.h): validation,
+// host-side preparation of the device layout, allocation, the CUDA-graph
+// step loop and readback.
+//
+// Preparation turns the reference's tables into the layout the kernels
+// stream (see ts_internal.cuh):
+//  * material: per-node moduli and inverse densities with the reference's
+//    averaging (sim_taichi_elastic.py:171-178, 223-227, 263, 293;
+//    shader_webgpu_viscoelastic.wgsl:863-868, 948-950, 1020, 1032;
+//    shader_webgpu_3D_viscoelastic.wgsl:1384-1388, 1481-1483, 1542-1544,
+//    1599-1601, 1676, 1690), folded with dt;
+//  * Zener constants evaluated like the shaders (wgsl:881-894) and folded
+//    into r' = A r + B d;
+//  * CPML tables re-indexed by grid node, strips found from where they
+//    differ from the identity;
+//  * sources: one entry per source node with the value table the reference
+//    would read at each step (Taichi: source_term[it-1, idx],
+//    sim_taichi_elastic.py:299; WGSL: flat[it * n_src + idx] when
+//    idx < n_src, wgsl:67-71), dropped where the reference cannot inject
+//    (rho <= 0, or outside the vy region in the Taichi kernel);
+//  * receivers: CSR lists of nodes; Taichi records row it-1 for 1-based
+//    it >= delay and only inside the normal-stress region
+//    (sim_taichi_elastic.py:188-190), WGSL row it for 0-based it >= delay
+//    over info_rec_pt (wgsl:1118-1134).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/taichi_sim_gb300.h"
+#include "ts_internal.cuh"
+
+namespace ts {
+
+__global__ void k_advance(int *step_base, int n) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *step_base += n;
+}
+
+void launch_advance(int *step_base, int n, cudaStream_t st) { k_advance<<<1, 32, 0, st>>>(step_base, n); }
+
+__global__ void k_reset_scalars(int *first_bad, int *step_base) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        *first_bad = 0x7fffffff;
+        *step_base = 0;
+    }
+}
+
+void launch_reset_scalars(int *first_bad, int *step_base, cudaStream_t st) {
+    k_reset_scalars<<<1, 32, 0, st>>>(first_bad, step_base);
+}
+
+}  // namespace ts
+
+using ts::Cpml;
+using ts::Source;
+using ts::StepParams;
+using ts::Strip;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return TS_E_CUDA;
+}
+
+#define TS_CUDA(call)                                                   \
+    do {                                                                \
+        cudaError_t _e = (call);                                        \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call);             \
+    } while (0)
+
+constexpr int kGraphSteps = 32;
+
+}  // namespace
+
+struct ts_sim {
+    int family = 0, dims = 2, ord = 2, zen_mode = 0;
+    int nx = 0, ny = 0, nz = 1, pitch = 0;
+    int64_t grid_elems = 0;
+    int n_rows = 0, n_rec = 0, n_blocks = 0;
+    int steps_done = 0;
+    int64_t launches = 0;
+    int64_t h2d_bytes = 0, d2h_bytes = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    std::vector<void *> allocs;
+    float *field[9] = {};
+    float *traces = nullptr;
+    float *block_max = nullptr;
+    int *first_bad = nullptr;
+    int *step_base = nullptr;
+    float *src_tab = nullptr;
+    // host copies needed to rebuild the source table
+    int src_rows = 0, src_cols_in = 0, n_src_el = 0;
+    std::vector<int> src_col_idx;  // reference column of each device column
+    std::vector<size_t> state_bytes;
+    std::vector<void *> state_ptrs;
+    StepParams p{};
+
+    template <typename T>
+    int alloc(T **ptr, size_t count, bool state) {
+        void *d = nullptr;
+        size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+        cudaError_t e = cudaMalloc(&d, bytes);
+        if (e != cudaSuccess) {
+            g_last_error = std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e);
+            return TS_E_NOMEM;
+        }
+        allocs.push_back(d);
+        *ptr = static_cast<T *>(d);
+        if (state) {
+            state_ptrs.push_back(d);
+            state_bytes.push_back(bytes);
+        }
+        return TS_OK;
+    }
+
+    template <typename T>
+    int upload(T **ptr, const std::vector<T> &h) {
+        int rc = alloc(ptr, h.size(), false);
+        if (rc) return rc;
+        if (!h.empty()) TS_CUDA(cudaMemcpy(*ptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+        h2d_bytes += (int64_t)(h.size() * sizeof(T));
+        return TS_OK;
+    }
+
+    // padded index of grid node (x, y[, z])
+    int64_t at(int x, int y, int z = 0) const {
+        return dims == 2 ? (int64_t)x * pitch + y : ((int64_t)x * ny + y) * pitch + z;
+    }
+};
+
+namespace {
+
+struct Axis {
+    std::vector<Cpml> full, half;
+    Strip strip;
+};
+
+bool identity(const Cpml &c) { return c.a == 0.f && c.b == 1.f && c.ik == 1.f; }
+
+Axis make_axis(int n, int ord, const float *a, const float *b, const float *k, const float *ah, const float *bh,
+               const float *kh) {
+    Axis ax;
+    const int off = ord - 1, ntab = n - 2 * (ord - 1);
+    ax.full.assign(n, Cpml{0.f, 1.f, 1.f, 0.f});
+    ax.half.assign(n, Cpml{0.f, 1.f, 1.f, 0.f});
+    std::vector<char> nonid(n, 0);
+    for (int x = 0; x < n; ++x) {
+        const int t = x - off;
+        if (t < 0 || t >= ntab || !a) continue;
+        ax.full[x] = Cpml{a[t], b[t], 1.f / k[t], 0.f};
+        ax.half[x] = Cpml{ah[t], bh[t], 1.f / kh[t], 0.f};
+        nonid[x] = !identity(ax.full[x]) || !identity(ax.half[x]);
+    }
+    int lo = 0, hi = n;
+    for (int x = 0; x < n / 2; ++x)
+        if (nonid[x]) lo = x + 1;
+    for (int x = n - 1; x >= n / 2; --x)
+        if (nonid[x]) hi = x;
+    ax.strip = Strip{lo, hi, lo + (n - hi)};
+    return ax;
+}
+
+int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+}  // namespace
+
+extern "C" {
+
+const char *ts_strerror(int code) {
+    switch (code) {
+    case TS_OK: return "ok";
+    case TS_E_ARG: return "invalid argument";
+    case TS_E_CUDA: return "CUDA runtime error";
+    case TS_E_NOMEM: return "device memory exhausted";
+    case TS_E_NODEV: return "no usable sm_103 device";
+    case TS_E_STATE: return "invalid state";
+    default: return "unknown error";
+    }
+}
+
+const char *ts_last_error(void) { return g_last_error.c_str(); }
+
+void ts_destroy(ts_sim *s) {
+    if (!s) return;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->done) cudaEventSynchronize(s->done);
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    for (void *d : s->allocs) cudaFree(d);
+    if (s->done) cudaEventDestroy(s->done);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    cudaSetDevice(prev);
+    delete s;
+}
+
+static int validate(const ts_desc *d) {
+    if (!d) return fail(TS_E_ARG, "null descriptor");
+    if (d->abi_version != TS_ABI_VERSION) return fail(TS_E_ARG, "abi_version mismatch");
+    if (d->family < TS_TAICHI2D || d->family > TS_WGSL3D) return fail(TS_E_ARG, "unknown family");
+    if (d->ord < 2 || d->ord > ts::kMaxOrd) return fail(TS_E_ARG, "ord must be in [2, 6]");
+    const int dims = d->family == TS_WGSL3D ? 3 : 2;
+    const int minn = 2 * d->ord + 1;
+    if (d->nx < minn || d->ny < minn || (dims == 3 && d->nz < minn)) return fail(TS_E_ARG, "grid smaller than the stencil");
+    if (dims == 2 && d->nz != 1) return fail(TS_E_ARG, "nz must be 1 in 2D");
+    if (d->n_steps < 1) return fail(TS_E_ARG, "n_steps must be positive");
+    if (!d->coefs || !d->rho || !d->cp || !d->cs) return fail(TS_E_ARG, "missing coefficient or material table");
+    if (!d->a_x || !d->b_x || !d->k_x || !d->a_xh || !d->b_xh || !d->k_xh || !d->a_y || !d->b_y || !d->k_y ||
+        !d->a_yh || !d->b_yh || !d->k_yh)
+        return fail(TS_E_ARG, "missing CPML table");
+    if (dims == 3 && (!d->a_z || !d->b_z || !d->k_z || !d->a_zh || !d->b_zh || !d->k_zh))
+        return fail(TS_E_ARG, "missing z CPML table");
+    if (!(d->dx > 0.f) || !(d->dy > 0.f) || !(d->dt > 0.f) || (dims == 3 && !(d->dz > 0.f)))
+        return fail(TS_E_ARG, "grid and time steps must be positive");
+    if (d->family == TS_TAICHI2D && d->visco) return fail(TS_E_ARG, "the Taichi family is elastic only");
+    if (d->visco) {
+        if (d->n_sls < 1 || d->n_sls > ts::kMaxSls) return fail(TS_E_ARG, "n_sls must be in [1, 8]");
+        if (!d->g_p && (!d->tau || !d->sum_alpha)) return fail(TS_E_ARG, "missing Zener tables");
+        if (d->g_p && (!d->g_s || !d->zc || !d->zh || !d->zm)) return fail(TS_E_ARG, "incomplete per-cell Q tables");
+    }
+    if (!d->source_term || !d->pos_sources || d->src_rows < 1 || d->src_cols < 1)
+        return fail(TS_E_ARG, "missing source term or source map");
+    if (d->n_rec < 0 || d->n_rec_pt < 0 || !d->delay_rec) return fail(TS_E_ARG, "bad receiver counts");
+    if (d->n_rec > 0 && d->family == TS_TAICHI2D && !d->pos_sensors) return fail(TS_E_ARG, "missing sensor map");
+    if (d->n_rec > 0 && d->family != TS_TAICHI2D && (!d->info_rec_pt || !d->offset_sensors))
+        return fail(TS_E_ARG, "missing receiver point table");
+    return TS_OK;
+}
+
+int ts_create(const ts_desc *d, ts_sim **out) {
+    if (!out) return fail(TS_E_ARG, "null output handle");
+    *out = nullptr;
+    int rc = validate(d);
+    if (rc) return rc;
+
+    int device = 0;
+    TS_CUDA(cudaGetDevice(&device));
+    cudaDeviceProp prop;
+    TS_CUDA(cudaGetDeviceProperties(&prop, device));
+    if (!(prop.major == 10 && prop.minor == 3))
+        return fail(TS_E_NODEV, "device " + std::string(prop.name) + " is sm_" + std::to_string(prop.major) +
+                                    std::to_string(prop.minor) + "; this library is built for sm_103a only");
+
+    ts_sim *s = new ts_sim();
+    s->device = device;
+    s->family = d->family;
+    s->dims = d->family == TS_WGSL3D ? 3 : 2;
+    s->ord = d->ord;
+    s->nx = d->nx;
+    s->ny = d->ny;
+    s->nz = s->dims == 3 ? d->nz : 1;
+    const int last = s->dims == 2 ? s->ny : s->nz;
+    s->pitch = round_up(last, 32);
+    s->grid_elems = (int64_t)s->nx * (s->dims == 2 ? 1 : s->ny) * s->pitch;
+    s->n_rows = d->n_steps;
+    s->n_rec = d->n_rec;
+    const int nx = s->nx, ny = s->ny, nz = s->nz, ord = s->ord;
+    const int64_t ncell = (int64_t)nx * ny * nz;
+    auto bail = [&](int code) {
+        ts_destroy(s);
+        return code;
+    };
+    auto href = [&](int x, int y, int z) -> int64_t { return ((int64_t)x * ny + y) * nz + z; };
+    auto rho = [&](int x, int y, int z) -> float {
+        if (x < 0 || x >= nx || y < 0 || y >= ny || z < 0 || z >= nz) return 0.f;
+        return d->rho[href(x, y, z)];
+    };
+    auto csv = [&](int x, int y, int z) -> float {
+        if (x < 0 || x >= nx || y < 0 || y >= ny || z < 0 || z >= nz) return 0.f;
+        return d->cs[href(x, y, z)];
+    };
+    auto cpv = [&](int x, int y, int z) -> float {
+        if (x < 0 || x >= nx || y < 0 || y >= ny || z < 0 || z >= nz) return 0.f;
+        return d->cp[href(x, y, z)];
+    };
+
+    StepParams &p = s->p;
+    p.family = s->family;
+    p.nx = nx;
+    p.ny = ny;
+    p.nz = nz;
+    p.pitch = s->pitch;
+    p.plane = s->dims == 2 ? s->pitch : (int64_t)ny * s->pitch;
+    p.grid_elems = s->grid_elems;
+    const float steps[3] = {d->dx, d->dy, d->dz};
+    for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < ts::kMaxOrd; ++c) p.cd[a][c] = c < ord ? d->coefs[c] / steps[a] : 0.f;
+
+    // ---- CPML tables and strips ----
+    Axis axes[3];
+    axes[0] = make_axis(nx, ord, d->a_x, d->b_x, d->k_x, d->a_xh, d->b_xh, d->k_xh);
+    axes[1] = make_axis(ny, ord, d->a_y, d->b_y, d->k_y, d->a_yh, d->b_yh, d->k_yh);
+    if (s->dims == 3) axes[2] = make_axis(nz, ord, d->a_z, d->b_z, d->k_z, d->a_zh, d->b_zh, d->k_zh);
+    else axes[2] = make_axis(1, ord, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    for (int a = 0; a < 3; ++a) {
+        Cpml *f = nullptr, *h = nullptr;
+        if ((rc = s->upload(&f, axes[a].full)) || (rc = s->upload(&h, axes[a].half))) return bail(rc);
+        p.tab_f[a] = f;
+        p.tab_h[a] = h;
+        p.strip[a] = axes[a].strip;
+    }
+
+    // ---- fields ----
+    const int nfields = s->dims == 2 ? 5 : 9;
+    const int field_ids2[5] = {TS_VX, TS_VY, TS_SXX, TS_SYY, TS_SXY};
+    for (int f = 0; f < nfields; ++f) {
+        const int id = s->dims == 2 ? field_ids2[f] : f;
+        if ((rc = s->alloc(&s->field[id], s->grid_elems, true))) return bail(rc);
+    }
+    for (int c = 0; c < 3; ++c) p.v[c] = s->field[TS_VX + c];
+    for (int c = 0; c < 6; ++c) p.s[c] = s->field[TS_SXX + c];
+
+    // ---- strip memories ----
+    const Strip &sx = p.strip[0], &sy = p.strip[1], &sz = p.strip[2];
+    if (s->dims == 2) {
+        const int64_t xs = (int64_t)sx.width * s->pitch, ys = (int64_t)nx * sy.width;
+        const int64_t sizes[8] = {xs, xs, ys, ys, xs, xs, ys, ys};
+        for (int k = 0; k < 8; ++k)
+            if ((rc = s->alloc(&p.psi[k], sizes[k], true))) return bail(rc);
+    } else {
+        const int64_t xs = (int64_t)sx.width * ny * s->pitch, ys = (int64_t)nx * sy.width * s->pitch,
+                      zs = (int64_t)nx * ny * sz.width;
+        // stress: 0 x, 1 y, 2 z, 3 x, 4 y, 5 x, 6 z, 7 y, 8 z; velocity: 9 x, 10 y, 11 z, 12 x, 13 y, 14 z, 15 x, 16 y, 17 z
+        const char axis_of[18] = {'x', 'y', 'z', 'x', 'y', 'x', 'z', 'y', 'z',
+                                  'x', 'y', 'z', 'x', 'y', 'z', 'x', 'y', 'z'};
+        for (int k = 0; k < 18; ++k) {
+            const int64_t n = axis_of[k] == 'x' ? xs : axis_of[k] == 'y' ? ys : zs;
+            if ((rc = s->alloc(&p.psi[k], n, true))) return bail(rc);
+        }
+    }
+
+    // ---- per-node coefficients (host, reference averaging, folded with dt) ----
+    const float dt = d->dt;
+    std::vector<float> lam(s->grid_elems, 0.f), mu(s->grid_elems, 0.f), dtr0(s->grid_elems, 0.f),
+        dtr1(s->grid_elems, 0.f);
+    std::vector<float> mus[3];
+    const int n_shear = s->dims == 2 ? 1 : 3;
+    for (int k = 0; k < n_shear; ++k) mus[k].assign(s->grid_elems, 0.f);
+    auto inv_or0 = [&](float r) { return r > 0.f ? dt / r : 0.f; };
+    if (s->dims == 2) {
+        for (int x = 0; x < nx; ++x)
+            for (int y = 0; y < ny; ++y) {
+                const int64_t i = s->at(x, y);
+                // normal node: x-averaged, mu zero where either cs is zero
+                const float rh = 0.5f * (rho(x + 1, y, 0) + rho(x, y, 0));
+                const float cph = 0.5f * (cpv(x + 1, y, 0) + cpv(x, y, 0));
+                const float c1 = csv(x + 1, y, 0), c0 = csv(x, y, 0);
+                const float csl = 0.5f * (c1 + c0);
+                const float csm = std::min(c1, c0) == 0.f ? 0.f : csl;
+                lam[i] = rh * (cph * cph - 2.f * csl * csl) * dt;
+                mu[i] = rh * (csm * csm) * dt;
+                // shear node: y-averaged
+                const float rhy = 0.5f * (rho(x, y + 1, 0) + rho(x, y, 0));
+                const float s1 = csv(x, y + 1, 0), s0 = csv(x, y, 0);
+                const float csh = std::min(s1, s0) == 0.f ? 0.f : 0.5f * (s1 + s0);
+                mus[0][i] = rhy * (csh * csh) * dt;
+                dtr0[i] = inv_or0(rho(x, y, 0));
+                const float r4 = s->family == TS_TAICHI2D
+                                     ? 0.25f * (rho(x, y + 1, 0) + rho(x, y, 0) + rho(x + 1, y + 1, 0) + rho(x + 1, y, 0))
+                                     : 0.25f * (rho(x, y, 0) + rho(x + 1, y, 0) + rho(x + 1, y + 1, 0) + rho(x, y + 1, 0));
+                dtr1[i] = inv_or0(r4);
+            }
+    } else {
+        for (int x = 0; x < nx; ++x)
+            for (int y = 0; y < ny; ++y)
+                for (int z = 0; z < nz; ++z) {
+                    const int64_t i = s->at(x, y, z);
+                    const float r = rho(x, y, z), cp = cpv(x, y, z), cs = csv(x, y, z);
+                    lam[i] = r * (cp * cp - 2.f * cs * cs) * dt;
+                    mu[i] = r * (cs * cs) * dt;
+                    const float rxy = 0.25f * (rho(x + 1, y, z) + rho(x, y, z) + rho(x, y + 1, z) + rho(x + 1, y + 1, z));
+                    const float cxy = 0.25f * (csv(x + 1, y, z) + csv(x, y, z) + csv(x, y + 1, z) + csv(x + 1, y + 1, z));
+                    const float rxz = 0.25f * (rho(x + 1, y, z) + rho(x, y, z) + rho(x, y, z + 1) + rho(x + 1, y, z + 1));
+                    const float cxz = 0.25f * (csv(x + 1, y, z) + csv(x, y, z) + csv(x, y, z + 1) + csv(x + 1, y, z + 1));
+                    const float ryz = 0.25f * (rho(x, y + 1, z) + rho(x, y, z) + rho(x, y, z + 1) + rho(x, y + 1, z + 1));
+                    const float cyz = 0.25f * (csv(x, y + 1, z) + csv(x, y, z) + csv(x, y, z + 1) + csv(x, y + 1, z + 1));
+                    mus[0][i] = rxy * (cxy * cxy) * dt;
+                    mus[1][i] = rxz * (cxz * cxz) * dt;
+                    mus[2][i] = ryz * (cyz * cyz) * dt;
+                    dtr0[i] = inv_or0(0.5f * (rho(x + 1, y, z) + r));
+                    dtr1[i] = inv_or0(0.5f * (rho(x, y + 1, z) + r));
+                }
+    }
+    float *dev = nullptr;
+    if ((rc = s->upload(&dev, lam))) return bail(rc);
+    p.lam_dt = dev;
+    if ((rc = s->upload(&dev, mu))) return bail(rc);
+    p.mu_dt = dev;
+    for (int k = 0; k < n_shear; ++k) {
+        if ((rc = s->upload(&dev, mus[k]))) return bail(rc);
+        p.mus_dt[k] = dev;
+    }
+    if ((rc = s->upload(&dev, dtr0))) return bail(rc);
+    p.dtr[0] = dev;
+    if ((rc = s->upload(&dev, dtr1))) return bail(rc);
+    p.dtr[1] = dev;
+    p.dtr[2] = dev;  // vz uses the vy-node density (wgsl3d:1748)
+
+    // ---- attenuation ----
+    s->zen_mode = !d->visco ? 0 : (d->g_p ? 2 : 1);
+    if (d->visco) {
+        const int L = d->n_sls;
+        p.zen.n = L;
+        for (int l = 0; l < L; ++l) {
+            float hp, hs, mp, ms, bp, bs;
+            if (s->zen_mode == 1) {
+                const float inv_p = 1.f / d->tau[1 * L + l], inv_s = 1.f / d->tau[3 * L + l];
+                const float ap = d->tau[0 * L + l] / d->tau[1 * L + l], as = d->tau[2 * L + l] / d->tau[3 * L + l];
+                const float php = dt * (1.f - ap) * inv_p / d->sum_alpha[0];
+                const float phs = dt * (1.f - as) * inv_s / d->sum_alpha[1];
+                hp = 0.5f * dt * inv_p;
+                hs = 0.5f * dt * inv_s;
+                mp = 1.f / (1.f + hp);
+                ms = 1.f / (1.f + hs);
+                bp = php * mp;
+                bs = phs * ms;
+            } else {
+                hp = hs = d->zh[l];
+                mp = ms = d->zm[l];
+                bp = bs = d->zc[l] * d->zm[l];
+            }
+            p.zen.Ap[l] = (1.f - hp) * mp;
+            p.zen.As[l] = (1.f - hs) * ms;
+            p.zen.Bp[l] = bp;
+            p.zen.Bs[l] = bs;
+        }
+        const int nmem = s->dims == 2 ? 3 : 6;
+        for (int m = 0; m < nmem; ++m)
+            if ((rc = s->alloc(&p.r[m], s->grid_elems * L, true))) return bail(rc);
+        if (s->zen_mode == 2) {
+            std::vector<float> gp(s->grid_elems, 0.f), gs(s->grid_elems, 0.f);
+            for (int x = 0; x < nx; ++x)
+                for (int y = 0; y < ny; ++y)
+                    for (int z = 0; z < nz; ++z) {
+                        gp[s->at(x, y, z)] = d->g_p[href(x, y, z)];
+                        gs[s->at(x, y, z)] = d->g_s[href(x, y, z)];
+                    }
+            if ((rc = s->upload(&dev, gp))) return bail(rc);
+            p.g_p = dev;
+            if ((rc = s->upload(&dev, gs))) return bail(rc);
+            p.g_s = dev;
+        }
+    }
+
+    // ---- launch geometry ----
+    s->n_blocks = s->dims == 2 ? ts::blocks_2d(p) : ts::blocks_3d(p);
+    auto block_of = [&](int x, int y, int z) -> int {
+        if (s->dims == 2) {
+            const int gx = (ny + ts::kBX2 - 1) / ts::kBX2;
+            return (x / ts::kBY2) * gx + y / ts::kBX2;
+        }
+        const int gx = (nz + ts::kBX3 - 1) / ts::kBX3, gy = (ny + ts::kBY3 - 1) / ts::kBY3;
+        return ((x / ts::kBZ3) * gy + y / ts::kBY3) * gx + z / ts::kBX3;
+    };
+
+    // ---- sources ----
+    {
+        s->src_rows = d->src_rows;
+        s->src_cols_in = d->src_cols;
+        s->n_src_el = d->n_src_el;
+        struct Cand {
+            int blk;
+            Source s;
+        };
+        std::vector<Cand> cands;
+        std::map<int, int> col_of;
+        for (int x = 0; x < nx; ++x)
+            for (int y = 0; y < ny; ++y)
+                for (int z = 0; z < nz; ++z) {
+                    const int idx = d->pos_sources[href(x, y, z)];
+                    if (idx == -1) continue;
+                    float r;
+                    if (s->family == TS_TAICHI2D) {
+                        const bool in_vy = x >= ord - 1 && x < nx - ord && y >= ord - 1 && y < ny - ord;
+                        if (!in_vy || idx < 0 || idx >= d->src_cols) continue;
+                        r = 0.25f * (rho(x, y + 1, 0) + rho(x, y, 0) + rho(x + 1, y + 1, 0) + rho(x + 1, y, 0));
+                    } else if (s->dims == 2) {
+                        r = 0.25f * (rho(x, y, 0) + rho(x + 1, y, 0) + rho(x + 1, y + 1, 0) + rho(x, y + 1, 0));
+                    } else {
+                        r = 0.5f * (rho(x, y + 1, z) + rho(x, y, z));
+                    }
+                    if (!(r > 0.f)) continue;
+                    if (!col_of.count(idx)) {
+                        const int c = (int)col_of.size();
+                        col_of[idx] = c;
+                        s->src_col_idx.push_back(idx);
+                    }
+                    cands.push_back({block_of(x, y, z), Source{s->at(x, y, z), col_of[idx], dt / r}});
+                }
+        std::stable_sort(cands.begin(), cands.end(), [](const Cand &a, const Cand &b) { return a.blk < b.blk; });
+        std::vector<Source> list;
+        std::vector<int> start(s->n_blocks + 1, 0);
+        for (const Cand &c : cands) {
+            list.push_back(c.s);
+            start[c.blk + 1]++;
+        }
+        for (int b = 0; b < s->n_blocks; ++b) start[b + 1] += start[b];
+        Source *dsrc = nullptr;
+        int *dstart = nullptr;
+        if ((rc = s->upload(&dsrc, list)) || (rc = s->upload(&dstart, start))) return bail(rc);
+        p.src = dsrc;
+        p.src_block_start = dstart;
+        p.src_rows = d->src_rows;
+        p.src_ncol = std::max<int>(1, (int)s->src_col_idx.size());
+        if ((rc = s->alloc(&s->src_tab, (size_t)p.src_rows * p.src_ncol, false))) return bail(rc);
+        p.src_tab = s->src_tab;
+        if ((rc = ts_set_sources(s, d->source_term))) return bail(rc);
+    }
+
+    // ---- receivers ----
+    {
+        std::vector<int> start(1, 0), first(d->n_rec, 0);
+        std::vector<int64_t> cells;
+        if (s->family == TS_TAICHI2D) {
+            std::vector<std::vector<int64_t>> per(d->n_rec);
+            for (int x = ord - 1; x < nx - ord; ++x)
+                for (int y = ord; y < ny - ord + 1; ++y) {
+                    const int sn = d->pos_sensors[href(x, y, 0)];
+                    if (sn >= 0 && sn < d->n_rec) per[sn].push_back(s->at(x, y));
+                }
+            for (int r = 0; r < d->n_rec; ++r) {
+                cells.insert(cells.end(), per[r].begin(), per[r].end());
+                start.push_back((int)cells.size());
+                first[r] = d->delay_rec[r] - 1;  // 1-based it >= delay
+            }
+        } else {
+            const int cols = 1 + s->dims;  // [ix, iy(, iz), receiver]
+            for (int r = 0; r < d->n_rec; ++r) {
+                for (int pt = d->offset_sensors[r]; pt >= 0 && pt < d->n_rec_pt && d->info_rec_pt[pt * cols + cols - 1] == r;
+                     ++pt) {
+                    const int *q = d->info_rec_pt + pt * cols;
+                    const int x = q[0], y = q[1], z = s->dims == 3 ? q[2] : 0;
+                    if (x < 0 || x >= nx || y < 0 || y >= ny || z < 0 || z >= nz) continue;  // reads as 0
+                    cells.push_back(s->at(x, y, z));
+                }
+                start.push_back((int)cells.size());
+                first[r] = d->delay_rec[r];
+            }
+        }
+        int *ds = nullptr, *df = nullptr;
+        int64_t *dc = nullptr;
+        if ((rc = s->upload(&ds, start)) || (rc = s->upload(&df, first)) || (rc = s->upload(&dc, cells))) return bail(rc);
+        p.n_rec = d->n_rec;
+        p.rec_start = ds;
+        p.rec_first_step = df;
+        p.rec_cell = dc;
+        if ((rc = s->alloc(&s->traces, (size_t)s->n_rows * std::max(1, d->n_rec), true))) return bail(rc);
+        p.traces = s->traces;
+    }
+
+    // ---- stability bookkeeping ----
+    p.v2_threshold = s->family == TS_TAICHI2D ? 1.0e38f : FLT_MAX;
+    if ((rc = s->alloc(&s->block_max, s->n_blocks, true)) || (rc = s->alloc(&s->first_bad, 1, false)) ||
+        (rc = s->alloc(&s->step_base, 1, false)))
+        return bail(rc);
+    p.block_max = s->block_max;
+    p.first_bad = s->first_bad;
+    p.step_base = s->step_base;
+
+    cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
+    e = cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaEventCreate"));
+    if ((rc = ts_reset(s))) return bail(rc);
+    *out = s;
+    return TS_OK;
+}
+
+int ts_set_sources(ts_sim *s, const float *source_term) {
+    if (!s || !source_term) return fail(TS_E_ARG, "null argument");
+    const int rows = s->src_rows, ncol = s->p.src_ncol;
+    std::vector<float> tab((size_t)rows * ncol, 0.f);
+    for (int c = 0; c < (int)s->src_col_idx.size(); ++c) {
+        const int idx = s->src_col_idx[c];
+        for (int k = 0; k < rows; ++k) {
+            float v = 0.f;
+            if (s->family == TS_TAICHI2D) {
+                v = source_term[(int64_t)k * s->src_cols_in + idx];
+            } else if (idx >= 0 && idx < s->n_src_el && k < s->n_rows) {
+                const int64_t flat = (int64_t)k * s->n_src_el + idx;
+                if (flat < (int64_t)rows * s->src_cols_in) v = source_term[flat];
+            }
+            tab[(size_t)k * ncol + c] = v;
+        }
+    }
+    if (s->done) TS_CUDA(cudaEventSynchronize(s->done));
+    TS_CUDA(cudaMemcpy(s->src_tab, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice));
+    s->h2d_bytes += (int64_t)(tab.size() * sizeof(float));
+    return TS_OK;
+}
+
+int ts_reset_async(ts_sim *s, void *stream) {
+    if (!s) return fail(TS_E_ARG, "null handle");
+    TS_CUDA(cudaSetDevice(s->device));
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : s->stream;
+    for (size_t k = 0; k < s->state_ptrs.size(); ++k)
+        TS_CUDA(cudaMemsetAsync(s->state_ptrs[k], 0, s->state_bytes[k], st));
+    ts::launch_reset_scalars(s->first_bad, s->step_base, st);
+    s->launches += 1;
+    TS_CUDA(cudaGetLastError());
+    TS_CUDA(cudaEventRecord(s->done, st));
+    s->steps_done = 0;
+    return TS_OK;
+}
+
+int ts_reset(ts_sim *s) {
+    int rc = ts_reset_async(s, nullptr);
+    if (rc) return rc;
+    TS_CUDA(cudaStreamSynchronize(s->stream));
+    return TS_OK;
+}
+
+int ts_profile_steps(ts_sim *s, int32_t n_steps, void *stream, float *ms_per_kernel) {
+    if (!s || !ms_per_kernel) return fail(TS_E_ARG, "null argument");
+    if (n_steps < 1 || s->steps_done + (int64_t)n_steps > s->n_rows)
+        return fail(TS_E_ARG, "steps beyond the source/trace length");
+    TS_CUDA(cudaSetDevice(s->device));
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : s->stream;
+    std::vector<cudaEvent_t> ev(2 * n_steps + 1);
+    for (auto &e : ev) TS_CUDA(cudaEventCreate(&e));
+    TS_CUDA(cudaEventRecord(ev[0], st));
+    for (int j = 0; j < n_steps; ++j) {
+        for (int part = 0; part < 2; ++part) {
+            if (s->dims == 2) ts::launch_step_2d(s->p, s->ord, s->zen_mode, j, st, 1 << part);
+            else ts::launch_step_3d(s->p, s->ord, s->zen_mode, j, st, 1 << part);
+            TS_CUDA(cudaEventRecord(ev[2 * j + part + 1], st));
+        }
+    }
+    ts::launch_advance(s->step_base, n_steps, st);
+    s->launches += 2 * (int64_t)n_steps + 1;
+    TS_CUDA(cudaGetLastError());
+    TS_CUDA(cudaEventSynchronize(ev.back()));
+    double tot[2] = {0.0, 0.0};
+    for (int j = 0; j < n_steps; ++j)
+        for (int part = 0; part < 2; ++part) {
+            float ms = 0.f;
+            TS_CUDA(cudaEventElapsedTime(&ms, ev[2 * j + part], ev[2 * j + part + 1]));
+            tot[part] += ms;
+        }
+    for (auto &e : ev) cudaEventDestroy(e);
+    ms_per_kernel[0] = (float)(tot[0] / n_steps);
+    ms_per_kernel[1] = (float)(tot[1] / n_steps);
+    TS_CUDA(cudaEventRecord(s->done, st));
+    s->steps_done += n_steps;
+    return TS_OK;
+}
+
+int ts_transfer_bytes(const ts_sim *s, int64_t *h2d, int64_t *d2h) {
+    if (!s) return fail(TS_E_ARG, "null handle");
+    if (h2d) *h2d = s->h2d_bytes;
+    if (d2h) *d2h = s->d2h_bytes;
+    return TS_OK;
+}
+
+int ts_launch_count(const ts_sim *s, int64_t *launches) {
+    if (!s || !launches) return fail(TS_E_ARG, "null argument");
+    *launches = s->launches;
+    return TS_OK;
+}
+
+int ts_run(ts_sim *s, int32_t n_steps, void *stream) {
+    if (!s) return fail(TS_E_ARG, "null handle");
+    if (n_steps < 0 || s->steps_done + (int64_t)n_steps > s->n_rows)
+        return fail(TS_E_ARG, "steps beyond the source/trace length");
+    TS_CUDA(cudaSetDevice(s->device));
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : s->stream;
+    auto launch_steps = [&](int count, cudaStream_t where) {
+        for (int j = 0; j < count; ++j) {
+            if (s->dims == 2) ts::launch_step_2d(s->p, s->ord, s->zen_mode, j, where);
+            else ts::launch_step_3d(s->p, s->ord, s->zen_mode, j, where);
+        }
+        ts::launch_advance(s->step_base, count, where);
+    };
+    if (!s->graph && n_steps >= kGraphSteps) {
+        cudaGraph_t g = nullptr;
+        TS_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        launch_steps(kGraphSteps, s->stream);
+        TS_CUDA(cudaStreamEndCapture(s->stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&s->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    int left = n_steps;
+    while (left >= kGraphSteps && s->graph) {
+        TS_CUDA(cudaGraphLaunch(s->graph, st));
+        s->launches += 2 * kGraphSteps + 1;
+        left -= kGraphSteps;
+    }
+    if (left > 0) {
+        launch_steps(left, st);
+        s->launches += 2 * left + 1;
+    }
+    TS_CUDA(cudaGetLastError());
+    TS_CUDA(cudaEventRecord(s->done, st));
+    s->steps_done += n_steps;
+    return TS_OK;
+}
+
+int ts_status(ts_sim *s, int32_t *steps_done, float *max_v2, int32_t *first_unstable) {
+    if (!s) return fail(TS_E_ARG, "null handle");
+    TS_CUDA(cudaSetDevice(s->device));
+    TS_CUDA(cudaEventSynchronize(s->done));
+    if (steps_done) *steps_done = s->steps_done;
+    if (max_v2) {
+        std::vector<unsigned> bm(s->n_blocks);
+        TS_CUDA(cudaMemcpy(bm.data(), s->block_max, bm.size() * sizeof(unsigned), cudaMemcpyDeviceToHost));
+        unsigned m = 0;
+        for (unsigned v : bm) m = std::max(m, v);
+        float f;
+        std::memcpy(&f, &m, sizeof(f));
+        *max_v2 = f;
+    }
+    if (first_unstable) {
+        int fb = 0;
+        TS_CUDA(cudaMemcpy(&fb, s->first_bad, sizeof(int), cudaMemcpyDeviceToHost));
+        *first_unstable = fb == 0x7fffffff ? -1 : fb;
+    }
+    return TS_OK;
+}
+
+int ts_read(ts_sim *s, int32_t what, void *dst, size_t bytes) {
+    if (!s || !dst) return fail(TS_E_ARG, "null argument");
+    TS_CUDA(cudaSetDevice(s->device));
+    TS_CUDA(cudaEventSynchronize(s->done));
+    if (what == TS_TRACES) {
+        const size_t need = (size_t)s->n_rows * s->n_rec * sizeof(float);
+        if (bytes < need) return fail(TS_E_ARG, "destination too small for the traces");
+        if (need) TS_CUDA(cudaMemcpy(dst, s->traces, need, cudaMemcpyDeviceToHost));
+        s->d2h_bytes += (int64_t)need;
+        return TS_OK;
+    }
+    if (what < TS_VX || what > TS_SYZ || !s->field[what]) return fail(TS_E_ARG, "no such field");
+    const int last = s->dims == 2 ? s->ny : s->nz;
+    const size_t rows = (size_t)s->nx * (s->dims == 2 ? 1 : s->ny);
+    const size_t need = rows * last * sizeof(float);
+    if (bytes < need) return fail(TS_E_ARG, "destination too small for the field");
+    TS_CUDA(cudaMemcpy2D(dst, last * sizeof(float), s->field[what], s->pitch * sizeof(float), last * sizeof(float),
+                         rows, cudaMemcpyDeviceToHost));
+    s->d2h_bytes += (int64_t)need;
+    return TS_OK;
+}
+
+int ts_device_buffer(ts_sim *s, int32_t what, void **dev_ptr, size_t *pitch_bytes) {
+    if (!s || !dev_ptr) return fail(TS_E_ARG, "null argument");
+    if (what == TS_TRACES) {
+        *dev_ptr = s->traces;
+        if (pitch_bytes) *pitch_bytes = (size_t)s->n_rec * sizeof(float);
+        return TS_OK;
+    }
+    if (what < TS_VX || what > TS_SYZ || !s->field[what]) return fail(TS_E_ARG, "no such field");
+    *dev_ptr = s->field[what];
+    if (pitch_bytes) *pitch_bytes = (size_t)s->pitch * sizeof(float);
+    return TS_OK;
+}
+
+int ts_launches_per_step(const ts_sim *s, int32_t *launches) {
+    if (!s || !launches) return fail(TS_E_ARG, "null argument");
+    *launches = 2;
+    return TS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,112 @@
+// Internal device-side layout of the GB300 stepper (not part of the C ABI).
+//
+// HBM layout, per simulation:
+//  * every grid (fields, memory variables, per-cell coefficients) is stored
+//    C-order with the last axis padded to a multiple of 32 floats (`pitch`),
+//    so each warp row starts on a 128-byte boundary;
+//  * CPML convolution memories exist only inside the boundary strips: per
+//    axis the strip is a prefix [0, lo) and a suffix [hi, n) of grid
+//    indices (where any of the axis' a/b/k tables differs from the identity
+//    a = 0, b = 1, k = 1); outside it the reference's update is the identity
+//    (psi stays 0 and d/k + psi = d), so it is skipped;
+//  * per-cell coefficients are precomputed on the host from rho/cp/cs with
+//    the reference's averaging (lambda*dt, mu*dt per stress node, dt/rho per
+//    velocity node);
+//  * sources are a sparse point list binned by thread block; receivers a
+//    CSR list of grid offsets per receiver.
+#pragma once
+#include <cstdint>
+
+namespace ts {
+
+constexpr int kMaxOrd = 6;
+constexpr int kMaxSls = 8;
+
+// CPML coefficients of one node along one axis: a, b, 1/k.
+struct Cpml {
+    float a, b, ik, pad;
+};
+
+// Prefix/suffix strip of one axis: index `i` maps to compact `i` (i < lo)
+// or `i - hi + lo` (i >= hi), and is outside the strip otherwise.
+struct Strip {
+    int lo, hi, width;  // width = lo + (n - hi)
+};
+
+__host__ __device__ inline int strip_index(const Strip &s, int i) {
+    return i < s.lo ? i : (i >= s.hi ? i - s.hi + s.lo : -1);
+}
+
+// Zener constants in update form r' = A r + B d (global taus), or
+// r' = A r + (C g) d (per-cell scale g).
+struct Zener {
+    int n;
+    float Ap[kMaxSls], Bp[kMaxSls], As[kMaxSls], Bs[kMaxSls];
+};
+
+struct Source {
+    int64_t cell;   // flat padded offset
+    int col;        // column of the device source table
+    float scale;    // dt / rho at the node (the reference divides by rho)
+};
+
+// Everything a 2D or 3D kernel reads, passed by value.
+struct StepParams {
+    int family;
+    int nx, ny, nz;        // nz = 1 in 2D
+    int pitch;             // padded last-axis length (floats)
+    int64_t plane;         // ny * pitch (3D x stride); 2D: pitch
+    float cd[3][kMaxOrd];  // coef[c] / d_axis (x, y, z)
+
+    // fields
+    float *v[3];           // vx, vy, vz
+    float *s[6];           // sxx, syy, szz, sxy, sxz, syz
+
+    // CPML node tables indexed by grid index, full and half grid
+    const Cpml *tab_f[3], *tab_h[3];
+    Strip strip[3];
+    // strip memories: stress kernel psi of velocity derivatives and
+    // velocity kernel psi of stress derivatives (see ts_stepper*.cu)
+    float *psi[18];
+
+    // per-cell coefficients
+    const float *lam_dt, *mu_dt;          // normal node
+    const float *mus_dt[3];               // shear nodes xy, xz, yz (2D: xy)
+    const float *dtr[3];                  // dt / rho at vx, vy, vz nodes (0: no update)
+    const float *g_p, *g_s;               // per-cell attenuation scale (or null)
+    float *r[6];                          // memory variables, [n_sls] grids each
+    int64_t grid_elems;                   // elements of one padded grid
+    Zener zen;
+
+    // sources
+    const float *src_tab;  // [rows][src_ncol]
+    int src_rows, src_ncol;
+    const Source *src;     // sorted by block
+    const int *src_block_start;  // [n_blocks + 1]
+
+    // receivers
+    int n_rec;
+    const int *rec_start;  // [n_rec + 1]
+    const int64_t *rec_cell;
+    const int *rec_first_step;  // record at step k if k >= rec_first_step[s]
+    float *traces;              // [rows][n_rec]
+
+    // stability bookkeeping
+    float v2_threshold;     // a step is unstable when !(v2 <= threshold)
+    float *block_max;       // [n_blocks] running max of |v|^2
+    int *first_bad;         // min unstable step
+    const int *step_base;   // device step counter; step k = *step_base + j
+};
+
+// Launch helpers (defined per dimension).  `parts` selects the kernels of
+// one step: 1 = stress, 2 = velocity, 3 = both (in that order).
+void launch_step_2d(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st, int parts = 3);
+void launch_step_3d(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st, int parts = 3);
+void launch_reset_scalars(int *first_bad, int *step_base, cudaStream_t st);
+void launch_advance(int *step_base, int n, cudaStream_t st);
+int blocks_2d(const StepParams &p);
+int blocks_3d(const StepParams &p);
+constexpr int kBX2 = 32, kBY2 = 8;              // 2D block: 32 (y) x 8 (x)
+constexpr int kBX3 = 32, kBY3 = 4, kBZ3 = 2;    // 3D block: 32 (z) x 4 (y) x 2 (x)
+
+}  // namespace ts

@@ -1,0 +1,125 @@
+"""GPU parity: the CUDA stepper (through the C ABI) against the CPU oracle.
+
+The oracle restates the reference's kernels in IEEE float with the
+reference's operation order; the CUDA kernels fold divisions into
+reciprocals and contract to fma, so they agree to rounding.  Tolerance:
+relative L2 <= 1e-5 on fields and receiver traces (the bound the reference
+comparison uses), and the float error of each implementation is also
+measured against the oracle's double-precision run.
+"""
+import numpy as np
+import pytest
+
+from _cases import case_2d, case_3d, rel_l2
+from oracle import oracle
+from taichi_sim_gb300 import engine
+from taichi_sim_gb300.sim_support.simulator import Simulator
+from taichi_sim_gb300.sim_support.Simulator3D import Simulator3D
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+CASES_2D = {
+    "taichi_elastic": (lambda: case_2d(linear=False), engine.TAICHI2D),
+    "taichi_elastic_acc4": (lambda: case_2d(linear=False, acc=4), engine.TAICHI2D),
+    "wgsl_elastic": (lambda: case_2d(visco=0), engine.WGSL2D),
+    "wgsl_visco": (lambda: case_2d(visco=1), engine.WGSL2D),
+    "wgsl_visco_acc3": (lambda: case_2d(visco=1, acc=3, seed=3), engine.WGSL2D),
+    "wgsl_visco_acc6": (lambda: case_2d(visco=1, acc=6, seed=6), engine.WGSL2D),
+    "wgsl_visco_q": (lambda: case_2d(visco=1, q=(30.0, 200.0), seed=1), engine.WGSL2D),
+    "wgsl_delayed_rx": (lambda: case_2d(visco=1, t0_rx=0.2, seed=2), engine.WGSL2D),
+    "taichi_delayed_rx": (lambda: case_2d(linear=False, t0_rx=0.2, seed=2), engine.TAICHI2D),
+}
+
+CASES_3D = {
+    "wgsl3d_elastic": lambda: case_3d(visco=0),
+    "wgsl3d_visco": lambda: case_3d(visco=1),
+    "wgsl3d_visco_matrix_q": lambda: case_3d(visco=1, matrix=True, q=(30.0, 300.0), seed=4),
+    "wgsl3d_acc4": lambda: case_3d(visco=1, acc=4, seed=5, w=34, d=30, h=36),
+}
+
+
+def _compare(sim, family, names):
+    fam_oracle = {engine.TAICHI2D: oracle.TAICHI2D, engine.WGSL2D: oracle.WGSL2D, engine.WGSL3D: oracle.WGSL3D}[family]
+    ref = oracle.run(sim, fam_oracle)
+    ref64 = oracle.run(sim, fam_oracle, precision="f64")
+    with engine.Stepper(sim, family=family) as st:
+        st.run(sim._n_steps)
+        n, vmax, bad = st.status()
+        assert n == sim._n_steps and bad == -1
+        errs = {}
+        for name in names:
+            got = st.read(name)
+            errs[name] = rel_l2(got, ref[name])
+            assert errs[name] <= TOL, (name, errs[name])
+            # the GPU's float error is of the same order as the oracle's own
+            e_gpu, e_orc = rel_l2(got, ref64[name]), rel_l2(ref[name], ref64[name])
+            assert e_gpu <= max(10 * e_orc, 1e-6), (name, e_gpu, e_orc)
+        traces = st.read("traces")
+        errs["traces"] = rel_l2(traces, ref["sens"])
+        assert np.abs(ref["sens"]).max() > 0, "case records nothing"
+        assert errs["traces"] <= TOL, errs
+        # unrecorded (gated) samples stay exactly zero, as in the reference
+        np.testing.assert_array_equal(traces[ref["sens"] == 0] != 0, False)
+        assert np.isclose(vmax, ref["vmax2"].max(), rtol=1e-4)
+    return errs
+
+
+@pytest.mark.parametrize("name", sorted(CASES_2D))
+def test_parity_2d(name):
+    build, family = CASES_2D[name]
+    sim = Simulator(build())
+    _compare(sim, family, ["vx", "vy", "sxx", "syy", "sxy"])
+
+
+@pytest.mark.parametrize("name", sorted(CASES_3D))
+def test_parity_3d(name):
+    sim = Simulator3D(CASES_3D[name]())
+    _compare(sim, engine.WGSL3D, ["vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "sxz", "syz"])
+
+
+def test_chunked_equals_single_run():
+    """Steps split over many ts_run calls (graph and non-graph paths) give
+    bit-identical results to one call."""
+    sim = Simulator(case_2d(visco=1, steps=150))
+    with engine.Stepper(sim) as a, engine.Stepper(sim) as b:
+        a.run(150)
+        for k in (1, 32, 5, 64, 33, 15):
+            b.run(k)
+        for f in ("vx", "vy", "sxx", "syy", "sxy", "traces"):
+            np.testing.assert_array_equal(a.read(f), b.read(f))
+
+
+def test_reset_and_rerun_is_deterministic():
+    sim = Simulator3D(case_3d(steps=40))
+    with engine.Stepper(sim) as st:
+        st.run(40)
+        first = st.read("szz"), st.read("traces")
+        st.reset()
+        st.run(40)
+        np.testing.assert_array_equal(first[0], st.read("szz"))
+        np.testing.assert_array_equal(first[1], st.read("traces"))
+
+
+def test_backend_drop_in_run():
+    """The drop-in backend's implementation() returns the reference's keys."""
+    from taichi_sim_gb300.backends import SimulatorCudaElastic, SimulatorCudaViscoelastic
+    cfg = case_2d(visco=1, steps=60)
+    res = SimulatorCudaViscoelastic(cfg).implementation()
+    assert set(res) >= {"stress", "sens_stress", "gpu_str", "sim_time"}
+    assert res["stress"].shape == Simulator(cfg).grid_shape()
+    res = SimulatorCudaElastic(case_2d(linear=False, steps=60)).implementation()
+    assert set(res) >= {"pressure", "sens_pressure", "gpu_str", "sim_time"}
+
+
+def test_stability_error_raised():
+    """A Courant-violating time step (forced past the host check) blows up and
+    the stepper raises StabilityError, as the reference's loop does."""
+    from taichi_sim_gb300.sim_support import StabilityError
+    cfg = case_2d(visco=0, steps=400, maps=False)
+    sim = Simulator(cfg)
+    sim._dt = np.float32(sim._dt * 3.0)   # CFL ~ 1.5
+    with engine.Stepper(sim, family=engine.TAICHI2D) as st:
+        with pytest.raises(StabilityError):
+            st.simulate(check_every=50)
