@@ -5,6 +5,8 @@
 // CPML, Dirichlet zeroing, source injection, receiver sampling of szz and
 // stability bookkeeping fused).  Thread (tx, ty, tz) owns node
 // (z = 32 bx + tx, y = 4 by + ty, x = 2 bz + tz): z is the contiguous axis.
+// As in 2D, every load of a node is issued before its first store so that
+// one memory latency is paid per node.
 //
 // Semantics: family TS_WGSL3D, shader_webgpu_3D_viscoelastic.wgsl:1341-1773
 // and :1824-1843, including its quirks (normal stresses use point
@@ -17,190 +19,353 @@
 namespace ts {
 namespace {
 
-__device__ __forceinline__ float cpml_update(float d, float *psi, const Cpml &t) {
-    float p = fmaf(t.b, *psi, t.a * d);
-    *psi = p;
-    return fmaf(d, t.ik, p);
+__device__ __forceinline__ float cpml(float d, float psi_old, float &psi_new, const Cpml &t) {
+    psi_new = fmaf(t.b, psi_old, t.a * d);
+    return fmaf(d, t.ik, psi_new);
 }
 
-struct Idx3 {
-    int x, y, z;
-    int64_t i;
+// Stencil values of one staggered derivative: hi[c] - lo[c] pairs.
+// PLUS: f[i + (c+1) s] - f[i - c s]; otherwise f[i + c s] - f[i - (c+1) s].
+template <int ORD>
+struct Pairs {
+    float hi[ORD], lo[ORD];
 };
 
-__device__ __forceinline__ float *psi_x(const StepParams &p, int k, int sx, const Idx3 &n) {
-    return p.psi[k] + ((int64_t)sx * p.ny + n.y) * p.pitch + n.z;
-}
-__device__ __forceinline__ float *psi_y(const StepParams &p, int k, int sy, const Idx3 &n) {
-    return p.psi[k] + ((int64_t)n.x * p.strip[1].width + sy) * p.pitch + n.z;
-}
-__device__ __forceinline__ float *psi_z(const StepParams &p, int k, int sz, const Idx3 &n) {
-    return p.psi[k] + ((int64_t)n.x * p.ny + n.y) * p.strip[2].width + sz;
-}
-
-// x, y and z derivative (forward-staggered "plus" or backward "minus")
 template <int ORD, bool PLUS>
-__device__ __forceinline__ float dfd(const float *__restrict__ f, int64_t i, int64_t stride, const float *cd) {
-    float a = 0.f;
+__device__ __forceinline__ Pairs<ORD> load_pairs(const float *__restrict__ f, int64_t i, int64_t s) {
+    Pairs<ORD> r;
 #pragma unroll
     for (int c = 0; c < ORD; ++c) {
-        const float hi = __ldg(f + i + (PLUS ? (c + 1) : c) * stride);
-        const float lo = __ldg(f + i - (PLUS ? c : (c + 1)) * stride);
-        a = fmaf(cd[c], hi - lo, a);
+        r.hi[c] = __ldg(f + i + (PLUS ? (c + 1) : c) * s);
+        r.lo[c] = __ldg(f + i - (PLUS ? c : (c + 1)) * s);
     }
+    return r;
+}
+
+template <int ORD>
+__device__ __forceinline__ float deriv(const Pairs<ORD> &q, const float *cd) {
+    float a = 0.f;
+#pragma unroll
+    for (int c = 0; c < ORD; ++c) a = fmaf(cd[c], q.hi[c] - q.lo[c], a);
     return a;
 }
 
-template <int ZM>
-__device__ __forceinline__ float zener_sum(const StepParams &p, int which, int64_t i, float drive, bool p_wave,
-                                           float g) {
-    float s = 0.f;
-#pragma unroll
-    for (int l = 0; l < kMaxSls; ++l) {
-        if (l >= p.zen.n) break;
-        float *rr = p.r[which] + l * p.grid_elems + i;
-        const float o = *rr;
-        const float A = p_wave ? p.zen.Ap[l] : p.zen.As[l];
-        const float B = (p_wave ? p.zen.Bp[l] : p.zen.Bs[l]) * g;
-        const float n_ = fmaf(A, o, B * drive);
-        s += o + n_;
-        *rr = n_;
-    }
-    return s;
-}
-
-template <int ORD, int ZM>
+template <int ORD, int ZM, int NS>
 __global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_stress3d(const StepParams p) {
-    Idx3 n;
-    n.z = blockIdx.x * kBX3 + threadIdx.x;
-    n.y = blockIdx.y * kBY3 + threadIdx.y;
-    n.x = blockIdx.z * kBZ3 + threadIdx.z;
-    if (n.x >= p.nx || n.y >= p.ny || n.z >= p.nz) return;
+    const int z = blockIdx.x * kBX3 + threadIdx.x;
+    const int y = blockIdx.y * kBY3 + threadIdx.y;
+    const int x = blockIdx.z * kBZ3 + threadIdx.z;
+    const bool in_n = x >= ORD - 1 && x < p.nx - ORD && y >= ORD && y < p.ny - ORD + 1 && z >= ORD && z < p.nz - ORD + 1;
+    const bool in_xy = x >= ORD && x < p.nx - ORD + 1 && y >= ORD - 1 && y < p.ny - ORD && z >= ORD - 1 && z < p.nz - ORD;
+    const bool in_yz = x >= ORD - 1 && x < p.nx - ORD && y >= ORD - 1 && y < p.ny - ORD && z >= ORD - 1 && z < p.nz - ORD;
+    if (!in_n && !in_xy && !in_yz) return;
     const int64_t X = p.plane, Y = p.pitch;
-    n.i = n.x * X + n.y * Y + n.z;
-    const int64_t i = n.i;
-    const int x = n.x, y = n.y, z = n.z;
+    const int64_t i = (int64_t)x * X + y * Y + z;
     const float *vx = p.v[0], *vy = p.v[1], *vz = p.v[2];
     const int sx = strip_index(p.strip[0], x), sy = strip_index(p.strip[1], y), sz = strip_index(p.strip[2], z);
-    const float gs = ZM == 2 ? __ldg(p.g_s + i) : 1.f;
+    const int64_t ix = ((int64_t)sx * p.ny + y) * p.pitch + z;
+    const int64_t iy = ((int64_t)x * p.strip[1].width + sy) * p.pitch + z;
+    const int64_t iz = ((int64_t)x * p.ny + y) * p.strip[2].width + sz;
+    const int n_mech = NS == 3 ? 3 : p.zen.n;
+    const int64_t G = p.grid_elems;
+    constexpr int R = NS > 0 ? NS : 1;
 
-    // ---- normal stresses ----
-    if (x >= ORD - 1 && x < p.nx - ORD && y >= ORD && y < p.ny - ORD + 1 && z >= ORD && z < p.nz - ORD + 1) {
-        float ddx = dfd<ORD, true>(vx, i, X, p.cd[0]);
-        float ddy = dfd<ORD, false>(vy, i, Y, p.cd[1]);
-        float ddz = dfd<ORD, false>(vz, i, 1, p.cd[2]);
-        if (sx >= 0) ddx = cpml_update(ddx, psi_x(p, 0, sx, n), p.tab_h[0][x]);
-        if (sy >= 0) ddy = cpml_update(ddy, psi_y(p, 1, sy, n), p.tab_f[1][y]);
-        if (sz >= 0) ddz = cpml_update(ddz, psi_z(p, 2, sz, n), p.tab_f[2][z]);
-        const float L = __ldg(p.lam_dt + i), M = __ldg(p.mu_dt + i);
+    // ---------------- loads ----------------
+    Pairs<ORD> n_x, n_y, n_z, a_vy, a_vx, b_vz, b_vx, c_vz, c_vy;
+    float s_n[3] = {0.f, 0.f, 0.f}, L = 0.f, M = 0.f, gp = 1.f, gs = 1.f;
+    float s_xy = 0.f, s_xz = 0.f, s_yz = 0.f, Mxy = 0.f, Mxz = 0.f, Myz = 0.f;
+    float psi[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float r0[R], r1[R], r2[R], r3[R], r4[R], r5[R];
+    if (in_n) {
+        n_x = load_pairs<ORD, true>(vx, i, X);
+        n_y = load_pairs<ORD, false>(vy, i, Y);
+        n_z = load_pairs<ORD, false>(vz, i, 1);
+        s_n[0] = p.s[0][i];
+        s_n[1] = p.s[1][i];
+        s_n[2] = p.s[2][i];
+        L = __ldg(p.lam_dt + i);
+        M = __ldg(p.mu_dt + i);
+        if (sx >= 0) psi[0] = p.psi[0][ix];
+        if (sy >= 0) psi[1] = p.psi[1][iy];
+        if (sz >= 0) psi[2] = p.psi[2][iz];
+        if (ZM == 2) gp = __ldg(p.g_p + i);
+        if (ZM != 0) {
+#pragma unroll
+            for (int l = 0; l < R; ++l)
+                if (l < n_mech) {
+                    r0[l] = p.r[0][l * G + i];
+                    r1[l] = p.r[1][l * G + i];
+                    r2[l] = p.r[2][l * G + i];
+                }
+        }
+    }
+    if (in_xy) {
+        a_vy = load_pairs<ORD, false>(vy, i, X);
+        a_vx = load_pairs<ORD, true>(vx, i, Y);
+        b_vz = load_pairs<ORD, false>(vz, i, X);
+        b_vx = load_pairs<ORD, true>(vx, i, 1);
+        s_xy = p.s[3][i];
+        s_xz = p.s[4][i];
+        Mxy = __ldg(p.mus_dt[0] + i);
+        Mxz = __ldg(p.mus_dt[1] + i);
+        if (sx >= 0) {
+            psi[3] = p.psi[3][ix];
+            psi[5] = p.psi[5][ix];
+        }
+        if (sy >= 0) psi[4] = p.psi[4][iy];
+        if (sz >= 0) psi[6] = p.psi[6][iz];
+        if (ZM != 0) {
+#pragma unroll
+            for (int l = 0; l < R; ++l)
+                if (l < n_mech) {
+                    r3[l] = p.r[3][l * G + i];
+                    r4[l] = p.r[4][l * G + i];
+                }
+        }
+    }
+    if (in_yz) {
+        c_vz = load_pairs<ORD, true>(vz, i, Y);
+        c_vy = load_pairs<ORD, true>(vy, i, 1);
+        s_yz = p.s[5][i];
+        Myz = __ldg(p.mus_dt[2] + i);
+        if (sy >= 0) psi[7] = p.psi[7][iy];
+        if (sz >= 0) psi[8] = p.psi[8][iz];
+        if (ZM != 0) {
+#pragma unroll
+            for (int l = 0; l < R; ++l)
+                if (l < n_mech) r5[l] = p.r[5][l * G + i];
+        }
+    }
+    if (ZM == 2) gs = __ldg(p.g_s + i);
+
+    // ---------------- normal stresses ----------------
+    if (in_n) {
+        float ddx = deriv(n_x, p.cd[0]), ddy = deriv(n_y, p.cd[1]), ddz = deriv(n_z, p.cd[2]);
+        float np_;
+        if (sx >= 0) {
+            ddx = cpml(ddx, psi[0], np_, p.tab_h[0][x]);
+            p.psi[0][ix] = np_;
+        }
+        if (sy >= 0) {
+            ddy = cpml(ddy, psi[1], np_, p.tab_f[1][y]);
+            p.psi[1][iy] = np_;
+        }
+        if (sz >= 0) {
+            ddz = cpml(ddz, psi[2], np_, p.tab_f[2][z]);
+            p.psi[2][iz] = np_;
+        }
         const float L2M = fmaf(2.f, M, L);
         float ux = fmaf(L2M, ddx, L * (ddy + ddz));
         float uy = fmaf(L2M, ddy, L * (ddx + ddz));
         float uz = fmaf(L2M, ddz, L * (ddx + ddy));
         if (ZM != 0) {
-            const float gp = ZM == 2 ? __ldg(p.g_p + i) : 1.f;
             const float div = ddx + ddy + ddz;
             const float third = div * (1.f / 3.f);
-            const float srxx = zener_sum<ZM>(p, 0, i, div, true, gp);
-            const float sryy = zener_sum<ZM>(p, 1, i, ddx - third, false, gs);
-            const float srzz = zener_sum<ZM>(p, 2, i, ddy - third, false, gs);
+            const float dy_ = ddx - third, dz_ = ddy - third;
+            float srxx = 0.f, sryy = 0.f, srzz = 0.f;
+#pragma unroll
+            for (int l = 0; l < R; ++l)
+                if (l < n_mech) {
+                    const float a = fmaf(p.zen.Ap[l], r0[l], (p.zen.Bp[l] * gp) * div);
+                    const float b = fmaf(p.zen.As[l], r1[l], (p.zen.Bs[l] * gs) * dy_);
+                    const float c = fmaf(p.zen.As[l], r2[l], (p.zen.Bs[l] * gs) * dz_);
+                    srxx += r0[l] + a;
+                    sryy += r1[l] + b;
+                    srzz += r2[l] + c;
+                    p.r[0][l * G + i] = a;
+                    p.r[1][l * G + i] = b;
+                    p.r[2][l * G + i] = c;
+                }
             const float hl23 = 0.5f * fmaf(2.f / 3.f, M, L);
             ux = fmaf(hl23, srxx, fmaf(M, sryy, ux));
             uy = fmaf(hl23, srxx, fmaf(M, srzz, uy));
             uz = fmaf(0.5f * L2M, srxx, fmaf(-M * (1.f / 3.f), sryy + srzz, uz));
         }
-        p.s[0][i] += ux;
-        p.s[1][i] += uy;
-        p.s[2][i] += uz;
+        p.s[0][i] = s_n[0] + ux;
+        p.s[1][i] = s_n[1] + uy;
+        p.s[2][i] = s_n[2] + uz;
     }
-    // ---- sigma_xy and sigma_xz: x in [ORD, nx-ORD+1), y, z in [ORD-1, n-ORD) ----
-    if (x >= ORD && x < p.nx - ORD + 1 && y >= ORD - 1 && y < p.ny - ORD && z >= ORD - 1 && z < p.nz - ORD) {
-        float a1 = dfd<ORD, false>(vy, i, X, p.cd[0]);
-        float a2 = dfd<ORD, true>(vx, i, Y, p.cd[1]);
-        if (sx >= 0) a1 = cpml_update(a1, psi_x(p, 3, sx, n), p.tab_f[0][x]);
-        if (sy >= 0) a2 = cpml_update(a2, psi_y(p, 4, sy, n), p.tab_h[1][y]);
-        const float Mxy = __ldg(p.mus_dt[0] + i);
-        float u = Mxy * (a1 + a2);
-        if (ZM != 0) u = fmaf(0.5f * Mxy, zener_sum<ZM>(p, 3, i, a1 + a2, false, gs), u);
-        p.s[3][i] += u;
-
-        float b1 = dfd<ORD, false>(vz, i, X, p.cd[0]);
-        float b2 = dfd<ORD, true>(vx, i, 1, p.cd[2]);
-        if (sx >= 0) b1 = cpml_update(b1, psi_x(p, 5, sx, n), p.tab_f[0][x]);
-        if (sz >= 0) b2 = cpml_update(b2, psi_z(p, 6, sz, n), p.tab_h[2][z]);
-        const float Mxz = __ldg(p.mus_dt[1] + i);
-        float w = Mxz * (b1 + b2);
-        if (ZM != 0) w = fmaf(0.5f * Mxz, zener_sum<ZM>(p, 4, i, b1 + b2, false, gs), w);
-        p.s[4][i] += w;
+    // ---------------- sigma_xy, sigma_xz ----------------
+    if (in_xy) {
+        float a1 = deriv(a_vy, p.cd[0]), a2 = deriv(a_vx, p.cd[1]);
+        float b1 = deriv(b_vz, p.cd[0]), b2 = deriv(b_vx, p.cd[2]);
+        float np_;
+        if (sx >= 0) {
+            a1 = cpml(a1, psi[3], np_, p.tab_f[0][x]);
+            p.psi[3][ix] = np_;
+            b1 = cpml(b1, psi[5], np_, p.tab_f[0][x]);
+            p.psi[5][ix] = np_;
+        }
+        if (sy >= 0) {
+            a2 = cpml(a2, psi[4], np_, p.tab_h[1][y]);
+            p.psi[4][iy] = np_;
+        }
+        if (sz >= 0) {
+            b2 = cpml(b2, psi[6], np_, p.tab_h[2][z]);
+            p.psi[6][iz] = np_;
+        }
+        const float ea = a1 + a2, eb = b1 + b2;
+        float u = Mxy * ea, w = Mxz * eb;
+        if (ZM != 0) {
+            float sa = 0.f, sb = 0.f;
+#pragma unroll
+            for (int l = 0; l < R; ++l)
+                if (l < n_mech) {
+                    const float na = fmaf(p.zen.As[l], r3[l], (p.zen.Bs[l] * gs) * ea);
+                    const float nb = fmaf(p.zen.As[l], r4[l], (p.zen.Bs[l] * gs) * eb);
+                    sa += r3[l] + na;
+                    sb += r4[l] + nb;
+                    p.r[3][l * G + i] = na;
+                    p.r[4][l * G + i] = nb;
+                }
+            u = fmaf(0.5f * Mxy, sa, u);
+            w = fmaf(0.5f * Mxz, sb, w);
+        }
+        p.s[3][i] = s_xy + u;
+        p.s[4][i] = s_xz + w;
     }
-    // ---- sigma_yz: x, y, z in [ORD-1, n-ORD) ----
-    if (x >= ORD - 1 && x < p.nx - ORD && y >= ORD - 1 && y < p.ny - ORD && z >= ORD - 1 && z < p.nz - ORD) {
-        float a1 = dfd<ORD, true>(vz, i, Y, p.cd[1]);
-        float a2 = dfd<ORD, true>(vy, i, 1, p.cd[2]);
-        if (sy >= 0) a1 = cpml_update(a1, psi_y(p, 7, sy, n), p.tab_h[1][y]);
-        if (sz >= 0) a2 = cpml_update(a2, psi_z(p, 8, sz, n), p.tab_h[2][z]);
-        const float Myz = __ldg(p.mus_dt[2] + i);
-        float u = Myz * (a1 + a2);
-        if (ZM != 0) u = fmaf(0.5f * Myz, zener_sum<ZM>(p, 5, i, a1 + a2, false, gs), u);
-        p.s[5][i] += u;
+    // ---------------- sigma_yz ----------------
+    if (in_yz) {
+        float a1 = deriv(c_vz, p.cd[1]), a2 = deriv(c_vy, p.cd[2]);
+        float np_;
+        if (sy >= 0) {
+            a1 = cpml(a1, psi[7], np_, p.tab_h[1][y]);
+            p.psi[7][iy] = np_;
+        }
+        if (sz >= 0) {
+            a2 = cpml(a2, psi[8], np_, p.tab_h[2][z]);
+            p.psi[8][iz] = np_;
+        }
+        const float e = a1 + a2;
+        float u = Myz * e;
+        if (ZM != 0) {
+            float sr = 0.f;
+#pragma unroll
+            for (int l = 0; l < R; ++l)
+                if (l < n_mech) {
+                    const float n_ = fmaf(p.zen.As[l], r5[l], (p.zen.Bs[l] * gs) * e);
+                    sr += r5[l] + n_;
+                    p.r[5][l * G + i] = n_;
+                }
+            u = fmaf(0.5f * Myz, sr, u);
+        }
+        p.s[5][i] = s_yz + u;
     }
 }
 
 template <int ORD>
 __global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_velocity3d(const StepParams p, const int j) {
-    Idx3 n;
-    n.z = blockIdx.x * kBX3 + threadIdx.x;
-    n.y = blockIdx.y * kBY3 + threadIdx.y;
-    n.x = blockIdx.z * kBZ3 + threadIdx.z;
+    const int z = blockIdx.x * kBX3 + threadIdx.x;
+    const int y = blockIdx.y * kBY3 + threadIdx.y;
+    const int x = blockIdx.z * kBZ3 + threadIdx.z;
     const int tid = (threadIdx.z * kBY3 + threadIdx.y) * kBX3 + threadIdx.x;
     const int blk = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
     const int k = *p.step_base + j;
-    const bool live = n.x < p.nx && n.y < p.ny && n.z < p.nz;
+    const bool live = x < p.nx && y < p.ny && z < p.nz;
     const int64_t X = p.plane, Y = p.pitch;
-    n.i = (int64_t)n.x * X + n.y * Y + n.z;
-    const int64_t i = n.i;
-    const int x = n.x, y = n.y, z = n.z;
-    float v2 = 0.f;
+    const int64_t i = (int64_t)x * X + y * Y + z;
+    const float *sxx = p.s[0], *syy = p.s[1], *szz = p.s[2], *sxy = p.s[3], *sxz = p.s[4], *syz = p.s[5];
+    const int sx = strip_index(p.strip[0], x), sy = strip_index(p.strip[1], y), sz = strip_index(p.strip[2], z);
+    const int64_t ix = ((int64_t)sx * p.ny + y) * p.pitch + z;
+    const int64_t iy = ((int64_t)x * p.strip[1].width + sy) * p.pitch + z;
+    const int64_t iz = ((int64_t)x * p.ny + y) * p.strip[2].width + sz;
+    // vz region; outside it all three components are zero (wgsl:1754-1758)
+    const bool in_vz = live && x >= ORD - 1 && x < p.nx - ORD && y >= ORD && y < p.ny - ORD + 1 && z >= ORD - 1 &&
+                       z < p.nz - ORD;
+    const bool in_vx = in_vz && x >= ORD && z >= ORD;        // vx region within the vz region
+    const bool in_vy = in_vz && y < p.ny - ORD && z >= ORD;  // vy region within the vz region
+    const int q0 = __ldg(p.src_block_start + blk), q1 = __ldg(p.src_block_start + blk + 1);
 
+    // ---------------- loads ----------------
+    Pairs<ORD> xa, xb, xe, ya, yb, ye, za, zb, ze;
+    float v0[3] = {0.f, 0.f, 0.f}, dtx = 0.f, dty = 0.f;
+    float psi[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (in_vx) {
+        xa = load_pairs<ORD, false>(sxx, i, X);
+        xb = load_pairs<ORD, false>(sxy, i, Y);
+        xe = load_pairs<ORD, false>(sxz, i, 1);
+        v0[0] = p.v[0][i];
+        dtx = __ldg(p.dtr[0] + i);
+        if (sx >= 0) psi[0] = p.psi[9][ix];
+        if (sy >= 0) psi[1] = p.psi[10][iy];
+        if (sz >= 0) psi[2] = p.psi[11][iz];
+    }
+    if (in_vy) {
+        ya = load_pairs<ORD, true>(sxy, i, X);
+        yb = load_pairs<ORD, true>(syy, i, Y);
+        ye = load_pairs<ORD, false>(syz, i, 1);
+        v0[1] = p.v[1][i];
+        if (sx >= 0) psi[3] = p.psi[12][ix];
+        if (sy >= 0) psi[4] = p.psi[13][iy];
+        if (sz >= 0) psi[5] = p.psi[14][iz];
+    }
+    if (in_vz) {
+        za = load_pairs<ORD, true>(sxz, i, X);
+        zb = load_pairs<ORD, false>(syz, i, Y);
+        ze = load_pairs<ORD, true>(szz, i, 1);
+        v0[2] = p.v[2][i];
+        dty = __ldg(p.dtr[1] + i);
+        if (sx >= 0) psi[6] = p.psi[15][ix];
+        if (sy >= 0) psi[7] = p.psi[16][iy];
+        if (sz >= 0) psi[8] = p.psi[17][iz];
+    }
+
+    // ---------------- update ----------------
+    float v2 = 0.f;
     if (live) {
-        const float *sxx = p.s[0], *syy = p.s[1], *szz = p.s[2], *sxy = p.s[3], *sxz = p.s[4], *syz = p.s[5];
-        const int sx = strip_index(p.strip[0], x), sy = strip_index(p.strip[1], y), sz = strip_index(p.strip[2], z);
-        // vz region; outside it all three components are zero (wgsl:1754-1758)
-        const bool in_vz = x >= ORD - 1 && x < p.nx - ORD && y >= ORD && y < p.ny - ORD + 1 && z >= ORD - 1 &&
-                           z < p.nz - ORD;
-        float vxn = 0.f, vyn = 0.f, vzn = 0.f;
-        if (in_vz) {
-            const float dtr_y = __ldg(p.dtr[1] + i);
-            if (x >= ORD && z >= ORD) {  // vx region within the vz region
-                float a = dfd<ORD, false>(sxx, i, X, p.cd[0]);
-                float b = dfd<ORD, false>(sxy, i, Y, p.cd[1]);
-                float e = dfd<ORD, false>(sxz, i, 1, p.cd[2]);
-                if (sx >= 0) a = cpml_update(a, psi_x(p, 9, sx, n), p.tab_f[0][x]);
-                if (sy >= 0) b = cpml_update(b, psi_y(p, 10, sy, n), p.tab_f[1][y]);
-                if (sz >= 0) e = cpml_update(e, psi_z(p, 11, sz, n), p.tab_f[2][z]);
-                vxn = fmaf(a + b + e, __ldg(p.dtr[0] + i), p.v[0][i]);
+        float vxn = 0.f, vyn = 0.f, vzn = 0.f, np_;
+        if (in_vx) {
+            float a = deriv(xa, p.cd[0]), b = deriv(xb, p.cd[1]), e = deriv(xe, p.cd[2]);
+            if (sx >= 0) {
+                a = cpml(a, psi[0], np_, p.tab_f[0][x]);
+                p.psi[9][ix] = np_;
             }
-            if (y < p.ny - ORD && z >= ORD) {  // vy region within the vz region
-                float a = dfd<ORD, true>(sxy, i, X, p.cd[0]);
-                float b = dfd<ORD, true>(syy, i, Y, p.cd[1]);
-                float e = dfd<ORD, false>(syz, i, 1, p.cd[2]);
-                if (sx >= 0) a = cpml_update(a, psi_x(p, 12, sx, n), p.tab_h[0][x]);
-                if (sy >= 0) b = cpml_update(b, psi_y(p, 13, sy, n), p.tab_h[1][y]);
-                if (sz >= 0) e = cpml_update(e, psi_z(p, 14, sz, n), p.tab_f[2][z]);
-                vyn = fmaf(a + b + e, dtr_y, p.v[1][i]);
+            if (sy >= 0) {
+                b = cpml(b, psi[1], np_, p.tab_f[1][y]);
+                p.psi[10][iy] = np_;
             }
-            float a = dfd<ORD, true>(sxz, i, X, p.cd[0]);
-            float b = dfd<ORD, false>(syz, i, Y, p.cd[1]);
-            float e = dfd<ORD, true>(szz, i, 1, p.cd[2]);
-            if (sx >= 0) a = cpml_update(a, psi_x(p, 15, sx, n), p.tab_h[0][x]);
-            if (sy >= 0) b = cpml_update(b, psi_y(p, 16, sy, n), p.tab_f[1][y]);
-            if (sz >= 0) e = cpml_update(e, psi_z(p, 17, sz, n), p.tab_h[2][z]);
-            vzn = fmaf(a + b + e, dtr_y, p.v[2][i]);
+            if (sz >= 0) {
+                e = cpml(e, psi[2], np_, p.tab_f[2][z]);
+                p.psi[11][iz] = np_;
+            }
+            vxn = fmaf(a + b + e, dtx, v0[0]);
         }
-        const int q0 = __ldg(p.src_block_start + blk), q1 = __ldg(p.src_block_start + blk + 1);
+        if (in_vy) {
+            float a = deriv(ya, p.cd[0]), b = deriv(yb, p.cd[1]), e = deriv(ye, p.cd[2]);
+            if (sx >= 0) {
+                a = cpml(a, psi[3], np_, p.tab_h[0][x]);
+                p.psi[12][ix] = np_;
+            }
+            if (sy >= 0) {
+                b = cpml(b, psi[4], np_, p.tab_h[1][y]);
+                p.psi[13][iy] = np_;
+            }
+            if (sz >= 0) {
+                e = cpml(e, psi[5], np_, p.tab_f[2][z]);
+                p.psi[14][iz] = np_;
+            }
+            vyn = fmaf(a + b + e, dty, v0[1]);
+        }
+        if (in_vz) {
+            float a = deriv(za, p.cd[0]), b = deriv(zb, p.cd[1]), e = deriv(ze, p.cd[2]);
+            if (sx >= 0) {
+                a = cpml(a, psi[6], np_, p.tab_h[0][x]);
+                p.psi[15][ix] = np_;
+            }
+            if (sy >= 0) {
+                b = cpml(b, psi[7], np_, p.tab_f[1][y]);
+                p.psi[16][iy] = np_;
+            }
+            if (sz >= 0) {
+                e = cpml(e, psi[8], np_, p.tab_h[2][z]);
+                p.psi[17][iz] = np_;
+            }
+            vzn = fmaf(a + b + e, dty, v0[2]);  // the vy-node density (wgsl3d:1748)
+        }
         for (int q = q0; q < q1; ++q) {
             const Source s = p.src[q];
-            if (s.cell == i && k < p.src_rows) vzn = fmaf(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), s.scale, vzn);
+            if (s.cell == i && k < p.src_rows)
+                vzn = fmaf(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), s.scale, vzn);
         }
         p.v[0][i] = vxn;
         p.v[1][i] = vyn;
@@ -216,7 +381,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_velocity3d(const StepParam
     }
 
     const bool bad = live && !(v2 <= p.v2_threshold);
-    unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(v2));
+    const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(v2));
     __shared__ unsigned wmax[kBX3 * kBY3 * kBZ3 / 32];
     if ((tid & 31) == 0) wmax[tid >> 5] = m;
     const int any_bad = __syncthreads_or(bad);
@@ -224,8 +389,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_velocity3d(const StepParam
         unsigned bm = wmax[0];
 #pragma unroll
         for (int w = 1; w < kBX3 * kBY3 * kBZ3 / 32; ++w) bm = max(bm, wmax[w]);
-        unsigned *slot = reinterpret_cast<unsigned *>(p.block_max) + blk;
-        *slot = max(*slot, bm);
+        atomicMax(reinterpret_cast<unsigned *>(p.block_max) + blk, bm);
         if (any_bad) atomicMin(p.first_bad, k);
     }
 }
@@ -234,10 +398,13 @@ template <int ORD>
 void launch_ord(const StepParams &p, int zen_mode, int j, cudaStream_t st, int parts) {
     dim3 block(kBX3, kBY3, kBZ3);
     dim3 grid((p.nz + kBX3 - 1) / kBX3, (p.ny + kBY3 - 1) / kBY3, (p.nx + kBZ3 - 1) / kBZ3);
+    const bool three = p.zen.n == 3;
     if (parts & 1) {
-        if (zen_mode == 0) k_stress3d<ORD, 0><<<grid, block, 0, st>>>(p);
-        else if (zen_mode == 1) k_stress3d<ORD, 1><<<grid, block, 0, st>>>(p);
-        else k_stress3d<ORD, 2><<<grid, block, 0, st>>>(p);
+        if (zen_mode == 0) k_stress3d<ORD, 0, 0><<<grid, block, 0, st>>>(p);
+        else if (zen_mode == 1 && three) k_stress3d<ORD, 1, 3><<<grid, block, 0, st>>>(p);
+        else if (zen_mode == 1) k_stress3d<ORD, 1, kMaxSls><<<grid, block, 0, st>>>(p);
+        else if (three) k_stress3d<ORD, 2, 3><<<grid, block, 0, st>>>(p);
+        else k_stress3d<ORD, 2, kMaxSls><<<grid, block, 0, st>>>(p);
     }
     if (parts & 2) k_velocity3d<ORD><<<grid, block, 0, st>>>(p, j);
 }
