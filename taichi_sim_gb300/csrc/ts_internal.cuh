@@ -98,6 +98,41 @@ struct StepParams {
     const int *step_base;   // device step counter; step k = *step_base + j
 };
 
+// Programmatic dependent launch: a step kernel may be scheduled while the
+// previous kernel of the stream drains.  Before the wait it may only read
+// data no earlier kernel writes (coefficients, tables); after it, all
+// writes of the previous kernels are visible.  The trigger lets the next
+// kernel's launch start once every block of this one has issued it.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Stability bookkeeping of one warp: max |v|^2 into the block's slot and the
+// first unstable step, both as reductions the warp does not wait for.
+__device__ __forceinline__ void warp_stability(float v2, bool bad, unsigned *block_slot, int *first_bad, int k) {
+    const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(v2));
+    const unsigned any_bad = __ballot_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(block_slot, m);
+        if (any_bad) atomicMin(first_bad, k);
+    }
+}
+
+// Launch a step kernel with programmatic stream serialisation (see above).
+template <typename... Params, typename... Args>
+inline void launch_pdl(void (*kern)(Params...), dim3 grid, dim3 block, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 // Launch helpers (defined per dimension).  `parts` selects the kernels of
 // one step: 1 = stress, 2 = velocity, 3 = both (in that order).
 void launch_step_2d(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st, int parts = 3);

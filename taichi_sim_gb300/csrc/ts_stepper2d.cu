@@ -56,8 +56,19 @@ __global__ void __launch_bounds__(kBX2 *kBY2) k_stress2d(const StepParams p) {
     const int64_t ix = (int64_t)sx * P + y, iy = (int64_t)x * p.strip[1].width + sy;
 
     // ---------------- loads ----------------
+    // per-node coefficients: no kernel writes them, so they are read before
+    // waiting for the previous kernel
+    float L = 0.f, M = 0.f, Ms = 0.f, gp = 1.f, gs = 1.f;
+    if (in_n) {
+        L = ldg(p.lam_dt + i);
+        M = ldg(p.mu_dt + i);
+        if (ZM == 2) gp = ldg(p.g_p + i);
+    }
+    if (in_s) Ms = ldg(p.mus_dt[0] + i);
+    if (ZM == 2) gs = ldg(p.g_s + i);
+    pdl_wait();
     float nvx[ORD][2], nvy[ORD][2], svy[ORD][2], svx[ORD][2];
-    float sxx = 0.f, syy = 0.f, L = 0.f, M = 0.f, sxy = 0.f, Ms = 0.f, gp = 1.f, gs = 1.f;
+    float sxx = 0.f, syy = 0.f, sxy = 0.f;
     float rxx[NS > 0 ? NS : 1], ryy[NS > 0 ? NS : 1], rxy[NS > 0 ? NS : 1];
     float psi_n[2] = {0.f, 0.f}, psi_s[2] = {0.f, 0.f};
     if (in_n) {
@@ -70,12 +81,9 @@ __global__ void __launch_bounds__(kBX2 *kBY2) k_stress2d(const StepParams p) {
         }
         sxx = p.s[0][i];
         syy = p.s[1][i];
-        L = ldg(p.lam_dt + i);
-        M = ldg(p.mu_dt + i);
         if (sx >= 0) psi_n[0] = p.psi[0][ix];
         if (sy >= 0) psi_n[1] = p.psi[2][iy];
         if (ZM != 0) {
-            if (ZM == 2) gp = ldg(p.g_p + i);
 #pragma unroll
             for (int l = 0; l < NS; ++l)
                 if (l < n_mech) {
@@ -93,7 +101,6 @@ __global__ void __launch_bounds__(kBX2 *kBY2) k_stress2d(const StepParams p) {
             svx[c][1] = ldg(vx + i - c);
         }
         sxy = p.s[3][i];
-        Ms = ldg(p.mus_dt[0] + i);
         if (sx >= 0) psi_s[0] = p.psi[1][ix];
         if (sy >= 0) psi_s[1] = p.psi[3][iy];
         if (ZM != 0) {
@@ -102,7 +109,6 @@ __global__ void __launch_bounds__(kBX2 *kBY2) k_stress2d(const StepParams p) {
                 if (l < n_mech) rxy[l] = p.r[2][l * p.grid_elems + i];
         }
     }
-    if (ZM == 2) gs = ldg(p.g_s + i);
 
     // ---------------- normal stresses ----------------
     if (in_n) {
@@ -187,6 +193,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2) k_stress2d(const StepParams p) {
         }
         p.s[3][i] = sxy + u;
     }
+    pdl_trigger();
 }
 
 template <int ORD, int FAM>
@@ -195,7 +202,6 @@ __global__ void __launch_bounds__(kBX2 *kBY2) k_velocity2d(const StepParams p, c
     const int x = blockIdx.y * kBY2 + threadIdx.y;
     const int tid = threadIdx.y * kBX2 + threadIdx.x;
     const int blk = blockIdx.y * gridDim.x + blockIdx.x;
-    const int k = *p.step_base + j;
     const bool live = x < p.nx && y < p.ny;
     const int P = p.pitch;
     const int64_t i = (int64_t)x * P + y;
@@ -210,10 +216,14 @@ __global__ void __launch_bounds__(kBX2 *kBY2) k_velocity2d(const StepParams p, c
     const int sx = strip_index(p.strip[0], x), sy = strip_index(p.strip[1], y);
     const int64_t ix = (int64_t)sx * P + y, iy = (int64_t)x * p.strip[1].width + sy;
     const int q0 = __ldg(p.src_block_start + blk), q1 = __ldg(p.src_block_start + blk + 1);
+    const float dx0 = in_vx ? ldg(p.dtr[0] + i) : 0.f;
+    const float dy0 = in_vy ? ldg(p.dtr[1] + i) : 0.f;
+    pdl_wait();
+    const int k = *p.step_base + j;
 
     // ---------------- loads ----------------
     float ax[ORD][2], bx[ORD][2], ay[ORD][2], by[ORD][2];
-    float vx0 = 0.f, vy0 = 0.f, dx0 = 0.f, dy0 = 0.f;
+    float vx0 = 0.f, vy0 = 0.f;
     float pxa = 0.f, pxb = 0.f, pya = 0.f, pyb = 0.f;
     if (in_vx) {
 #pragma unroll
@@ -224,7 +234,6 @@ __global__ void __launch_bounds__(kBX2 *kBY2) k_velocity2d(const StepParams p, c
             bx[c][1] = ldg(sxy + i - c - 1);
         }
         vx0 = p.v[0][i];
-        dx0 = ldg(p.dtr[0] + i);
         if (sx >= 0) pxa = p.psi[4][ix];
         if (sy >= 0) pxb = p.psi[6][iy];
     }
@@ -237,7 +246,6 @@ __global__ void __launch_bounds__(kBX2 *kBY2) k_velocity2d(const StepParams p, c
             by[c][1] = ldg(syy + i - c);
         }
         vy0 = p.v[1][i];
-        dy0 = ldg(p.dtr[1] + i);
         if (sx >= 0) pya = p.psi[5][ix];
         if (sy >= 0) pyb = p.psi[7][iy];
     }
@@ -303,20 +311,9 @@ __global__ void __launch_bounds__(kBX2 *kBY2) k_velocity2d(const StepParams p, c
         p.traces[(int64_t)k * p.n_rec + g] = acc;
     }
 
-    // stability bookkeeping: block max of |v|^2 (a reduction the issuing
-    // thread does not wait for) and the first unstable step
-    const bool bad = live && !(v2 <= p.v2_threshold);
-    const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(v2));
-    __shared__ unsigned wmax[kBX2 * kBY2 / 32];
-    if ((tid & 31) == 0) wmax[tid >> 5] = m;
-    const int any_bad = __syncthreads_or(bad);
-    if (tid == 0) {
-        unsigned bm = wmax[0];
-#pragma unroll
-        for (int w = 1; w < kBX2 * kBY2 / 32; ++w) bm = max(bm, wmax[w]);
-        atomicMax(reinterpret_cast<unsigned *>(p.block_max) + blk, bm);
-        if (any_bad) atomicMin(p.first_bad, k);
-    }
+    warp_stability(v2, live && !(v2 <= p.v2_threshold), reinterpret_cast<unsigned *>(p.block_max) + blk,
+                   p.first_bad, k);
+    pdl_trigger();
 }
 
 template <int ORD>
@@ -325,18 +322,18 @@ void launch_ord(const StepParams &p, int zen_mode, int j, cudaStream_t st, int p
     dim3 grid((p.ny + kBX2 - 1) / kBX2, (p.nx + kBY2 - 1) / kBY2);
     const bool three = p.zen.n == 3;
     if (p.family == kTaichi) {
-        if (parts & 1) k_stress2d<ORD, 0, 0, 0><<<grid, block, 0, st>>>(p);
-        if (parts & 2) k_velocity2d<ORD, 0><<<grid, block, 0, st>>>(p, j);
+        if (parts & 1) launch_pdl(k_stress2d<ORD, 0, 0, 0>, grid, block, st, p);
+        if (parts & 2) launch_pdl(k_velocity2d<ORD, 0>, grid, block, st, p, j);
         return;
     }
     if (parts & 1) {
-        if (zen_mode == 0) k_stress2d<ORD, 1, 0, 0><<<grid, block, 0, st>>>(p);
-        else if (zen_mode == 1 && three) k_stress2d<ORD, 1, 1, 3><<<grid, block, 0, st>>>(p);
-        else if (zen_mode == 1) k_stress2d<ORD, 1, 1, kMaxSls><<<grid, block, 0, st>>>(p);
-        else if (three) k_stress2d<ORD, 1, 2, 3><<<grid, block, 0, st>>>(p);
-        else k_stress2d<ORD, 1, 2, kMaxSls><<<grid, block, 0, st>>>(p);
+        if (zen_mode == 0) launch_pdl(k_stress2d<ORD, 1, 0, 0>, grid, block, st, p);
+        else if (zen_mode == 1 && three) launch_pdl(k_stress2d<ORD, 1, 1, 3>, grid, block, st, p);
+        else if (zen_mode == 1) launch_pdl(k_stress2d<ORD, 1, 1, kMaxSls>, grid, block, st, p);
+        else if (three) launch_pdl(k_stress2d<ORD, 1, 2, 3>, grid, block, st, p);
+        else launch_pdl(k_stress2d<ORD, 1, 2, kMaxSls>, grid, block, st, p);
     }
-    if (parts & 2) k_velocity2d<ORD, 1><<<grid, block, 0, st>>>(p, j);
+    if (parts & 2) launch_pdl(k_velocity2d<ORD, 1>, grid, block, st, p, j);
 }
 
 }  // namespace

@@ -71,9 +71,23 @@ __global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_stress3d(const StepParams 
     constexpr int R = NS > 0 ? NS : 1;
 
     // ---------------- loads ----------------
+    // per-node coefficients (never written) before waiting for the previous kernel
+    float L = 0.f, M = 0.f, gp = 1.f, gs = 1.f, Mxy = 0.f, Mxz = 0.f, Myz = 0.f;
+    if (in_n) {
+        L = __ldg(p.lam_dt + i);
+        M = __ldg(p.mu_dt + i);
+        if (ZM == 2) gp = __ldg(p.g_p + i);
+    }
+    if (in_xy) {
+        Mxy = __ldg(p.mus_dt[0] + i);
+        Mxz = __ldg(p.mus_dt[1] + i);
+    }
+    if (in_yz) Myz = __ldg(p.mus_dt[2] + i);
+    if (ZM == 2) gs = __ldg(p.g_s + i);
+    pdl_wait();
     Pairs<ORD> n_x, n_y, n_z, a_vy, a_vx, b_vz, b_vx, c_vz, c_vy;
-    float s_n[3] = {0.f, 0.f, 0.f}, L = 0.f, M = 0.f, gp = 1.f, gs = 1.f;
-    float s_xy = 0.f, s_xz = 0.f, s_yz = 0.f, Mxy = 0.f, Mxz = 0.f, Myz = 0.f;
+    float s_n[3] = {0.f, 0.f, 0.f};
+    float s_xy = 0.f, s_xz = 0.f, s_yz = 0.f;
     float psi[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     float r0[R], r1[R], r2[R], r3[R], r4[R], r5[R];
     if (in_n) {
@@ -83,12 +97,9 @@ __global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_stress3d(const StepParams 
         s_n[0] = p.s[0][i];
         s_n[1] = p.s[1][i];
         s_n[2] = p.s[2][i];
-        L = __ldg(p.lam_dt + i);
-        M = __ldg(p.mu_dt + i);
         if (sx >= 0) psi[0] = p.psi[0][ix];
         if (sy >= 0) psi[1] = p.psi[1][iy];
         if (sz >= 0) psi[2] = p.psi[2][iz];
-        if (ZM == 2) gp = __ldg(p.g_p + i);
         if (ZM != 0) {
 #pragma unroll
             for (int l = 0; l < R; ++l)
@@ -106,8 +117,6 @@ __global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_stress3d(const StepParams 
         b_vx = load_pairs<ORD, true>(vx, i, 1);
         s_xy = p.s[3][i];
         s_xz = p.s[4][i];
-        Mxy = __ldg(p.mus_dt[0] + i);
-        Mxz = __ldg(p.mus_dt[1] + i);
         if (sx >= 0) {
             psi[3] = p.psi[3][ix];
             psi[5] = p.psi[5][ix];
@@ -127,7 +136,6 @@ __global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_stress3d(const StepParams 
         c_vz = load_pairs<ORD, true>(vz, i, Y);
         c_vy = load_pairs<ORD, true>(vy, i, 1);
         s_yz = p.s[5][i];
-        Myz = __ldg(p.mus_dt[2] + i);
         if (sy >= 0) psi[7] = p.psi[7][iy];
         if (sz >= 0) psi[8] = p.psi[8][iz];
         if (ZM != 0) {
@@ -136,7 +144,6 @@ __global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_stress3d(const StepParams 
                 if (l < n_mech) r5[l] = p.r[5][l * G + i];
         }
     }
-    if (ZM == 2) gs = __ldg(p.g_s + i);
 
     // ---------------- normal stresses ----------------
     if (in_n) {
@@ -251,6 +258,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_stress3d(const StepParams 
         }
         p.s[5][i] = s_yz + u;
     }
+    pdl_trigger();
 }
 
 template <int ORD>
@@ -260,7 +268,6 @@ __global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_velocity3d(const StepParam
     const int x = blockIdx.z * kBZ3 + threadIdx.z;
     const int tid = (threadIdx.z * kBY3 + threadIdx.y) * kBX3 + threadIdx.x;
     const int blk = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-    const int k = *p.step_base + j;
     const bool live = x < p.nx && y < p.ny && z < p.nz;
     const int64_t X = p.plane, Y = p.pitch;
     const int64_t i = (int64_t)x * X + y * Y + z;
@@ -275,17 +282,20 @@ __global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_velocity3d(const StepParam
     const bool in_vx = in_vz && x >= ORD && z >= ORD;        // vx region within the vz region
     const bool in_vy = in_vz && y < p.ny - ORD && z >= ORD;  // vy region within the vz region
     const int q0 = __ldg(p.src_block_start + blk), q1 = __ldg(p.src_block_start + blk + 1);
+    const float dtx = in_vx ? __ldg(p.dtr[0] + i) : 0.f;
+    const float dty = in_vz ? __ldg(p.dtr[1] + i) : 0.f;
+    pdl_wait();
+    const int k = *p.step_base + j;
 
     // ---------------- loads ----------------
     Pairs<ORD> xa, xb, xe, ya, yb, ye, za, zb, ze;
-    float v0[3] = {0.f, 0.f, 0.f}, dtx = 0.f, dty = 0.f;
+    float v0[3] = {0.f, 0.f, 0.f};
     float psi[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (in_vx) {
         xa = load_pairs<ORD, false>(sxx, i, X);
         xb = load_pairs<ORD, false>(sxy, i, Y);
         xe = load_pairs<ORD, false>(sxz, i, 1);
         v0[0] = p.v[0][i];
-        dtx = __ldg(p.dtr[0] + i);
         if (sx >= 0) psi[0] = p.psi[9][ix];
         if (sy >= 0) psi[1] = p.psi[10][iy];
         if (sz >= 0) psi[2] = p.psi[11][iz];
@@ -304,7 +314,6 @@ __global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_velocity3d(const StepParam
         zb = load_pairs<ORD, false>(syz, i, Y);
         ze = load_pairs<ORD, true>(szz, i, 1);
         v0[2] = p.v[2][i];
-        dty = __ldg(p.dtr[1] + i);
         if (sx >= 0) psi[6] = p.psi[15][ix];
         if (sy >= 0) psi[7] = p.psi[16][iy];
         if (sz >= 0) psi[8] = p.psi[17][iz];
@@ -380,18 +389,9 @@ __global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_velocity3d(const StepParam
         p.traces[(int64_t)k * p.n_rec + g] = acc;
     }
 
-    const bool bad = live && !(v2 <= p.v2_threshold);
-    const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(v2));
-    __shared__ unsigned wmax[kBX3 * kBY3 * kBZ3 / 32];
-    if ((tid & 31) == 0) wmax[tid >> 5] = m;
-    const int any_bad = __syncthreads_or(bad);
-    if (tid == 0) {
-        unsigned bm = wmax[0];
-#pragma unroll
-        for (int w = 1; w < kBX3 * kBY3 * kBZ3 / 32; ++w) bm = max(bm, wmax[w]);
-        atomicMax(reinterpret_cast<unsigned *>(p.block_max) + blk, bm);
-        if (any_bad) atomicMin(p.first_bad, k);
-    }
+    warp_stability(v2, live && !(v2 <= p.v2_threshold), reinterpret_cast<unsigned *>(p.block_max) + blk,
+                   p.first_bad, k);
+    pdl_trigger();
 }
 
 template <int ORD>
@@ -400,13 +400,13 @@ void launch_ord(const StepParams &p, int zen_mode, int j, cudaStream_t st, int p
     dim3 grid((p.nz + kBX3 - 1) / kBX3, (p.ny + kBY3 - 1) / kBY3, (p.nx + kBZ3 - 1) / kBZ3);
     const bool three = p.zen.n == 3;
     if (parts & 1) {
-        if (zen_mode == 0) k_stress3d<ORD, 0, 0><<<grid, block, 0, st>>>(p);
-        else if (zen_mode == 1 && three) k_stress3d<ORD, 1, 3><<<grid, block, 0, st>>>(p);
-        else if (zen_mode == 1) k_stress3d<ORD, 1, kMaxSls><<<grid, block, 0, st>>>(p);
-        else if (three) k_stress3d<ORD, 2, 3><<<grid, block, 0, st>>>(p);
-        else k_stress3d<ORD, 2, kMaxSls><<<grid, block, 0, st>>>(p);
+        if (zen_mode == 0) launch_pdl(k_stress3d<ORD, 0, 0>, grid, block, st, p);
+        else if (zen_mode == 1 && three) launch_pdl(k_stress3d<ORD, 1, 3>, grid, block, st, p);
+        else if (zen_mode == 1) launch_pdl(k_stress3d<ORD, 1, kMaxSls>, grid, block, st, p);
+        else if (three) launch_pdl(k_stress3d<ORD, 2, 3>, grid, block, st, p);
+        else launch_pdl(k_stress3d<ORD, 2, kMaxSls>, grid, block, st, p);
     }
-    if (parts & 2) k_velocity3d<ORD><<<grid, block, 0, st>>>(p, j);
+    if (parts & 2) launch_pdl(k_velocity3d<ORD>, grid, block, st, p, j);
 }
 
 }  // namespace
