@@ -169,6 +169,55 @@ void ts_destroy(ts_sim *sim);
 const char *ts_strerror(int code);
 const char *ts_last_error(void);
 
+/*
+ * Allocation-free 2D elastic stepper.  No counterpart in the reference: it
+ * is for callers that cannot call cudaMalloc (an application that gives
+ * this code only buffers from its own pre-sized device pool, a process whose
+ * memory budget is fixed at start-up, a time-critical loop that cannot pay
+ * an allocation's latency and implicit synchronisation).
+ *
+ * ts_run_noalloc_2d advances steps step0 .. step0 + n_steps - 1 of a 2D
+ * elastic simulation with the WGSL backend's semantics
+ * (shader_webgpu_viscoelastic.wgsl:829-1072 with viscoelastic_attn = 0) in
+ * device buffers the caller owns, enqueued on `stream` (NULL: the legacy
+ * default stream).  Its only scratch, the eight CPML convolution memories
+ * (one grid each), lives in a fixed device array of
+ * TS_NOALLOC_SCRATCH_FLOATS floats (32 MiB) that every GPU loading this
+ * library keeps until exit; grids above TS_NOALLOC_SCRATCH_FLOATS / 8 nodes
+ * are rejected with TS_E_ARG.  The function calls no allocating routine.
+ * All calls share that array, which keeps the last call's contents: step0 ==
+ * 0 clears it (a new simulation); step0 > 0 continues the previous call's
+ * simulation.  Calls that overlap on the GPU, or that interleave two
+ * simulations, race on it.  The first call on each device looks up the
+ * array's device address; make it before any stream capture.  No stability
+ * check is made (the caller can inspect the fields).
+ */
+#define TS_NOALLOC_SCRATCH_FLOATS (8u << 20)
+
+typedef struct ts_noalloc2d_args {
+    int32_t nx, ny;            /* grid, [nx][ny] with y contiguous, no padding */
+    int32_t ord;               /* 2..6 */
+    float coefs[6];            /* first ord used */
+    float dx, dy, dt;
+    /* device pointers */
+    float *vx, *vy, *sxx, *syy, *sxy;      /* wavefield, read and written */
+    const float *rho, *cp, *cs;            /* material grids as the host model leaves them */
+    const float *a_x, *b_x, *k_x, *a_xh, *b_xh, *k_xh;   /* [nx - 2 (ord - 1)] */
+    const float *a_y, *b_y, *k_y, *a_yh, *b_yh, *k_yh;   /* [ny - 2 (ord - 1)] */
+    int32_t n_src;                         /* source nodes */
+    const int32_t *src_cell;               /* [n_src] flat node index x * ny + y */
+    const float *src_value;                /* [n_rows][n_src] force at each step (divided by rho inside) */
+    int32_t n_rec;                         /* receivers, one node each */
+    const int32_t *rec_cell;               /* [n_rec] flat node index */
+    const int32_t *rec_first_step;         /* [n_rec] first recorded step */
+    float *traces;                         /* [n_rows][n_rec], rows < first step left untouched */
+    int32_t n_rows;                        /* rows of src_value and traces */
+    int32_t step0, n_steps;
+} ts_noalloc2d_args;
+
+int ts_run_noalloc_2d(const ts_noalloc2d_args *args, void *stream);
+const char *ts_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -305,3 +305,40 @@ class Stepper:
                 print(f'Time step # {done} out of {self.n_rows}')
                 print(f'Max norm velocity vector V (m/s) = {np.sqrt(vmax)}')
         return done
+
+
+class NoAlloc2DArgs(ctypes.Structure):
+    """Mirror of ``ts_noalloc2d_args`` (see :func:`run_noalloc_2d`)."""
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("ord", ctypes.c_int32),
+                ("coefs", ctypes.c_float * 6), ("dx", ctypes.c_float), ("dy", ctypes.c_float),
+                ("dt", ctypes.c_float)] + \
+               [(n, ctypes.c_void_p) for n in ("vx", "vy", "sxx", "syy", "sxy", "rho", "cp", "cs",
+                                                "a_x", "b_x", "k_x", "a_xh", "b_xh", "k_xh",
+                                                "a_y", "b_y", "k_y", "a_yh", "b_yh", "k_yh")] + \
+               [("n_src", ctypes.c_int32), ("src_cell", ctypes.c_void_p), ("src_value", ctypes.c_void_p),
+                ("n_rec", ctypes.c_int32), ("rec_cell", ctypes.c_void_p), ("rec_first_step", ctypes.c_void_p),
+                ("traces", ctypes.c_void_p), ("n_rows", ctypes.c_int32), ("step0", ctypes.c_int32),
+                ("n_steps", ctypes.c_int32)]
+
+
+def run_noalloc_2d(args, stream=None):
+    """Advance an allocation-free 2D elastic simulation in caller-owned
+    device buffers (``ts_run_noalloc_2d``).
+
+    For callers that cannot allocate device memory: every buffer in ``args``
+    is the caller's; the CPML memories live in the library's fixed 32 MiB
+    device array (grids up to 1,048,576 nodes), shared by all calls and kept
+    between them, so ``step0 == 0`` starts a simulation and later calls
+    continue it; overlapping calls race.  Make the first call on a device
+    before any stream capture.
+    """
+    lib = load_library()
+    fn = lib.ts_run_noalloc_2d
+    fn.argtypes = [ctypes.POINTER(NoAlloc2DArgs), ctypes.c_void_p]
+    fn.restype = ctypes.c_int
+    err = lib.ts_noalloc_last_error
+    err.argtypes = []
+    err.restype = ctypes.c_char_p
+    rc = fn(ctypes.byref(args), ctypes.c_void_p(stream or 0))
+    if rc != 0:
+        raise RuntimeError(f"ts_run_noalloc_2d: {lib.ts_strerror(rc).decode()} ({err().decode()})")
