@@ -170,6 +170,41 @@ const char *ts_strerror(int code);
 const char *ts_last_error(void);
 
 /*
+ * Batched 2D stepping (no single reference counterpart: it replaces the
+ * reference's shot loop, Simulator.run() calling implementation() once per
+ * emission law, sim_support/simulator.py:326-337, with one device pass over
+ * every shot of every phantom).  Each phantom is a full ts_desc (family
+ * TS_WGSL2D, ord 2 or 4; all phantoms of a batch share ord, dt, n_steps and
+ * the attenuation model) plus n_shots[p] shots; shot s of phantom p injects,
+ * at every node of the phantom's source map, column idx of its own table
+ * shot_sources[p][s][n_steps][src_cols] (idx = the map's value).  Traces
+ * are [n_shots][n_steps][n_rec] per phantom.  block_cells (0 = 8) sets the
+ * block shape, 32 shots x block_cells nodes; it is fixed at creation.
+ */
+typedef struct ts_batch ts_batch;
+
+typedef struct ts_batch_desc {
+    int32_t abi_version;
+    int32_t n_phantoms;               /* 1..8 */
+    const ts_desc *phantoms;          /* [n_phantoms] */
+    const int32_t *n_shots;           /* [n_phantoms] */
+    const float *const *shot_sources; /* [n_phantoms] -> [n_shots][n_steps][src_cols] */
+    int32_t block_cells;              /* 0, 4, 8 or 16 */
+} ts_batch_desc;
+
+int ts_batch_create(const ts_batch_desc *desc, ts_batch **out);
+int ts_batch_run(ts_batch *b, int32_t n_steps, void *stream);
+int ts_batch_reset(ts_batch *b, void *stream);
+int ts_batch_status(ts_batch *b, int32_t *steps_done, float *max_v2, int32_t *first_unstable_step);
+int ts_batch_read_traces(ts_batch *b, int32_t phantom, void *host_dst, size_t bytes);
+/* field of every shot of a phantom as [n_shots][nx][ny] floats */
+int ts_batch_read_field(ts_batch *b, int32_t phantom, int32_t what, void *host_dst, size_t bytes);
+int ts_batch_profile_steps(ts_batch *b, int32_t n_steps, void *stream, float *ms_per_kernel);
+int ts_batch_launch_count(const ts_batch *b, int64_t *launches);
+void ts_batch_destroy(ts_batch *b);
+const char *ts_batch_last_error(void);
+
+/*
  * Allocation-free 2D elastic stepper.  No counterpart in the reference: it
  * is for callers that cannot call cudaMalloc (an application that gives
  * this code only buffers from its own pre-sized device pool, a process whose

@@ -71,6 +71,17 @@ static inline FN(zener) FN(zener_at)(const ts_oracle_desc *d, int l, long cell) 
     return d->g_p ? FN(zener_cell)(d, l, cell) : FN(zener_global)(d, l);
 }
 
+/* offset_sensors[s] as the WGSL store kernel reads it (wgsl:797-799,
+ * 1125): the array holds one entry per group of equal ids in info_rec_pt
+ * (sim_support/simulator.py:289-294); past its end there is no point. */
+static int FN(first_point)(const ts_oracle_desc *d, int sn, int cols) {
+    if (d->n_rec_pt <= 0) return -1;
+    int groups = 1;
+    for (int pt = 1; pt < d->n_rec_pt; ++pt)
+        if (d->info_rec_pt[pt * cols + cols - 1] != d->info_rec_pt[(pt - 1) * cols + cols - 1]) ++groups;
+    return sn < groups ? d->offset_sensors[sn] : -1;
+}
+
 /* CPML convolution update of one derivative (b psi + a d; d/k + psi). */
 static inline real FN(cpml)(real deriv, real *psi, real a, real b, real k) {
     real p = b * (*psi) + a * deriv;
@@ -333,7 +344,7 @@ static int FN(run_wgsl2d)(const ts_oracle_desc *d, real **v, real **s, real *sen
         vmax2[it] = vmax;
         /* ---- store_sensors_kernel (:1118-1134) ---- */
         for (int sn = 0; sn < d->n_rec; ++sn) {
-            int pt = d->offset_sensors[sn];
+            int pt = FN(first_point)(d, sn, 3);
             while (pt >= 0 && pt < d->n_rec_pt && d->info_rec_pt[pt * 3 + 2] == sn) {
                 if (it >= d->delay_rec[sn]) {
                     long x = d->info_rec_pt[pt * 3 + 0], y = d->info_rec_pt[pt * 3 + 1];
@@ -571,7 +582,7 @@ static int FN(run_wgsl3d)(const ts_oracle_desc *d, real **v, real **s, real *sen
         vmax2[it] = vmax;
         /* ---- store_sensors_kernel (:1824-1843) ---- */
         for (int sn = 0; sn < d->n_rec; ++sn) {
-            int pt = d->offset_sensors[sn];
+            int pt = FN(first_point)(d, sn, 4);
             while (pt >= 0 && pt < d->n_rec_pt && d->info_rec_pt[pt * 4 + 3] == sn) {
                 if (it >= d->delay_rec[sn]) {
                     long x = d->info_rec_pt[pt * 4 + 0], y = d->info_rec_pt[pt * 4 + 1], z = d->info_rec_pt[pt * 4 + 2];

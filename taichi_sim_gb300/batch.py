@@ -1,0 +1,210 @@
+"""Batched shots: many shots of several phantoms in one device pass.
+
+The reference runs one complete simulation per emission law
+(``Simulator.run()`` -> ``implementation()``, sim_support/simulator.py:326-337),
+re-uploading every table each time.  :class:`BatchStepper` advances every
+shot of every phantom together (``ts_batch_*`` in the C ABI): per phantom
+the shot index is the innermost array axis, so a warp computes 32 shots of
+one grid node and the per-node coefficients are read once for all shots.
+
+:func:`fmc_shot_sources` builds the shots of a full-matrix capture (shot e
+fires element e of a linear array); :func:`autotune` picks the block shape
+by timing each candidate and caches the choice in ``_build/autotune.json``.
+"""
+import ctypes
+import json
+import os
+import time
+
+import numpy as np
+
+from . import engine
+
+_f = ctypes.POINTER(ctypes.c_float)
+
+
+class BatchDesc(ctypes.Structure):
+    _fields_ = [("abi_version", ctypes.c_int32), ("n_phantoms", ctypes.c_int32),
+                ("phantoms", ctypes.POINTER(engine.TsDesc)), ("n_shots", ctypes.POINTER(ctypes.c_int32)),
+                ("shot_sources", ctypes.POINTER(_f)), ("block_cells", ctypes.c_int32)]
+
+
+def _bind(lib):
+    if getattr(lib, "_batch_bound", False):
+        return lib
+    P = ctypes.c_void_p
+    sigs = {
+        "ts_batch_create": ([ctypes.POINTER(BatchDesc), ctypes.POINTER(P)], ctypes.c_int),
+        "ts_batch_run": ([P, ctypes.c_int32, P], ctypes.c_int),
+        "ts_batch_reset": ([P, P], ctypes.c_int),
+        "ts_batch_status": ([P, ctypes.POINTER(ctypes.c_int32), _f, ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
+        "ts_batch_read_traces": ([P, ctypes.c_int32, P, ctypes.c_size_t], ctypes.c_int),
+        "ts_batch_read_field": ([P, ctypes.c_int32, ctypes.c_int32, P, ctypes.c_size_t], ctypes.c_int),
+        "ts_batch_profile_steps": ([P, ctypes.c_int32, P, _f], ctypes.c_int),
+        "ts_batch_launch_count": ([P, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+        "ts_batch_destroy": ([P], None),
+        "ts_batch_last_error": ([], ctypes.c_char_p),
+    }
+    for name, (args, res) in sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    lib._batch_bound = True
+    return lib
+
+
+def _check(lib, rc, where):
+    if rc != 0:
+        raise RuntimeError(f"{where}: {lib.ts_strerror(rc).decode()} ({lib.ts_batch_last_error().decode()})")
+
+
+def fmc_shot_sources(sim):
+    """Full-matrix capture shots of a model whose first emitting probe is a
+    linear array with every element emitting: shot e keeps column e of the
+    source term and silences the others.  Returns ``[n_elem][n_steps][n_elem]``."""
+    st = np.asarray(sim._source_term, np.float32)
+    st = st[:, None] if st.ndim == 1 else st
+    n_steps, n_col = st.shape
+    shots = np.zeros((n_col, n_steps, n_col), np.float32)
+    for e in range(n_col):
+        shots[e, :, e] = st[:, e]
+    return shots
+
+
+class BatchStepper:
+    """Every shot of several phantoms advanced together on the GPU.
+
+    ``sims`` are 2D host models (one per phantom, WGSL semantics, sharing
+    ``acc``, ``dt``, ``time_steps`` and the attenuation model); ``shot_sources[p]``
+    is ``[n_shots, n_steps, src_cols]`` for phantom p.
+    """
+
+    def __init__(self, sims, shot_sources, block_cells=0):
+        self._lib = _bind(engine.load_library())
+        self.sims = list(sims)
+        self.n_ph = len(self.sims)
+        self._describers = [engine.Stepper.__new__(engine.Stepper) for _ in self.sims]
+        descs = (engine.TsDesc * self.n_ph)()
+        keep = []
+        for q, (sim, dsc) in enumerate(zip(self.sims, self._describers)):
+            dsc.sim = sim
+            dsc.family = engine.WGSL2D
+            dsc.visco = bool(sim._configs.get("simul_configs", {}).get("viscoelastic_attn", 0))
+            dsc.shape = sim.grid_shape()
+            dsc.n_rows = int(sim._n_steps)
+            dsc.n_rec = int(sim._n_rec)
+            dsc._keep = []
+            descs[q] = dsc._describe()
+            keep.append(dsc._keep)
+        self.shot_sources = [np.ascontiguousarray(np.asarray(s, np.float32)) for s in shot_sources]
+        self.n_shots = [int(s.shape[0]) for s in self.shot_sources]
+        for q, s in enumerate(self.shot_sources):
+            if s.shape[1:] != self._describers[q]._src_shape:
+                raise ValueError(f"phantom {q}: shot table {s.shape[1:]} != source term {self._describers[q]._src_shape}")
+        n_shots = (ctypes.c_int32 * self.n_ph)(*self.n_shots)
+        ptrs = (_f * self.n_ph)(*[s.ctypes.data_as(_f) for s in self.shot_sources])
+        bd = BatchDesc(abi_version=engine.ABI_VERSION, n_phantoms=self.n_ph, phantoms=descs, n_shots=n_shots,
+                       shot_sources=ptrs, block_cells=int(block_cells))
+        h = ctypes.c_void_p()
+        _check(self._lib, self._lib.ts_batch_create(ctypes.byref(bd), ctypes.byref(h)), "ts_batch_create")
+        self._h = h
+        self.n_rows = int(self.sims[0]._n_steps)
+        del keep
+
+    def run(self, n_steps, stream=None):
+        _check(self._lib, self._lib.ts_batch_run(self._h, int(n_steps), ctypes.c_void_p(stream or 0)), "ts_batch_run")
+
+    def reset(self, stream=None):
+        _check(self._lib, self._lib.ts_batch_reset(self._h, ctypes.c_void_p(stream or 0)), "ts_batch_reset")
+
+    def status(self):
+        n, m, b = ctypes.c_int32(), ctypes.c_float(), ctypes.c_int32()
+        _check(self._lib, self._lib.ts_batch_status(self._h, ctypes.byref(n), ctypes.byref(m), ctypes.byref(b)),
+               "ts_batch_status")
+        return n.value, m.value, b.value
+
+    def traces(self, phantom):
+        """``[n_shots, n_steps, n_rec]`` traces of one phantom."""
+        sim = self.sims[phantom]
+        out = np.zeros((self.n_shots[phantom], self.n_rows, sim._n_rec), np.float32)
+        _check(self._lib, self._lib.ts_batch_read_traces(self._h, phantom, out.ctypes.data_as(ctypes.c_void_p),
+                                                         out.nbytes), "ts_batch_read_traces")
+        return out
+
+    def field(self, phantom, what="syy"):
+        """``[n_shots, nx, ny]`` field of every shot of one phantom."""
+        sim = self.sims[phantom]
+        out = np.zeros((self.n_shots[phantom],) + tuple(sim.grid_shape()), np.float32)
+        code = engine.FIELD_NAMES[what]
+        _check(self._lib, self._lib.ts_batch_read_field(self._h, phantom, code, out.ctypes.data_as(ctypes.c_void_p),
+                                                        out.nbytes), "ts_batch_read_field")
+        return out
+
+    def profile_steps(self, n_steps, stream=None):
+        out = (ctypes.c_float * 2)()
+        _check(self._lib, self._lib.ts_batch_profile_steps(self._h, int(n_steps), ctypes.c_void_p(stream or 0),
+                                                           ctypes.cast(out, _f)), "ts_batch_profile_steps")
+        return list(out)
+
+    def launch_count(self):
+        n = ctypes.c_int64()
+        _check(self._lib, self._lib.ts_batch_launch_count(self._h, ctypes.byref(n)), "ts_batch_launch_count")
+        return n.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.ts_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def _cache_path():
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
+
+
+def _key(sims, shot_sources):
+    shapes = [list(s.grid_shape()) for s in sims]
+    return json.dumps({"grids": shapes, "shots": [int(np.shape(x)[0]) for x in shot_sources],
+                       "acc": int(sims[0]._coefs.shape[0]),
+                       "visco": bool(sims[0]._configs.get("simul_configs", {}).get("viscoelastic_attn", 0))},
+                      sort_keys=True)
+
+
+def autotune(sims, shot_sources, candidates=(4, 8, 16), steps=12, use_cache=True):
+    """Pick the block shape (32 shots x ``block_cells`` nodes) with the
+    shortest measured step on this GPU; the choice is cached per problem
+    shape.  Returns ``(block_cells, {candidate: ms_per_step})``."""
+    key = _key(sims, shot_sources)
+    path = _cache_path()
+    cache = {}
+    if use_cache and os.path.exists(path):
+        try:
+            with open(path) as f:
+                cache = json.load(f)
+        except (OSError, ValueError):
+            cache = {}
+        if key in cache:
+            return cache[key]["block_cells"], cache[key]["timings"]
+    timings = {}
+    for c in candidates:
+        with BatchStepper(sims, shot_sources, block_cells=c) as b:
+            b.profile_steps(2)
+            ms = b.profile_steps(steps)
+            timings[c] = float(sum(ms))
+    best = min(timings, key=timings.get)
+    cache[key] = {"block_cells": best, "timings": {str(k): v for k, v in timings.items()}, "when": time.time()}
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    with open(path, "w") as f:
+        json.dump(cache, f, indent=1)
+    return best, timings

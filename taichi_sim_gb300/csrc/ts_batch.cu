@@ -1,0 +1,772 @@
+// Batched 2D (visco)elastic stepping: many shots of several phantoms (grids
+// of uneven sizes) advanced together, one launch per kernel per time step.
+//
+// Layout: per phantom every field is [nx][ny][S] with the shot index
+// innermost (S = shots rounded up to 32).  A warp is 32 shots of one grid
+// node, so every load and store is one contiguous 128-byte row, the
+// per-node coefficients (lambda*dt, mu*dt, dt/rho, Q scale) are one
+// broadcast load shared by all shots, and the region and CPML-strip tests
+// are uniform across the warp.  Blocks are 32 shots x CY nodes along y;
+// the flat block index runs over (phantom, x, y-block, shot-block), so
+// phantoms of any size share one launch.
+//
+// Semantics: the WGSL 2D kernels (shader_webgpu_viscoelastic.wgsl:829-1072
+// and :1118-1134) per shot, except for the source columns: shot s injects
+// column idx of its own source table (the column the reference's source map
+// names), so one-element shots of a full-matrix capture fire the element
+// they name.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/taichi_sim_gb300.h"
+#include "ts_internal.cuh"
+#include "ts_prep.h"
+
+namespace ts {
+namespace {
+
+constexpr int kMaxPhantoms = 8;
+
+struct BSrc {
+    int cell;     // x * ny + y
+    int col;      // source column
+    float scale;  // dt / rho at the vy node
+};
+
+struct BPh {
+    int nx, ny, S, n_shots;
+    int64_t G;  // nx * ny * S
+    int block0, yblocks, sblocks;
+    float cd[2][kMaxOrd];
+    float *v[2], *s[3], *r[3], *psi[8];
+    const Cpml *tab_f[2], *tab_h[2];
+    Strip strip[2];
+    const float *lam, *mu, *mus, *dtr0, *dtr1, *gp, *gs;
+    const BSrc *src;
+    const int *src_start;  // [nx * yblocks + 1]
+    const float *shot_tab;  // [n_shots][rows][ncol]
+    int ncol;
+    int n_rec;
+    const int *rec_start, *rec_cell, *rec_first;
+    float *traces;  // [n_shots][rows][n_rec]
+    int rec_work0;
+};
+
+struct BParams {
+    int n_ph;
+    const BPh *ph;
+    int block_end[kMaxPhantoms];  // exclusive flat block end per phantom
+    Zener zen;
+    int rows;
+    float v2_threshold;
+    float *block_max;
+    int *first_bad;
+    const int *step_base;
+    int rec_work;
+};
+
+__device__ __forceinline__ float cpml(float d, float psi_old, float &psi_new, const Cpml &t) {
+    psi_new = fmaf(t.b, psi_old, t.a * d);
+    return fmaf(d, t.ik, psi_new);
+}
+
+struct Loc {
+    const BPh *ph;
+    int x, y, s, cell;
+    int64_t i;
+    bool live;
+};
+
+template <int CY>
+__device__ __forceinline__ Loc locate(const BParams &p) {
+    const int b = blockIdx.x;
+    int q = 0;
+#pragma unroll 1
+    while (q + 1 < p.n_ph && b >= p.block_end[q]) ++q;
+    Loc L;
+    L.ph = p.ph + q;
+    const BPh &h = *L.ph;
+    const int local = b - h.block0;
+    const int sb = local % h.sblocks, t = local / h.sblocks;
+    const int yb = t % h.yblocks;
+    L.x = t / h.yblocks;
+    L.y = yb * CY + threadIdx.y;
+    L.s = sb * 32 + threadIdx.x;
+    L.live = L.y < h.ny;
+    L.cell = L.x * h.ny + L.y;
+    L.i = (int64_t)L.cell * h.S + L.s;
+    return L;
+}
+
+template <int ORD, int ZM, int NS, int CY>
+__global__ void __launch_bounds__(32 * CY) k_bstress(const BParams p) {
+    const Loc at = locate<CY>(p);
+    const BPh &h = *at.ph;
+    const int x = at.x, y = at.y;
+    const bool in_n = at.live && x >= ORD - 1 && x < h.nx - ORD && y >= ORD && y < h.ny - ORD + 1;
+    const bool in_s = at.live && x >= ORD && x < h.nx - ORD + 1 && y >= ORD - 1 && y < h.ny - ORD;
+    if (!in_n && !in_s) return;
+    const int64_t i = at.i, X = (int64_t)h.ny * h.S, Y = h.S;
+    const int sx = strip_index(h.strip[0], x), sy = strip_index(h.strip[1], y);
+    const int64_t ix = ((int64_t)sx * h.ny + y) * h.S + at.s, iy = ((int64_t)x * h.strip[1].width + sy) * h.S + at.s;
+    const int n_mech = NS == 3 ? 3 : p.zen.n;
+    constexpr int R = NS > 0 ? NS : 1;
+
+    float L = 0.f, M = 0.f, Ms = 0.f, gp = 1.f, gs = 1.f;
+    if (in_n) {
+        L = __ldg(h.lam + at.cell);
+        M = __ldg(h.mu + at.cell);
+        if (ZM == 2) gp = __ldg(h.gp + at.cell);
+    }
+    if (in_s) Ms = __ldg(h.mus + at.cell);
+    if (ZM == 2) gs = __ldg(h.gs + at.cell);
+    pdl_wait();
+    const float *vx = h.v[0], *vy = h.v[1];
+    float nvx[ORD][2], nvy[ORD][2], svy[ORD][2], svx[ORD][2];
+    float sxx = 0.f, syy = 0.f, sxy = 0.f, pn0 = 0.f, pn1 = 0.f, ps0 = 0.f, ps1 = 0.f;
+    float rxx[R], ryy[R], rxy[R];
+    if (in_n) {
+#pragma unroll
+        for (int c = 0; c < ORD; ++c) {
+            nvx[c][0] = __ldg(vx + i + (c + 1) * X);
+            nvx[c][1] = __ldg(vx + i - c * X);
+            nvy[c][0] = __ldg(vy + i + c * Y);
+            nvy[c][1] = __ldg(vy + i - (c + 1) * Y);
+        }
+        sxx = h.s[0][i];
+        syy = h.s[1][i];
+        if (sx >= 0) pn0 = h.psi[0][ix];
+        if (sy >= 0) pn1 = h.psi[2][iy];
+        if (ZM != 0) {
+#pragma unroll
+            for (int l = 0; l < R; ++l)
+                if (l < n_mech) {
+                    rxx[l] = h.r[0][l * h.G + i];
+                    ryy[l] = h.r[1][l * h.G + i];
+                }
+        }
+    }
+    if (in_s) {
+#pragma unroll
+        for (int c = 0; c < ORD; ++c) {
+            svy[c][0] = __ldg(vy + i + c * X);
+            svy[c][1] = __ldg(vy + i - (c + 1) * X);
+            svx[c][0] = __ldg(vx + i + (c + 1) * Y);
+            svx[c][1] = __ldg(vx + i - c * Y);
+        }
+        sxy = h.s[2][i];
+        if (sx >= 0) ps0 = h.psi[1][ix];
+        if (sy >= 0) ps1 = h.psi[3][iy];
+        if (ZM != 0) {
+#pragma unroll
+            for (int l = 0; l < R; ++l)
+                if (l < n_mech) rxy[l] = h.r[2][l * h.G + i];
+        }
+    }
+    if (in_n) {
+        float ddx = 0.f, ddy = 0.f, np_;
+#pragma unroll
+        for (int c = 0; c < ORD; ++c) {
+            ddx = fmaf(h.cd[0][c], nvx[c][0] - nvx[c][1], ddx);
+            ddy = fmaf(h.cd[1][c], nvy[c][0] - nvy[c][1], ddy);
+        }
+        if (sx >= 0) {
+            ddx = cpml(ddx, pn0, np_, h.tab_h[0][x]);
+            h.psi[0][ix] = np_;
+        }
+        if (sy >= 0) {
+            ddy = cpml(ddy, pn1, np_, h.tab_f[1][y]);
+            h.psi[2][iy] = np_;
+        }
+        const float L2M = fmaf(2.f, M, L);
+        float ux = fmaf(L2M, ddx, L * ddy), uy = fmaf(L, ddx, L2M * ddy);
+        if (ZM != 0) {
+            float srxx = 0.f, sryy = 0.f;
+            const float dsum = ddx + ddy, ddif = 0.5f * (ddx - ddy);
+#pragma unroll
+            for (int l = 0; l < R; ++l)
+                if (l < n_mech) {
+                    const float a = fmaf(p.zen.Ap[l], rxx[l], (p.zen.Bp[l] * gp) * dsum);
+                    const float b = fmaf(p.zen.As[l], ryy[l], (p.zen.Bs[l] * gs) * ddif);
+                    srxx += rxx[l] + a;
+                    sryy += ryy[l] + b;
+                    h.r[0][l * h.G + i] = a;
+                    h.r[1][l * h.G + i] = b;
+                }
+            const float hl = 0.5f * (L + M);
+            ux = fmaf(hl, srxx, fmaf(M, sryy, ux));
+            uy = fmaf(hl, srxx, fmaf(-M, sryy, uy));
+        }
+        h.s[0][i] = sxx + ux;
+        h.s[1][i] = syy + uy;
+    }
+    if (in_s) {
+        float a = 0.f, b = 0.f, np_;
+#pragma unroll
+        for (int c = 0; c < ORD; ++c) {
+            a = fmaf(h.cd[0][c], svy[c][0] - svy[c][1], a);
+            b = fmaf(h.cd[1][c], svx[c][0] - svx[c][1], b);
+        }
+        if (sx >= 0) {
+            a = cpml(a, ps0, np_, h.tab_f[0][x]);
+            h.psi[1][ix] = np_;
+        }
+        if (sy >= 0) {
+            b = cpml(b, ps1, np_, h.tab_h[1][y]);
+            h.psi[3][iy] = np_;
+        }
+        const float e = a + b;
+        float u = Ms * e;
+        if (ZM != 0) {
+            float sr = 0.f;
+#pragma unroll
+            for (int l = 0; l < R; ++l)
+                if (l < n_mech) {
+                    const float n_ = fmaf(p.zen.As[l], rxy[l], (p.zen.Bs[l] * gs) * e);
+                    sr += rxy[l] + n_;
+                    h.r[2][l * h.G + i] = n_;
+                }
+            u = fmaf(0.5f * Ms, sr, u);
+        }
+        h.s[2][i] = sxy + u;
+    }
+    pdl_trigger();
+}
+
+template <int ORD, int CY>
+__global__ void __launch_bounds__(32 * CY) k_bvelocity(const BParams p, const int j) {
+    const Loc at = locate<CY>(p);
+    const BPh &h = *at.ph;
+    const int x = at.x, y = at.y;
+    const int64_t i = at.i, X = (int64_t)h.ny * h.S, Y = h.S;
+    const bool in_vy = at.live && x >= ORD - 1 && x < h.nx - ORD && y >= ORD - 1 && y < h.ny - ORD;
+    const bool in_vx = in_vy && x >= ORD && y >= ORD;
+    const int sx = strip_index(h.strip[0], x), sy = strip_index(h.strip[1], y);
+    const int64_t ix = ((int64_t)sx * h.ny + y) * h.S + at.s, iy = ((int64_t)x * h.strip[1].width + sy) * h.S + at.s;
+    const int yb = y / CY;
+    const int q0 = __ldg(h.src_start + x * h.yblocks + yb), q1 = __ldg(h.src_start + x * h.yblocks + yb + 1);
+    const float dx0 = in_vx ? __ldg(h.dtr0 + at.cell) : 0.f;
+    const float dy0 = in_vy ? __ldg(h.dtr1 + at.cell) : 0.f;
+    pdl_wait();
+    const int k = *p.step_base + j;
+    const float *sxx = h.s[0], *syy = h.s[1], *sxy = h.s[2];
+    float ax[ORD][2], bx[ORD][2], ay[ORD][2], by[ORD][2];
+    float vx0 = 0.f, vy0 = 0.f, pxa = 0.f, pxb = 0.f, pya = 0.f, pyb = 0.f;
+    if (in_vx) {
+#pragma unroll
+        for (int c = 0; c < ORD; ++c) {
+            ax[c][0] = __ldg(sxx + i + c * X);
+            ax[c][1] = __ldg(sxx + i - (c + 1) * X);
+            bx[c][0] = __ldg(sxy + i + c * Y);
+            bx[c][1] = __ldg(sxy + i - (c + 1) * Y);
+        }
+        vx0 = h.v[0][i];
+        if (sx >= 0) pxa = h.psi[4][ix];
+        if (sy >= 0) pxb = h.psi[6][iy];
+    }
+    if (in_vy) {
+#pragma unroll
+        for (int c = 0; c < ORD; ++c) {
+            ay[c][0] = __ldg(sxy + i + (c + 1) * X);
+            ay[c][1] = __ldg(sxy + i - c * X);
+            by[c][0] = __ldg(syy + i + (c + 1) * Y);
+            by[c][1] = __ldg(syy + i - c * Y);
+        }
+        vy0 = h.v[1][i];
+        if (sx >= 0) pya = h.psi[5][ix];
+        if (sy >= 0) pyb = h.psi[7][iy];
+    }
+    float v2 = 0.f;
+    if (at.live) {
+        float vxn = 0.f, vyn = 0.f, np_;
+        if (in_vx) {
+            float a = 0.f, b = 0.f;
+#pragma unroll
+            for (int c = 0; c < ORD; ++c) {
+                a = fmaf(h.cd[0][c], ax[c][0] - ax[c][1], a);
+                b = fmaf(h.cd[1][c], bx[c][0] - bx[c][1], b);
+            }
+            if (sx >= 0) {
+                a = cpml(a, pxa, np_, h.tab_f[0][x]);
+                h.psi[4][ix] = np_;
+            }
+            if (sy >= 0) {
+                b = cpml(b, pxb, np_, h.tab_f[1][y]);
+                h.psi[6][iy] = np_;
+            }
+            vxn = fmaf(a + b, dx0, vx0);
+        }
+        if (in_vy) {
+            float a = 0.f, b = 0.f;
+#pragma unroll
+            for (int c = 0; c < ORD; ++c) {
+                a = fmaf(h.cd[0][c], ay[c][0] - ay[c][1], a);
+                b = fmaf(h.cd[1][c], by[c][0] - by[c][1], b);
+            }
+            if (sx >= 0) {
+                a = cpml(a, pya, np_, h.tab_h[0][x]);
+                h.psi[5][ix] = np_;
+            }
+            if (sy >= 0) {
+                b = cpml(b, pyb, np_, h.tab_h[1][y]);
+                h.psi[7][iy] = np_;
+            }
+            vyn = fmaf(a + b, dy0, vy0);
+        }
+        if (at.s < h.n_shots && k < p.rows)
+            for (int q = q0; q < q1; ++q) {
+                const BSrc s = h.src[q];
+                if (s.cell == at.cell)
+                    vyn = fmaf(__ldg(h.shot_tab + ((int64_t)at.s * p.rows + k) * h.ncol + s.col), s.scale, vyn);
+            }
+        h.v[0][i] = vxn;
+        h.v[1][i] = vyn;
+        v2 = fmaf(vxn, vxn, vyn * vyn);
+    }
+    // receivers: flat work item g = (phantom, shot, receiver)
+    const int g = blockIdx.x * (32 * CY) + threadIdx.y * 32 + threadIdx.x;
+    if (g < p.rec_work) {
+        int q = 0;
+        while (q + 1 < p.n_ph && g >= p.ph[q + 1].rec_work0) ++q;
+        const BPh &r = p.ph[q];
+        const int w = g - r.rec_work0, shot = w / r.n_rec, rec = w % r.n_rec;
+        if (k >= __ldg(r.rec_first + rec)) {
+            float acc = 0.f;
+            for (int t = __ldg(r.rec_start + rec); t < __ldg(r.rec_start + rec + 1); ++t)
+                acc += r.s[1][(int64_t)__ldg(r.rec_cell + t) * r.S + shot];
+            r.traces[((int64_t)shot * p.rows + k) * r.n_rec + rec] = acc;
+        }
+    }
+    warp_stability(v2, at.live && !(v2 <= p.v2_threshold), reinterpret_cast<unsigned *>(p.block_max) + blockIdx.x,
+                   p.first_bad, k);
+    pdl_trigger();
+}
+
+template <int ORD, int CY>
+void launch_cy(const BParams &p, int n_blocks, int zen_mode, int j, cudaStream_t st, int parts) {
+    const dim3 block(32, CY), grid(n_blocks);
+    const bool three = p.zen.n == 3;
+    if (parts & 1) {
+        if (zen_mode == 0) launch_pdl(k_bstress<ORD, 0, 0, CY>, grid, block, st, p);
+        else if (zen_mode == 1 && three) launch_pdl(k_bstress<ORD, 1, 3, CY>, grid, block, st, p);
+        else if (zen_mode == 1) launch_pdl(k_bstress<ORD, 1, kMaxSls, CY>, grid, block, st, p);
+        else if (three) launch_pdl(k_bstress<ORD, 2, 3, CY>, grid, block, st, p);
+        else launch_pdl(k_bstress<ORD, 2, kMaxSls, CY>, grid, block, st, p);
+    }
+    if (parts & 2) launch_pdl(k_bvelocity<ORD, CY>, grid, block, st, p, j);
+}
+
+template <int ORD>
+void launch_ord(const BParams &p, int n_blocks, int cy, int zen_mode, int j, cudaStream_t st, int parts) {
+    if (cy == 4) launch_cy<ORD, 4>(p, n_blocks, zen_mode, j, st, parts);
+    else if (cy == 16) launch_cy<ORD, 16>(p, n_blocks, zen_mode, j, st, parts);
+    else launch_cy<ORD, 8>(p, n_blocks, zen_mode, j, st, parts);
+}
+
+void launch_batch(const BParams &p, int n_blocks, int ord, int cy, int zen_mode, int j, cudaStream_t st,
+                  int parts = 3) {
+    switch (ord) {
+    case 2: launch_ord<2>(p, n_blocks, cy, zen_mode, j, st, parts); break;
+    case 4: launch_ord<4>(p, n_blocks, cy, zen_mode, j, st, parts); break;
+    default: break;
+    }
+}
+
+thread_local std::string g_batch_error;
+
+int bfail(int code, const std::string &m) {
+    g_batch_error = m;
+    return code;
+}
+
+}  // namespace
+}  // namespace ts
+
+using namespace ts;
+
+struct ts_batch {
+    int device = 0, ord = 2, cy = 8, zen_mode = 0, rows = 0;
+    int n_blocks = 0, steps_done = 0, n_ph = 0;
+    int64_t launches = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_cy = 0;
+    std::vector<void *> allocs;
+    std::vector<std::pair<void *, size_t>> state;
+    std::vector<BPh> ph;
+    BPh *d_ph = nullptr;
+    BParams p{};
+    std::vector<int> shots, nrec, ncol, cells;
+
+    template <typename T>
+    int alloc(T **ptr, size_t n, bool is_state) {
+        void *d = nullptr;
+        const size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+        cudaError_t e = cudaMalloc(&d, bytes);
+        if (e != cudaSuccess) return bfail(TS_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        allocs.push_back(d);
+        if (is_state) state.push_back({d, bytes});
+        *ptr = static_cast<T *>(d);
+        return TS_OK;
+    }
+    template <typename T>
+    int upload(T **ptr, const std::vector<T> &h) {
+        int rc = alloc(ptr, h.size(), false);
+        if (rc) return rc;
+        if (!h.empty() && cudaMemcpy(*ptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+            return bfail(TS_E_CUDA, "cudaMemcpy");
+        return TS_OK;
+    }
+};
+
+extern "C" {
+
+void ts_batch_destroy(ts_batch *b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->done) cudaEventSynchronize(b->done);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (void *d : b->allocs) cudaFree(d);
+    if (b->done) cudaEventDestroy(b->done);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+const char *ts_batch_last_error(void) { return g_batch_error.c_str(); }
+
+int ts_batch_reset(ts_batch *b, void *stream) {
+    if (!b) return bfail(TS_E_ARG, "null handle");
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : b->stream;
+    for (auto &s : b->state)
+        if (cudaMemsetAsync(s.first, 0, s.second, st) != cudaSuccess) return bfail(TS_E_CUDA, "cudaMemsetAsync");
+    launch_reset_scalars(b->p.first_bad, const_cast<int *>(b->p.step_base), st);
+    b->launches += 1;
+    if (cudaEventRecord(b->done, st) != cudaSuccess) return bfail(TS_E_CUDA, "cudaEventRecord");
+    b->steps_done = 0;
+    if (!stream && cudaStreamSynchronize(b->stream) != cudaSuccess) return bfail(TS_E_CUDA, "sync");
+    return TS_OK;
+}
+
+int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
+    if (!out || !bd) return bfail(TS_E_ARG, "null argument");
+    *out = nullptr;
+    if (bd->abi_version != TS_ABI_VERSION) return bfail(TS_E_ARG, "abi_version mismatch");
+    if (bd->n_phantoms < 1 || bd->n_phantoms > kMaxPhantoms) return bfail(TS_E_ARG, "n_phantoms must be in [1, 8]");
+    if (!bd->phantoms || !bd->n_shots || !bd->shot_sources) return bfail(TS_E_ARG, "missing phantom tables");
+    if (!(bd->block_cells == 0 || bd->block_cells == 4 || bd->block_cells == 8 || bd->block_cells == 16))
+        return bfail(TS_E_ARG, "block_cells must be 0 (default), 4, 8 or 16");
+    const ts_desc *d0 = bd->phantoms;
+    for (int q = 0; q < bd->n_phantoms; ++q) {
+        const ts_desc *d = bd->phantoms + q;
+        if (d->family != TS_WGSL2D) return bfail(TS_E_ARG, "batched stepping supports the TS_WGSL2D family");
+        if (d->ord != 2 && d->ord != 4) return bfail(TS_E_ARG, "batched stepping supports ord 2 and 4");
+        if (d->ord != d0->ord || d->dt != d0->dt || d->n_steps != d0->n_steps || d->visco != d0->visco ||
+            (d->g_p == nullptr) != (d0->g_p == nullptr) || (d->visco && d->n_sls != d0->n_sls))
+            return bfail(TS_E_ARG, "phantoms of one batch must share ord, dt, n_steps and attenuation model");
+        if (d->nx < 2 * d->ord + 1 || d->ny < 2 * d->ord + 1 || d->nz != 1) return bfail(TS_E_ARG, "bad grid");
+        if (bd->n_shots[q] < 1) return bfail(TS_E_ARG, "every phantom needs at least one shot");
+        if (!bd->shot_sources[q]) return bfail(TS_E_ARG, "missing shot source table");
+        if (!d->rho || !d->cp || !d->cs || !d->pos_sources || !d->coefs || !d->a_x || !d->a_y || !d->b_x ||
+            !d->b_y || !d->k_x || !d->k_y || !d->a_xh || !d->b_xh || !d->k_xh || !d->a_yh || !d->b_yh || !d->k_yh)
+            return bfail(TS_E_ARG, "missing table");
+        if (d->n_rec > 0 && (!d->info_rec_pt || !d->offset_sensors || !d->delay_rec))
+            return bfail(TS_E_ARG, "missing receiver tables");
+        if (d->visco && !d->g_p && (!d->tau || !d->sum_alpha)) return bfail(TS_E_ARG, "missing Zener tables");
+    }
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) return bfail(TS_E_CUDA, "cudaGetDevice");
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return bfail(TS_E_CUDA, "cudaGetDeviceProperties");
+    if (!(prop.major == 10 && prop.minor == 3)) return bfail(TS_E_NODEV, "this library is built for sm_103a only");
+
+    ts_batch *b = new ts_batch();
+    auto bail = [&](int rc) {
+        ts_batch_destroy(b);
+        return rc;
+    };
+    b->device = device;
+    b->ord = d0->ord;
+    b->rows = d0->n_steps;
+    b->n_ph = bd->n_phantoms;
+    b->cy = bd->block_cells ? bd->block_cells : 8;
+    b->zen_mode = !d0->visco ? 0 : (d0->g_p ? 2 : 1);
+    b->ph.resize(b->n_ph);
+    int block0 = 0, rec0 = 0, rc;
+    for (int q = 0; q < b->n_ph; ++q) {
+        const ts_desc *d = bd->phantoms + q;
+        BPh &h = b->ph[q];
+        h = BPh{};
+        h.nx = d->nx;
+        h.ny = d->ny;
+        h.n_shots = bd->n_shots[q];
+        h.S = round_up(h.n_shots, 32);
+        h.G = (int64_t)h.nx * h.ny * h.S;
+        h.yblocks = (h.ny + b->cy - 1) / b->cy;
+        h.sblocks = h.S / 32;
+        h.block0 = block0;
+        block0 += h.nx * h.yblocks * h.sblocks;
+        const float steps[2] = {d->dx, d->dy};
+        for (int a = 0; a < 2; ++a)
+            for (int c = 0; c < kMaxOrd; ++c) h.cd[a][c] = c < d->ord ? d->coefs[c] / steps[a] : 0.f;
+        Axis ax[2] = {make_axis(h.nx, d->ord, d->a_x, d->b_x, d->k_x, d->a_xh, d->b_xh, d->k_xh),
+                      make_axis(h.ny, d->ord, d->a_y, d->b_y, d->k_y, d->a_yh, d->b_yh, d->k_yh)};
+        for (int a = 0; a < 2; ++a) {
+            Cpml *f = nullptr, *hh = nullptr;
+            if ((rc = b->upload(&f, ax[a].full)) || (rc = b->upload(&hh, ax[a].half))) return bail(rc);
+            h.tab_f[a] = f;
+            h.tab_h[a] = hh;
+            h.strip[a] = ax[a].strip;
+        }
+        for (int f = 0; f < 2; ++f)
+            if ((rc = b->alloc(&h.v[f], h.G, true))) return bail(rc);
+        for (int f = 0; f < 3; ++f)
+            if ((rc = b->alloc(&h.s[f], h.G, true))) return bail(rc);
+        const int64_t xs = (int64_t)h.strip[0].width * h.ny * h.S, ys = (int64_t)h.nx * h.strip[1].width * h.S;
+        const int64_t psz[8] = {xs, xs, ys, ys, xs, xs, ys, ys};
+        for (int k = 0; k < 8; ++k)
+            if ((rc = b->alloc(&h.psi[k], psz[k], true))) return bail(rc);
+        if (d->visco)
+            for (int m = 0; m < 3; ++m)
+                if ((rc = b->alloc(&h.r[m], h.G * d->n_sls, true))) return bail(rc);
+        // per-node coefficients, shared by every shot
+        const int64_t cells = (int64_t)h.nx * h.ny;
+        std::vector<float> lam(cells), mu(cells), mus(cells), dtr0(cells), dtr1(cells), rho_vy(cells);
+        for (int x = 0; x < h.nx; ++x)
+            for (int y = 0; y < h.ny; ++y) {
+                const Coef2D c = coef_2d(d, x, y);
+                const int64_t i = (int64_t)x * h.ny + y;
+                lam[i] = c.lam;
+                mu[i] = c.mu;
+                mus[i] = c.mus;
+                dtr0[i] = c.dtr_vx;
+                dtr1[i] = c.dtr_vy;
+                rho_vy[i] = c.rho_vy;
+            }
+        float *dev = nullptr;
+        if ((rc = b->upload(&dev, lam))) return bail(rc);
+        h.lam = dev;
+        if ((rc = b->upload(&dev, mu))) return bail(rc);
+        h.mu = dev;
+        if ((rc = b->upload(&dev, mus))) return bail(rc);
+        h.mus = dev;
+        if ((rc = b->upload(&dev, dtr0))) return bail(rc);
+        h.dtr0 = dev;
+        if ((rc = b->upload(&dev, dtr1))) return bail(rc);
+        h.dtr1 = dev;
+        if (b->zen_mode == 2) {
+            std::vector<float> gp(d->g_p, d->g_p + cells), gs(d->g_s, d->g_s + cells);
+            if ((rc = b->upload(&dev, gp))) return bail(rc);
+            h.gp = dev;
+            if ((rc = b->upload(&dev, gs))) return bail(rc);
+            h.gs = dev;
+        }
+        // sources: nodes of the source map, binned by (x, y-block)
+        std::vector<std::vector<BSrc>> bins((size_t)h.nx * h.yblocks);
+        int maxcol = 0;
+        for (int x = 0; x < h.nx; ++x)
+            for (int y = 0; y < h.ny; ++y) {
+                const int idx = d->pos_sources[(int64_t)x * h.ny + y];
+                const float r4 = rho_vy[(int64_t)x * h.ny + y];
+                if (idx < 0 || idx >= d->src_cols || !(r4 > 0.f)) continue;
+                bins[(size_t)x * h.yblocks + y / b->cy].push_back(BSrc{x * h.ny + y, idx, d->dt / r4});
+                maxcol = std::max(maxcol, idx + 1);
+            }
+        std::vector<BSrc> list;
+        std::vector<int> start(1, 0);
+        for (auto &v : bins) {
+            list.insert(list.end(), v.begin(), v.end());
+            start.push_back((int)list.size());
+        }
+        BSrc *dsrc = nullptr;
+        int *dstart = nullptr;
+        if ((rc = b->upload(&dsrc, list)) || (rc = b->upload(&dstart, start))) return bail(rc);
+        h.src = dsrc;
+        h.src_start = dstart;
+        h.ncol = d->src_cols;
+        std::vector<float> tab(bd->shot_sources[q], bd->shot_sources[q] + (size_t)h.n_shots * b->rows * d->src_cols);
+        float *dtab = nullptr;
+        if ((rc = b->upload(&dtab, tab))) return bail(rc);
+        h.shot_tab = dtab;
+        // receivers (WGSL order over info_rec_pt)
+        std::vector<int> rstart(1, 0), rcell, rfirst(std::max(1, d->n_rec), 0);
+        for (int r = 0; r < d->n_rec; ++r) {
+            for (int pt = receiver_first_point(d, r, 3); pt >= 0 && pt < d->n_rec_pt && d->info_rec_pt[pt * 3 + 2] == r; ++pt) {
+                const int x = d->info_rec_pt[pt * 3], y = d->info_rec_pt[pt * 3 + 1];
+                if (x >= 0 && x < h.nx && y >= 0 && y < h.ny) rcell.push_back(x * h.ny + y);
+            }
+            rstart.push_back((int)rcell.size());
+            rfirst[r] = d->delay_rec[r];
+        }
+        int *d1 = nullptr, *d2 = nullptr, *d3 = nullptr;
+        if ((rc = b->upload(&d1, rstart)) || (rc = b->upload(&d2, rcell)) || (rc = b->upload(&d3, rfirst))) return bail(rc);
+        h.n_rec = d->n_rec;
+        h.rec_start = d1;
+        h.rec_cell = d2;
+        h.rec_first = d3;
+        if ((rc = b->alloc(&h.traces, (size_t)h.n_shots * b->rows * std::max(1, d->n_rec), true))) return bail(rc);
+        h.rec_work0 = rec0;
+        rec0 += h.n_shots * d->n_rec;
+        b->shots.push_back(h.n_shots);
+        b->nrec.push_back(d->n_rec);
+        b->ncol.push_back(d->src_cols);
+        b->cells.push_back(h.nx * h.ny);
+    }
+    b->n_blocks = block0;
+    if ((rc = b->upload(&b->d_ph, b->ph))) return bail(rc);
+    BParams &p = b->p;
+    p.n_ph = b->n_ph;
+    p.ph = b->d_ph;
+    for (int q = 0; q < kMaxPhantoms; ++q) p.block_end[q] = q < b->n_ph ? b->ph[q].block0 + (b->ph[q].nx * b->ph[q].yblocks * b->ph[q].sblocks) : block0;
+    p.zen = zener_constants(d0);
+    p.rows = b->rows;
+    p.v2_threshold = FLT_MAX;
+    p.rec_work = rec0;
+    if ((rc = b->alloc(&p.block_max, b->n_blocks, true))) return bail(rc);
+    int *fb = nullptr, *sb = nullptr;
+    if ((rc = b->alloc(&fb, 1, false)) || (rc = b->alloc(&sb, 1, false))) return bail(rc);
+    p.first_bad = fb;
+    p.step_base = sb;
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess)
+        return bail(bfail(TS_E_CUDA, "stream/event creation"));
+    if ((rc = ts_batch_reset(b, nullptr))) return bail(rc);
+    *out = b;
+    return TS_OK;
+}
+
+int ts_batch_run(ts_batch *b, int32_t n_steps, void *stream) {
+    if (!b) return bfail(TS_E_ARG, "null handle");
+    if (n_steps < 0 || b->steps_done + (int64_t)n_steps > b->rows) return bfail(TS_E_ARG, "steps beyond n_steps");
+    cudaSetDevice(b->device);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : b->stream;
+    constexpr int G = 16;
+    auto steps = [&](int count, cudaStream_t where) {
+        for (int j = 0; j < count; ++j) launch_batch(b->p, b->n_blocks, b->ord, b->cy, b->zen_mode, j, where);
+        launch_advance(const_cast<int *>(b->p.step_base), count, where);
+    };
+    if ((!b->graph || b->graph_cy != b->cy) && n_steps >= G) {
+        if (b->graph) cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+            return bfail(TS_E_CUDA, "capture");
+        steps(G, b->stream);
+        if (cudaStreamEndCapture(b->stream, &g) != cudaSuccess) return bfail(TS_E_CUDA, "end capture");
+        cudaError_t e = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return bfail(TS_E_CUDA, std::string("graph: ") + cudaGetErrorString(e));
+        b->graph_cy = b->cy;
+    }
+    int left = n_steps;
+    while (left >= G && b->graph) {
+        if (cudaGraphLaunch(b->graph, st) != cudaSuccess) return bfail(TS_E_CUDA, "cudaGraphLaunch");
+        b->launches += 2 * G + 1;
+        left -= G;
+    }
+    if (left > 0) {
+        steps(left, st);
+        b->launches += 2 * left + 1;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return bfail(TS_E_CUDA, cudaGetErrorString(e));
+    cudaEventRecord(b->done, st);
+    b->steps_done += n_steps;
+    return TS_OK;
+}
+
+int ts_batch_status(ts_batch *b, int32_t *steps_done, float *max_v2, int32_t *first_unstable) {
+    if (!b) return bfail(TS_E_ARG, "null handle");
+    cudaEventSynchronize(b->done);
+    if (steps_done) *steps_done = b->steps_done;
+    if (max_v2) {
+        std::vector<unsigned> bm(b->n_blocks);
+        if (cudaMemcpy(bm.data(), b->p.block_max, bm.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return bfail(TS_E_CUDA, "cudaMemcpy");
+        unsigned m = 0;
+        for (unsigned v : bm) m = std::max(m, v);
+        float f;
+        memcpy(&f, &m, 4);
+        *max_v2 = f;
+    }
+    if (first_unstable) {
+        int fb = 0;
+        if (cudaMemcpy(&fb, b->p.first_bad, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return bfail(TS_E_CUDA, "cudaMemcpy");
+        *first_unstable = fb == 0x7fffffff ? -1 : fb;
+    }
+    return TS_OK;
+}
+
+int ts_batch_read_traces(ts_batch *b, int32_t phantom, void *dst, size_t bytes) {
+    if (!b || !dst || phantom < 0 || phantom >= b->n_ph) return bfail(TS_E_ARG, "bad argument");
+    cudaEventSynchronize(b->done);
+    const size_t need = (size_t)b->shots[phantom] * b->rows * b->nrec[phantom] * 4;
+    if (bytes < need) return bfail(TS_E_ARG, "destination too small");
+    if (need && cudaMemcpy(dst, b->ph[phantom].traces, need, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return bfail(TS_E_CUDA, "cudaMemcpy");
+    return TS_OK;
+}
+
+int ts_batch_read_field(ts_batch *b, int32_t phantom, int32_t what, void *dst, size_t bytes) {
+    if (!b || !dst || phantom < 0 || phantom >= b->n_ph) return bfail(TS_E_ARG, "bad argument");
+    const BPh &h = b->ph[phantom];
+    const float *src = what == TS_VX ? h.v[0] : what == TS_VY ? h.v[1] : what == TS_SXX ? h.s[0]
+                     : what == TS_SYY ? h.s[1] : what == TS_SXY ? h.s[2] : nullptr;
+    if (!src) return bfail(TS_E_ARG, "no such field");
+    cudaEventSynchronize(b->done);
+    const size_t need = (size_t)h.nx * h.ny * h.n_shots * 4;
+    if (bytes < need) return bfail(TS_E_ARG, "destination too small");
+    // device layout [nx][ny][S] -> host [n_shots][nx][ny]
+    std::vector<float> tmp((size_t)h.G);
+    if (cudaMemcpy(tmp.data(), src, tmp.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return bfail(TS_E_CUDA, "cudaMemcpy");
+    float *o = static_cast<float *>(dst);
+    const int64_t cells = (int64_t)h.nx * h.ny;
+    for (int s = 0; s < h.n_shots; ++s)
+        for (int64_t c = 0; c < cells; ++c) o[s * cells + c] = tmp[c * h.S + s];
+    return TS_OK;
+}
+
+int ts_batch_profile_steps(ts_batch *b, int32_t n_steps, void *stream, float *ms_per_kernel) {
+    if (!b || !ms_per_kernel || n_steps < 1 || b->steps_done + (int64_t)n_steps > b->rows)
+        return bfail(TS_E_ARG, "bad argument");
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : b->stream;
+    std::vector<cudaEvent_t> ev(2 * n_steps + 1);
+    for (auto &e : ev) cudaEventCreate(&e);
+    cudaEventRecord(ev[0], st);
+    for (int j = 0; j < n_steps; ++j)
+        for (int part = 0; part < 2; ++part) {
+            launch_batch(b->p, b->n_blocks, b->ord, b->cy, b->zen_mode, j, st, 1 << part);
+            cudaEventRecord(ev[2 * j + part + 1], st);
+        }
+    launch_advance(const_cast<int *>(b->p.step_base), n_steps, st);
+    b->launches += 2 * (int64_t)n_steps + 1;
+    cudaEventSynchronize(ev.back());
+    double tot[2] = {0, 0};
+    for (int j = 0; j < n_steps; ++j)
+        for (int part = 0; part < 2; ++part) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[2 * j + part], ev[2 * j + part + 1]);
+            tot[part] += ms;
+        }
+    for (auto &e : ev) cudaEventDestroy(e);
+    ms_per_kernel[0] = (float)(tot[0] / n_steps);
+    ms_per_kernel[1] = (float)(tot[1] / n_steps);
+    cudaEventRecord(b->done, st);
+    b->steps_done += n_steps;
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? TS_OK : bfail(TS_E_CUDA, cudaGetErrorString(e));
+}
+
+int ts_batch_launch_count(const ts_batch *b, int64_t *n) {
+    if (!b || !n) return bfail(TS_E_ARG, "null argument");
+    *n = b->launches;
+    return TS_OK;
+}
+
+}  // extern "C"

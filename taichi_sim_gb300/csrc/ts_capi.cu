@@ -28,6 +28,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -35,6 +36,7 @@
 
 #include "../../include/taichi_sim_gb300.h"
 #include "ts_internal.cuh"
+#include "ts_prep.h"
 
 namespace ts {
 
@@ -145,41 +147,9 @@ struct ts_sim {
     }
 };
 
-namespace {
-
-struct Axis {
-    std::vector<Cpml> full, half;
-    Strip strip;
-};
-
-bool identity(const Cpml &c) { return c.a == 0.f && c.b == 1.f && c.ik == 1.f; }
-
-Axis make_axis(int n, int ord, const float *a, const float *b, const float *k, const float *ah, const float *bh,
-               const float *kh) {
-    Axis ax;
-    const int off = ord - 1, ntab = n - 2 * (ord - 1);
-    ax.full.assign(n, Cpml{0.f, 1.f, 1.f, 0.f});
-    ax.half.assign(n, Cpml{0.f, 1.f, 1.f, 0.f});
-    std::vector<char> nonid(n, 0);
-    for (int x = 0; x < n; ++x) {
-        const int t = x - off;
-        if (t < 0 || t >= ntab || !a) continue;
-        ax.full[x] = Cpml{a[t], b[t], 1.f / k[t], 0.f};
-        ax.half[x] = Cpml{ah[t], bh[t], 1.f / kh[t], 0.f};
-        nonid[x] = !identity(ax.full[x]) || !identity(ax.half[x]);
-    }
-    int lo = 0, hi = n;
-    for (int x = 0; x < n / 2; ++x)
-        if (nonid[x]) lo = x + 1;
-    for (int x = n - 1; x >= n / 2; --x)
-        if (nonid[x]) hi = x;
-    ax.strip = Strip{lo, hi, lo + (n - hi)};
-    return ax;
-}
-
-int round_up(int v, int m) { return (v + m - 1) / m * m; }
-
-}  // namespace
+using ts::Axis;
+using ts::make_axis;
+using ts::round_up;
 
 extern "C" {
 
@@ -294,6 +264,18 @@ int ts_create(const ts_desc *d, ts_sim **out) {
 
     StepParams &p = s->p;
     p.family = s->family;
+    // nodes per thread along x (2D): enough blocks to fill the GPU, as few
+    // index/region/bookkeeping instructions per node as that allows
+    {
+        const int64_t cells = (int64_t)d->nx * d->ny;
+        // measured on GB300: 2 nodes per thread is fastest from ~200k nodes
+        // (1024^2 viscoelastic, 512^2 elastic); 4 loses occupancy to registers
+        p.tx = s->dims == 3 ? 1 : (cells >= 200000 ? 2 : 1);
+        if (const char *env = getenv("TS_2D_NODES_PER_THREAD")) {
+            const int v = atoi(env);
+            if (v == 1 || v == 2 || v == 4) p.tx = v;
+        }
+    }
     p.nx = nx;
     p.ny = ny;
     p.nz = nz;
@@ -356,27 +338,17 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     for (int k = 0; k < n_shear; ++k) mus[k].assign(s->grid_elems, 0.f);
     auto inv_or0 = [&](float r) { return r > 0.f ? dt / r : 0.f; };
     if (s->dims == 2) {
+        // normal node x-averaged (mu zero where either cs is zero), shear
+        // node y-averaged, vy node 4-point averaged (ts_prep.h)
         for (int x = 0; x < nx; ++x)
             for (int y = 0; y < ny; ++y) {
                 const int64_t i = s->at(x, y);
-                // normal node: x-averaged, mu zero where either cs is zero
-                const float rh = 0.5f * (rho(x + 1, y, 0) + rho(x, y, 0));
-                const float cph = 0.5f * (cpv(x + 1, y, 0) + cpv(x, y, 0));
-                const float c1 = csv(x + 1, y, 0), c0 = csv(x, y, 0);
-                const float csl = 0.5f * (c1 + c0);
-                const float csm = std::min(c1, c0) == 0.f ? 0.f : csl;
-                lam[i] = rh * (cph * cph - 2.f * csl * csl) * dt;
-                mu[i] = rh * (csm * csm) * dt;
-                // shear node: y-averaged
-                const float rhy = 0.5f * (rho(x, y + 1, 0) + rho(x, y, 0));
-                const float s1 = csv(x, y + 1, 0), s0 = csv(x, y, 0);
-                const float csh = std::min(s1, s0) == 0.f ? 0.f : 0.5f * (s1 + s0);
-                mus[0][i] = rhy * (csh * csh) * dt;
-                dtr0[i] = inv_or0(rho(x, y, 0));
-                const float r4 = s->family == TS_TAICHI2D
-                                     ? 0.25f * (rho(x, y + 1, 0) + rho(x, y, 0) + rho(x + 1, y + 1, 0) + rho(x + 1, y, 0))
-                                     : 0.25f * (rho(x, y, 0) + rho(x + 1, y, 0) + rho(x + 1, y + 1, 0) + rho(x, y + 1, 0));
-                dtr1[i] = inv_or0(r4);
+                const ts::Coef2D c = ts::coef_2d(d, x, y);
+                lam[i] = c.lam;
+                mu[i] = c.mu;
+                mus[0][i] = c.mus;
+                dtr0[i] = c.dtr_vx;
+                dtr1[i] = c.dtr_vy;
             }
     } else {
         for (int x = 0; x < nx; ++x)
@@ -418,30 +390,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     s->zen_mode = !d->visco ? 0 : (d->g_p ? 2 : 1);
     if (d->visco) {
         const int L = d->n_sls;
-        p.zen.n = L;
-        for (int l = 0; l < L; ++l) {
-            float hp, hs, mp, ms, bp, bs;
-            if (s->zen_mode == 1) {
-                const float inv_p = 1.f / d->tau[1 * L + l], inv_s = 1.f / d->tau[3 * L + l];
-                const float ap = d->tau[0 * L + l] / d->tau[1 * L + l], as = d->tau[2 * L + l] / d->tau[3 * L + l];
-                const float php = dt * (1.f - ap) * inv_p / d->sum_alpha[0];
-                const float phs = dt * (1.f - as) * inv_s / d->sum_alpha[1];
-                hp = 0.5f * dt * inv_p;
-                hs = 0.5f * dt * inv_s;
-                mp = 1.f / (1.f + hp);
-                ms = 1.f / (1.f + hs);
-                bp = php * mp;
-                bs = phs * ms;
-            } else {
-                hp = hs = d->zh[l];
-                mp = ms = d->zm[l];
-                bp = bs = d->zc[l] * d->zm[l];
-            }
-            p.zen.Ap[l] = (1.f - hp) * mp;
-            p.zen.As[l] = (1.f - hs) * ms;
-            p.zen.Bp[l] = bp;
-            p.zen.Bs[l] = bs;
-        }
+        p.zen = ts::zener_constants(d);
         const int nmem = s->dims == 2 ? 3 : 6;
         for (int m = 0; m < nmem; ++m)
             if ((rc = s->alloc(&p.r[m], s->grid_elems * L, true))) return bail(rc);
@@ -463,10 +412,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     // ---- launch geometry ----
     s->n_blocks = s->dims == 2 ? ts::blocks_2d(p) : ts::blocks_3d(p);
     auto block_of = [&](int x, int y, int z) -> int {
-        if (s->dims == 2) {
-            const int gx = (ny + ts::kBX2 - 1) / ts::kBX2;
-            return (x / ts::kBY2) * gx + y / ts::kBX2;
-        }
+        if (s->dims == 2) return ts::block_of_2d(p, x, y);
         const int gx = (nz + ts::kBX3 - 1) / ts::kBX3, gy = (ny + ts::kBY3 - 1) / ts::kBY3;
         return ((x / ts::kBZ3) * gy + y / ts::kBY3) * gx + z / ts::kBX3;
     };
@@ -544,7 +490,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         } else {
             const int cols = 1 + s->dims;  // [ix, iy(, iz), receiver]
             for (int r = 0; r < d->n_rec; ++r) {
-                for (int pt = d->offset_sensors[r]; pt >= 0 && pt < d->n_rec_pt && d->info_rec_pt[pt * cols + cols - 1] == r;
+                for (int pt = ts::receiver_first_point(d, r, cols); pt >= 0 && pt < d->n_rec_pt && d->info_rec_pt[pt * cols + cols - 1] == r;
                      ++pt) {
                     const int *q = d->info_rec_pt + pt * cols;
                     const int x = q[0], y = q[1], z = s->dims == 3 ? q[2] : 0;

@@ -53,6 +53,7 @@ struct Source {
 // Everything a 2D or 3D kernel reads, passed by value.
 struct StepParams {
     int family;
+    int tx;                // 2D: nodes each thread updates along x (1, 2 or 4)
     int nx, ny, nz;        // nz = 1 in 2D
     int pitch;             // padded last-axis length (floats)
     int64_t plane;         // ny * pitch (3D x stride); 2D: pitch
@@ -141,7 +142,13 @@ void launch_reset_scalars(int *first_bad, int *step_base, cudaStream_t st);
 void launch_advance(int *step_base, int n, cudaStream_t st);
 int blocks_2d(const StepParams &p);
 int blocks_3d(const StepParams &p);
-constexpr int kBX2 = 32, kBY2 = 8;              // 2D block: 32 (y) x 8 (x)
+constexpr int kBX2 = 32, kBY2 = 8;              // 2D block: 32 (y) x 8 (x) threads, p.tx nodes each along x
+
+// Flat index of the 2D block that updates node (x, y).
+inline int block_of_2d(const StepParams &p, int x, int y) {
+    const int gx = (p.ny + kBX2 - 1) / kBX2;
+    return (x / (kBY2 * p.tx)) * gx + y / kBX2;
+}
 constexpr int kBX3 = 32, kBY3 = 4, kBZ3 = 2;    // 3D block: 32 (z) x 4 (y) x 2 (x)
 
 }  // namespace ts

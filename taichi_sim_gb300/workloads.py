@@ -67,7 +67,8 @@ def _ellipses(shape, dx, rng, n, semi=(0.5, 3.0), z_min_mm=2.0):
     for k in range(1, n + 1):
         a, b = rng.uniform(*semi, 2)
         cx = rng.uniform(0.15, 0.85) * w * dx
-        cz = rng.uniform(z_min_mm + 3.0, h * dx - 3.0)
+        height = h * dx
+        cz = rng.uniform(min(z_min_mm + 3.0, 0.4 * height), max(height - 3.0, 0.6 * height))
         th = rng.uniform(0.0, np.pi)
         u = (X - cx) * np.cos(th) + (Z - cz) * np.sin(th)
         v = -(X - cx) * np.sin(th) + (Z - cz) * np.cos(th)
@@ -149,6 +150,48 @@ def visco3d_256(n_grid=256, n_steps=1000, n_rx=64, seed=0):
                             "qp": float(props[0, 3]), "qs": float(props[0, 4]), "qp_map": maps[3],
                             "qs_map": maps[4]},
     }
+
+
+def fmc2d_phantoms(n_steps=3000, shapes=((512, 768), (768, 768), (1024, 768)), n_elem=64, seed=0,
+                   dx=0.1, pml=20):
+    """Full-matrix-capture phantoms: one config per grid shape (nx, ny).
+
+    Each is a steel block with 8 seeded fluid inclusions and per-region Q
+    (as :func:`visco2d_1024`) under a 64-element linear array on the top
+    surface (0.5 mm elements, 0.6 mm pitch, 5 MHz pulse of about 3 cycles),
+    every element emitting and receiving.  ``dx`` = 0.1 mm so the 38.3 mm
+    array fits the narrowest (512-node) phantom.  Shots (one firing element
+    each) come from :func:`taichi_sim_gb300.batch.fmc_shot_sources`.
+    """
+    cfgs = []
+    for k, (nx, ny) in enumerate(shapes):
+        rng = np.random.default_rng(seed + k)
+        w, h = nx - 2 * pml - 2, ny - 2 * pml - 2
+        labels = _ellipses((w, h), dx, rng, 8)
+        cp = np.full((w, h), 5.9, np.float32)
+        cs = np.full((w, h), 3.23, np.float32)
+        rho = np.full((w, h), 7850.0, np.float32)
+        incl = labels > 0
+        cp[incl], cs[incl], rho[incl] = 1.48, 0.0, 1000.0
+        q = rng.uniform(50.0, 200.0, (9, 2)).astype(np.float32)
+        roi = {"coord_ref": [[0.0, 0.0, 0.0]], "height": round(h * dx, 6), "h_len": h, "width": round(w * dx, 6),
+               "w_len": w, "depth": 0.0, "d_len": 1, "len_pml_xmin": pml, "len_pml_xmax": pml,
+               "len_pml_ymin": 0, "len_pml_ymax": 0, "len_pml_zmin": pml, "len_pml_zmax": pml,
+               "rcoef_pml": 0.001, "npower_pml": 2.0, "k_max_pml": 1.0}
+        cfgs.append({
+            "roi": roi,
+            "probes": [{"linear": {"id": "fmc", "num_elem": n_elem, "dim_a": 0.5, "dim_p": 10.0, "inter_elem": 0.1,
+                                   "freq": 5.0, "bw": BW_3_CYCLES, "gain": 1.0,
+                                   "coord_center": [w * dx / 2, 0.0, 0.2], "emitters": "all",
+                                   "t0_emission": 0.4, "receivers": "all", "t0_reception": 0.0}}],
+            "simul_params": {"time_steps": n_steps, "dt": courant_dt(5.9, dx, 2), "acc": 2, "it_display": 500},
+            "simul_configs": {"n_iter": 1, "show_anim": 0, "viscoelastic_attn": 1,
+                              "zener_fit": {"f_min": 2.0, "f_max": 8.0, "n_sls": 3}},
+            "specimen_params": {"cp": 5.9, "cs": 3.23, "rho": 7850.0, "cp_map": cp, "cs_map": cs, "rho_map": rho,
+                                "qp": float(q[0, 0]), "qs": float(q[0, 1]), "qp_map": q[labels, 0],
+                                "qs_map": q[labels, 1]},
+        })
+    return cfgs
 
 
 WORKLOADS = {"elastic2d": elastic2d_512, "visco2d": visco2d_1024, "visco3d": visco3d_256}

@@ -1,0 +1,85 @@
+"""Batched shots agree with one simulation per shot.
+
+Every shot of a batch (phantoms of uneven sizes, shots innermost on the
+device) must match the regular stepper run on that shot alone, within the
+parity tolerance; and the plain stepper is itself checked against the CPU
+oracle for one shot, closing the chain to the reference's kernels.
+"""
+import numpy as np
+import pytest
+
+from _cases import rel_l2
+from oracle import oracle
+from taichi_sim_gb300 import engine, workloads
+from taichi_sim_gb300.batch import BatchStepper, autotune, fmc_shot_sources
+from taichi_sim_gb300.sim_support.simulator import Simulator
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def _phantoms(steps=160, n_elem=6):
+    cfgs = workloads.fmc2d_phantoms(n_steps=steps, shapes=((72, 84), (96, 84)), n_elem=n_elem, dx=0.1, pml=8)
+    for c in cfgs:  # a smaller array for the small grids
+        c["probes"][0]["linear"].update(dim_a=0.3, inter_elem=0.1)
+    return [Simulator(c) for c in cfgs]
+
+
+def _single_shot(sim, table):
+    """The regular stepper on one shot: the shot's table as the source term,
+    read as source_term[k, idx] (the stride is the table's width)."""
+    st = engine.Stepper.__new__(engine.Stepper)
+    saved = sim._source_term, sim._n_src
+    sim._source_term, sim._n_src = table, table.shape[1]
+    try:
+        st.__init__(sim, family=engine.WGSL2D)
+    finally:
+        sim._source_term, sim._n_src = saved
+    return st
+
+
+@pytest.mark.parametrize("block_cells", [4, 8, 16])
+def test_batch_matches_single_shots(block_cells):
+    sims = _phantoms()
+    shots = [fmc_shot_sources(s) for s in sims]
+    with BatchStepper(sims, shots, block_cells=block_cells) as b:
+        b.run(sims[0]._n_steps)
+        n, vmax, bad = b.status()
+        assert n == sims[0]._n_steps and bad == -1
+        for q, sim in enumerate(sims):
+            tr = b.traces(q)
+            syy = b.field(q, "syy")
+            for s in (0, 2, shots[q].shape[0] - 1):
+                with _single_shot(sim, shots[q][s]) as one:
+                    one.run(sim._n_steps)
+                    want_tr, want_f = one.read("traces"), one.read("syy")
+                assert np.abs(want_tr).max() > 0
+                assert rel_l2(tr[s], want_tr) <= TOL, (q, s, rel_l2(tr[s], want_tr))
+                assert rel_l2(syy[s], want_f) <= TOL, (q, s, rel_l2(syy[s], want_f))
+
+
+def test_single_shot_matches_oracle():
+    sim = _phantoms(steps=120)[1]
+    table = fmc_shot_sources(sim)[3]
+    with _single_shot(sim, table) as one:
+        one.run(sim._n_steps)
+        got_tr, got_f = one.read("traces"), one.read("syy")
+    saved = sim._source_term, sim._n_src
+    sim._source_term, sim._n_src = table, table.shape[1]
+    try:
+        ref = oracle.run(sim, oracle.WGSL2D)
+    finally:
+        sim._source_term, sim._n_src = saved
+    assert rel_l2(got_tr, ref["sens"]) <= TOL
+    assert rel_l2(got_f, ref["syy"]) <= TOL
+
+
+def test_autotuner_picks_and_caches(tmp_path, monkeypatch):
+    from taichi_sim_gb300 import batch
+    monkeypatch.setattr(batch, "_cache_path", lambda: str(tmp_path / "autotune.json"))
+    sims = _phantoms(steps=40)
+    shots = [fmc_shot_sources(s) for s in sims]
+    best, timings = autotune(sims, shots, steps=4)
+    assert best in (4, 8, 16) and set(timings) == {4, 8, 16}
+    again, _ = autotune(sims, shots, steps=4)
+    assert again == best and (tmp_path / "autotune.json").exists()

@@ -73,6 +73,16 @@ def test_parity_2d(name):
     _compare(sim, family, ["vx", "vy", "sxx", "syy", "sxy"])
 
 
+@pytest.mark.parametrize("tx", [1, 2, 4])
+@pytest.mark.parametrize("name", ["taichi_elastic", "wgsl_visco_q", "wgsl_visco_acc6"])
+def test_parity_2d_nodes_per_thread(name, tx, monkeypatch):
+    """Every variant of the x-marching 2D kernels (1, 2, 4 nodes per thread)."""
+    monkeypatch.setenv("TS_2D_NODES_PER_THREAD", str(tx))
+    build, family = CASES_2D[name]
+    sim = Simulator(build())
+    _compare(sim, family, ["vx", "vy", "sxx", "syy", "sxy"])
+
+
 @pytest.mark.parametrize("name", sorted(CASES_3D))
 def test_parity_3d(name):
     sim = Simulator3D(CASES_3D[name]())
