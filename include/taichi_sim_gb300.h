@@ -205,6 +205,62 @@ void ts_batch_destroy(ts_batch *b);
 const char *ts_batch_last_error(void);
 
 /*
+ * Adjoint (time-reversed) gradient of the 2D (visco)elastic stepper, family
+ * TS_WGSL2D, ord 2 or 4.  No counterpart in the reference, which has no
+ * differentiation: it runs the forward of shader_webgpu_viscoelastic.wgsl:829-1072
+ * (receivers :1118-1134) and then the transposed velocity/stress/Zener/CPML
+ * updates backward in time.
+ *
+ * The material enters as the per-node coefficients the stepper uses, on the
+ * padded layout [nx][pitch] (ts_adj_pitch; pitch = ny rounded up to 32):
+ * L = lambda dt and M = mu dt at the normal node, Ms = mu dt at the shear
+ * node, Bx = dt / rho at the vx node, By = dt / rho at the vy node (also the
+ * source scale), each a device pointer.  The caller maps per-cell lambda, mu,
+ * rho to them with the reference's staggered averaging
+ * (shader_webgpu_viscoelastic.wgsl:863-868, 948-950, 1020, 1032) and chains
+ * the returned gradients back.  With per-cell Q (desc g_p/g_s) the scales
+ * g_p, g_s [nx][pitch] are passed too.
+ *
+ *   ts_adj_create      checkpoint_every = 0 keeps the 8 per-node features of
+ *                      every step (8 * nx * pitch * n_steps floats);
+ *                      K > 0 keeps the forward state every K steps and
+ *                      recomputes each K-step segment in the backward pass
+ *   ts_adj_set_sources replaces the source table (a new shot)
+ *   ts_adj_forward     traces[n_steps][n_rec] (device), as ts_run records them
+ *   ts_adj_backward    given residual[n_steps][n_rec] = dJ/dtraces (device),
+ *                      writes dJ/dL, dJ/dM, dJ/dMs, dJ/dBx, dJ/dBy (device,
+ *                      [nx][pitch], overwritten) for the last forward
+ *
+ * ts_adj_forward and ts_adj_backward are enqueued on `stream` (NULL: the
+ * legacy default stream, which is PyTorch's default stream) and do not
+ * synchronise; ts_adj_set_sources and ts_adj_read_field synchronise the
+ * device.  The handle keeps its own copy of the coefficients of the last
+ * forward.
+ */
+typedef struct ts_adj ts_adj;
+
+typedef struct ts_adj_coefs {
+    const float *L, *M, *Ms, *Bx, *By;   /* device, [nx][pitch] */
+    const float *g_p, *g_s;              /* device, [nx][pitch]; per-cell Q only */
+} ts_adj_coefs;
+
+typedef struct ts_adj_grads {
+    float *gL, *gM, *gMs, *gBx, *gBy;    /* device, [nx][pitch] */
+} ts_adj_grads;
+
+int ts_adj_create(const ts_desc *desc, int32_t checkpoint_every, ts_adj **out);
+int ts_adj_pitch(const ts_adj *a, int32_t *pitch);
+int ts_adj_set_sources(ts_adj *a, const float *source_term);   /* host, [src_rows][src_cols] */
+int ts_adj_forward(ts_adj *a, const ts_adj_coefs *coefs, float *traces, void *stream);
+int ts_adj_backward(ts_adj *a, const float *residual, const ts_adj_grads *grads, void *stream);
+/* forward field (TS_VX, TS_VY, TS_SXX, TS_SYY, TS_SXY) after the last
+ * ts_adj_forward, as [nx][ny] floats; synchronises the device */
+int ts_adj_read_field(ts_adj *a, int32_t what, void *host_dst, size_t bytes);
+int ts_adj_launch_count(const ts_adj *a, int64_t *launches);
+void ts_adj_destroy(ts_adj *a);
+const char *ts_adj_last_error(void);
+
+/*
  * Allocation-free 2D elastic stepper.  No counterpart in the reference: it
  * is for callers that cannot call cudaMalloc (an application that gives
  * this code only buffers from its own pre-sized device pool, a process whose

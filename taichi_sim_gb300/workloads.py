@@ -194,6 +194,53 @@ def fmc2d_phantoms(n_steps=3000, shapes=((512, 768), (768, 768), (1024, 768)), n
     return cfgs
 
 
+def adjoint2d_512x1024(n_steps=3000, shape=(512, 1024), n_elem=16, n_rec=256, seed=0, true_model=True,
+                       n_blobs=5, dx=0.05, pml=20):
+    """The adjoint-gradient experiment: a 512 x 1024 grid (x across, y in
+    depth), dx = 0.05 mm, 20-cell CPML; true model = steel with n_blobs
+    seeded Gaussian blobs of +-5 % in vp and vs (sigma 1-2 mm), start model
+    = plain steel (``true_model=False``); viscoelastic with the reference's
+    fixed relaxation times (L = 3, no per-cell Q); a 16-element linear array
+    (0.5 mm elements, 0.6 mm pitch, 5 MHz pulse of about 3 cycles) on the top
+    surface, shot e firing element e (shots from
+    :func:`taichi_sim_gb300.batch.fmc_shot_sources`), and 256 one-node
+    receivers at 1.5 dx pitch under it; 3000 steps."""
+    nx, ny = shape
+    w, h = nx - 2 * pml - 2, ny - 2 * pml - 2
+    rng = np.random.default_rng(seed)
+    cp = np.full((w, h), 5.9, np.float32)
+    cs = np.full((w, h), 3.23, np.float32)
+    rho = np.full((w, h), 7850.0, np.float32)
+    if true_model:
+        X, Z = np.meshgrid(np.arange(w) * dx, np.arange(h) * dx, indexing="ij")
+        pert = np.zeros((w, h))
+        for _ in range(n_blobs):
+            cx, cz = rng.uniform(0.2, 0.8) * w * dx, rng.uniform(0.15, 0.7) * h * dx
+            s = rng.uniform(1.0, 2.0)
+            pert += rng.choice([-1.0, 1.0]) * 0.05 * np.exp(-((X - cx) ** 2 + (Z - cz) ** 2) / (2 * s * s))
+        cp = (cp * (1 + pert)).astype(np.float32)
+        cs = (cs * (1 + pert)).astype(np.float32)
+    roi = {"coord_ref": [[0.0, 0.0, 0.0]], "height": round(h * dx, 6), "h_len": h, "width": round(w * dx, 6),
+           "w_len": w, "depth": 0.0, "d_len": 1, "len_pml_xmin": pml, "len_pml_xmax": pml,
+           "len_pml_ymin": 0, "len_pml_ymax": 0, "len_pml_zmin": pml, "len_pml_zmax": pml,
+           "rcoef_pml": 0.001, "npower_pml": 2.0, "k_max_pml": 1.0}
+    center = w * dx / 2
+    return {
+        "roi": roi,
+        "probes": [
+            {"linear": {"id": "tx", "num_elem": n_elem, "dim_a": 0.5, "dim_p": 10.0, "inter_elem": 0.1,
+                        "freq": 5.0, "bw": BW_3_CYCLES, "gain": 1.0, "coord_center": [center, 0.0, 0.2],
+                        "emitters": "all", "t0_emission": 0.4, "receivers": "none", "t0_reception": 0.0}},
+            {"linear": {"id": "rx", "num_elem": n_rec, "dim_a": dx, "dim_p": 0.0, "inter_elem": 0.5 * dx,
+                        "freq": 5.0, "bw": BW_3_CYCLES, "gain": 1.0, "coord_center": [center, 0.0, 0.3],
+                        "emitters": "none", "receivers": "all", "t0_reception": 0.0}},
+        ],
+        "simul_params": {"time_steps": n_steps, "dt": courant_dt(5.9 * 1.06, dx, 2), "acc": 2, "it_display": 500},
+        "simul_configs": {"n_iter": 1, "show_anim": 0, "viscoelastic_attn": 1},
+        "specimen_params": {"cp": 5.9, "cs": 3.23, "rho": 7850.0, "cp_map": cp, "cs_map": cs, "rho_map": rho},
+    }
+
+
 WORKLOADS = {"elastic2d": elastic2d_512, "visco2d": visco2d_1024, "visco3d": visco3d_256}
 
 # Algorithmic bytes per cell-update (float32): every per-cell state array

@@ -70,6 +70,34 @@ def case_2d(w=72, h=60, steps=240, acc=2, visco=0, seed=0, maps=True, linear=Tru
     return cfg
 
 
+def gaussian_blobs(shape, seed, n=5, amp=0.05, sigma=(1.0, 2.0), dx=0.05, background=(5.9, 3.23, 7850.0)):
+    """cp/cs/rho maps: steel with n seeded Gaussian blobs of +-amp in cp and cs
+    (sigma in mm), the adjoint gradient's true model."""
+    rng = np.random.default_rng(seed)
+    w, h = shape
+    X, Z = np.meshgrid(np.arange(w) * dx, np.arange(h) * dx, indexing="ij")
+    pert = np.zeros(shape)
+    for _ in range(n):
+        cx, cz = rng.uniform(0.25, 0.75) * w * dx, rng.uniform(0.35, 0.8) * h * dx
+        s = rng.uniform(*sigma)
+        pert += rng.choice([-1.0, 1.0]) * amp * np.exp(-((X - cx) ** 2 + (Z - cz) ** 2) / (2 * s * s))
+    cp = (background[0] * (1 + pert)).astype(np.float32)
+    cs = (background[1] * (1 + pert)).astype(np.float32)
+    rho = np.full(shape, background[2], np.float32)
+    return cp, cs, rho
+
+
+def case_adjoint(w=64, h=64, steps=200, acc=2, visco=1, seed=0, true_model=True, q=None, n_elem=8):
+    """The adjoint cut-down: a linear array (all emit/receive) on steel with
+    Gaussian blobs (true model) or plain steel (start model)."""
+    cfg = case_2d(w=w, h=h, steps=steps, acc=acc, visco=visco, seed=seed, maps=False, q=q)
+    cfg["probes"][0]["linear"]["num_elem"] = n_elem
+    if true_model:
+        cp, cs, rho = gaussian_blobs((w, h), seed, sigma=(0.15 * w * 0.05, 0.3 * w * 0.05))
+        cfg["specimen_params"].update({"cp_map": cp, "cs_map": cs, "rho_map": rho})
+    return cfg
+
+
 def case_3d(w=30, d=26, h=34, steps=90, acc=2, visco=1, seed=0, q=None, matrix=False):
     """A 3D experiment: layered block, Ricker point source, receivers on top."""
     dx = 0.1
