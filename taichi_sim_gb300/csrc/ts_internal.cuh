@@ -97,7 +97,15 @@ struct StepParams {
     float *block_max;       // [n_blocks] running max of |v|^2
     int *first_bad;         // min unstable step
     const int *step_base;   // device step counter; step k = *step_base + j
+
+    // 2D adjoint record of one step, [kFeat][grid_elems] (launch_step_2d_feat)
+    float *feat;
 };
+
+// Slots of the 2D adjoint record: what the stress and velocity updates
+// multiply lambda*dt, mu*dt (normal node: x and y rows), mu*dt (shear node)
+// and dt/rho (vx, vy nodes) by.
+enum { kFeatLam = 0, kFeatMuX, kFeatMuY, kFeatShear, kFeatVx, kFeatVy, kFeat };
 
 // Programmatic dependent launch: a step kernel may be scheduled while the
 // previous kernel of the stream drains.  Before the wait it may only read
@@ -137,6 +145,9 @@ inline void launch_pdl(void (*kern)(Params...), dim3 grid, dim3 block, cudaStrea
 // Launch helpers (defined per dimension).  `parts` selects the kernels of
 // one step: 1 = stress, 2 = velocity, 3 = both (in that order).
 void launch_step_2d(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st, int parts = 3);
+// Family TS_WGSL2D step that also writes the adjoint record to p.feat
+// (p.tx must be 2).
+void launch_step_2d_feat(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st);
 void launch_step_3d(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st, int parts = 3);
 void launch_reset_scalars(int *first_bad, int *step_base, cudaStream_t st);
 void launch_advance(int *step_base, int n, cudaStream_t st);

@@ -1,0 +1,362 @@
+// 2D staggered-grid (visco)elastic step kernels on sm_103a (internal header,
+// included by the translation units that instantiate them).
+//
+// One time step = two launches on one stream:
+//   k_stress2d   : sxx, syy (normal node) and sxy (shear node) from the
+//                  velocities, with the CPML convolution in the boundary
+//                  strips and the Zener memory-variable update fused in;
+//   k_velocity2d : vx, vy from the stresses, with CPML, Dirichlet zeroing,
+//                  source injection, receiver sampling of syy and the
+//                  stability bookkeeping fused in.
+//
+// Thread (tx, ty) of block (bx, by) owns column y = 32 bx + tx and updates
+// TX consecutive nodes x = TX (8 by + ty) + t: a warp reads 128 contiguous
+// bytes per row (y is the contiguous axis).  Marching along x, the x-stencil
+// values sit in a register window that takes one new row per node, and the
+// index, region and bookkeeping work is paid once per TX nodes; these kernels
+// are otherwise limited by the instructions they issue per node.  Within a
+// node every load is issued before the first store, so one memory latency is
+// paid per node.
+//
+// With FEAT the kernels also record, per node, the quantities the adjoint
+// multiplies the coefficients by (slots of StepParams::feat, see
+// ts_internal.cuh): at the normal node (dx~ + dy~ + Sxx/2),
+// (2 dx~ + Sxx/2 + Syy) and (2 dy~ + Sxx/2 - Syy), at the shear node
+// (e + Sxy/2), at the velocity nodes the CPML-corrected stress divergences.
+//
+// Semantics follow the reference (family TS_TAICHI2D:
+// sim_taichi_elastic.py:138-309; family TS_WGSL2D:
+// shader_webgpu_viscoelastic.wgsl:829-1072 and :1118-1134) with the
+// divisions by dx/dy/rho/k replaced by multiplications with precomputed
+// reciprocals and a*b+c contracted to fma: results agree with the
+// reference's float arithmetic to rounding (checked against the CPU oracle).
+#pragma once
+#include <cuda_runtime.h>
+#include "ts_internal.cuh"
+
+namespace ts {
+namespace {
+
+constexpr int kTaichi = 0;
+
+__device__ __forceinline__ float ldg(const float *p) { return __ldg(p); }
+
+// b * psi + a * d, then d / k + psi
+__device__ __forceinline__ float cpml(float d, float psi_old, float &psi_new, const Cpml &t) {
+    psi_new = fmaf(t.b, psi_old, t.a * d);
+    return fmaf(d, t.ik, psi_new);
+}
+
+// Window of 2*ORD rows of one field at column y, first row `r0`; rows
+// outside the grid read 0 (they are only used by nodes outside the regions).
+template <int ORD>
+__device__ __forceinline__ void load_window(float (&w)[2 * ORD], const float *f, int r0, int nx, int P, int y) {
+#pragma unroll
+    for (int j = 0; j < 2 * ORD; ++j) {
+        const int r = r0 + j;
+        w[j] = (r >= 0 && r < nx) ? ldg(f + (int64_t)r * P + y) : 0.f;
+    }
+}
+
+template <int ORD>
+__device__ __forceinline__ void shift_window(float (&w)[2 * ORD], const float *f, int r_new, int nx, int P, int y) {
+#pragma unroll
+    for (int j = 0; j < 2 * ORD - 1; ++j) w[j] = w[j + 1];
+    w[2 * ORD - 1] = (r_new >= 0 && r_new < nx) ? ldg(f + (int64_t)r_new * P + y) : 0.f;
+}
+
+template <int ORD, int FAM, int ZM, int NS, int TX, bool FEAT = false>
+__global__ void __launch_bounds__(kBX2 *kBY2) k_stress2d(const StepParams p) {
+    const int y = blockIdx.x * kBX2 + threadIdx.x;
+    const int x0 = (blockIdx.y * kBY2 + threadIdx.y) * TX;
+    if (y >= p.ny || x0 >= p.nx) return;
+    const int P = p.pitch, nx = p.nx;
+    const float *__restrict__ vx = p.v[0];
+    const float *__restrict__ vy = p.v[1];
+    const int n_mech = NS == 3 ? 3 : p.zen.n;
+    constexpr int R = NS > 0 ? NS : 1;
+    const bool yn = y >= ORD && y < p.ny - ORD + 1;   // normal-stress rows in y
+    const bool ys = y >= ORD - 1 && y < p.ny - ORD;   // shear-stress rows in y
+    const int sy = strip_index(p.strip[1], y);
+    pdl_wait();
+    // vx rows [x-ORD+1, x+ORD] (normal x-derivative), vy rows [x-ORD, x+ORD-1] (shear)
+    float wvx[2 * ORD], wvy[2 * ORD];
+    load_window<ORD>(wvx, vx, x0 - ORD + 1, nx, P, y);
+    load_window<ORD>(wvy, vy, x0 - ORD, nx, P, y);
+
+#pragma unroll
+    for (int t = 0; t < TX; ++t) {
+        const int x = x0 + t;
+        if (x >= nx) break;
+        const int64_t i = (int64_t)x * P + y;
+        const bool in_n = yn && x >= ORD - 1 && x < nx - ORD;
+        const bool in_s = ys && x >= ORD && x < nx - ORD + 1;
+        if (in_n || in_s) {
+            const int sx = strip_index(p.strip[0], x);
+            const int64_t ix = (int64_t)sx * P + y, iy = (int64_t)x * p.strip[1].width + sy;
+            // ---- loads ----
+            float L = 0.f, M = 0.f, Ms = 0.f, gp = 1.f, gs = 1.f, sxx = 0.f, syy = 0.f, sxy = 0.f;
+            float ny_lo[ORD], ny_hi[ORD - 1 > 0 ? ORD - 1 : 1], sx_lo[ORD - 1 > 0 ? ORD - 1 : 1], sx_hi[ORD];
+            float rxx[R], ryy[R], rxy[R];
+            float pn0 = 0.f, pn1 = 0.f, ps0 = 0.f, ps1 = 0.f;
+            if (in_n) {
+                L = ldg(p.lam_dt + i);
+                M = ldg(p.mu_dt + i);
+                if (ZM == 2) gp = ldg(p.g_p + i);
+#pragma unroll
+                for (int c = 0; c < ORD; ++c) ny_lo[c] = ldg(vy + i - c - 1);   // vy[y-c-1]
+#pragma unroll
+                for (int c = 1; c < ORD; ++c) ny_hi[c - 1] = ldg(vy + i + c);   // vy[y+c], c >= 1
+                sxx = p.s[0][i];
+                syy = p.s[1][i];
+                if (sx >= 0) pn0 = p.psi[0][ix];
+                if (sy >= 0) pn1 = p.psi[2][iy];
+                if (ZM != 0) {
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) {
+                            rxx[l] = p.r[0][l * p.grid_elems + i];
+                            ryy[l] = p.r[1][l * p.grid_elems + i];
+                        }
+                }
+            }
+            if (in_s) {
+                Ms = ldg(p.mus_dt[0] + i);
+#pragma unroll
+                for (int c = 0; c < ORD; ++c) sx_hi[c] = ldg(vx + i + c + 1);   // vx[y+c+1]
+#pragma unroll
+                for (int c = 1; c < ORD; ++c) sx_lo[c - 1] = ldg(vx + i - c);   // vx[y-c], c >= 1
+                sxy = p.s[3][i];
+                if (sx >= 0) ps0 = p.psi[1][ix];
+                if (sy >= 0) ps1 = p.psi[3][iy];
+                if (ZM != 0) {
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) rxy[l] = p.r[2][l * p.grid_elems + i];
+                }
+            }
+            if (ZM == 2) gs = ldg(p.g_s + i);
+            // ---- normal stresses ----
+            if (in_n) {
+                float ddx = 0.f, ddy = 0.f, np_;
+#pragma unroll
+                for (int c = 0; c < ORD; ++c) {
+                    ddx = fmaf(p.cd[0][c], wvx[c + ORD] - wvx[ORD - 1 - c], ddx);
+                    const float hi = c == 0 ? wvy[ORD] : ny_hi[c > 0 ? c - 1 : 0];
+                    ddy = fmaf(p.cd[1][c], hi - ny_lo[c], ddy);
+                }
+                if (sx >= 0) {
+                    ddx = cpml(ddx, pn0, np_, p.tab_h[0][x]);
+                    p.psi[0][ix] = np_;
+                }
+                if (sy >= 0) {
+                    ddy = cpml(ddy, pn1, np_, p.tab_f[1][y]);
+                    p.psi[2][iy] = np_;
+                }
+                if (FAM == kTaichi) {
+                    const float dl = L * (ddx + ddy);
+                    sxx += fmaf(2.f * M, ddx, dl);
+                    syy += fmaf(2.f * M, ddy, dl);
+                } else {
+                    const float L2M = fmaf(2.f, M, L);
+                    float ux = fmaf(L2M, ddx, L * ddy), uy = fmaf(L, ddx, L2M * ddy);
+                    float srxx = 0.f, sryy = 0.f;
+                    if (ZM != 0) {
+                        const float dsum = ddx + ddy, ddif = 0.5f * (ddx - ddy);
+#pragma unroll
+                        for (int l = 0; l < R; ++l)
+                            if (l < n_mech) {
+                                const float a = fmaf(p.zen.Ap[l], rxx[l], (p.zen.Bp[l] * gp) * dsum);
+                                const float b = fmaf(p.zen.As[l], ryy[l], (p.zen.Bs[l] * gs) * ddif);
+                                srxx += rxx[l] + a;
+                                sryy += ryy[l] + b;
+                                p.r[0][l * p.grid_elems + i] = a;
+                                p.r[1][l * p.grid_elems + i] = b;
+                            }
+                        const float hl = 0.5f * (L + M);
+                        ux = fmaf(hl, srxx, fmaf(M, sryy, ux));
+                        uy = fmaf(hl, srxx, fmaf(-M, sryy, uy));
+                    }
+                    sxx += ux;
+                    syy += uy;
+                    if (FEAT) {
+                        const float h = 0.5f * srxx;
+                        p.feat[kFeatLam * p.grid_elems + i] = ddx + ddy + h;
+                        p.feat[kFeatMuX * p.grid_elems + i] = fmaf(2.f, ddx, h + sryy);
+                        p.feat[kFeatMuY * p.grid_elems + i] = fmaf(2.f, ddy, h - sryy);
+                    }
+                }
+                p.s[0][i] = sxx;
+                p.s[1][i] = syy;
+            }
+            // ---- shear stress ----
+            if (in_s) {
+                float a = 0.f, b = 0.f, np_;
+#pragma unroll
+                for (int c = 0; c < ORD; ++c) {
+                    a = fmaf(p.cd[0][c], wvy[c + ORD] - wvy[ORD - 1 - c], a);
+                    const float lo = c == 0 ? wvx[ORD - 1] : sx_lo[c > 0 ? c - 1 : 0];
+                    b = fmaf(p.cd[1][c], sx_hi[c] - lo, b);
+                }
+                if (sx >= 0) {
+                    a = cpml(a, ps0, np_, p.tab_f[0][x]);
+                    p.psi[1][ix] = np_;
+                }
+                if (sy >= 0) {
+                    b = cpml(b, ps1, np_, p.tab_h[1][y]);
+                    p.psi[3][iy] = np_;
+                }
+                const float e = a + b;
+                float u = Ms * e, sr = 0.f;
+                if (FAM != kTaichi && ZM != 0) {
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) {
+                            const float n_ = fmaf(p.zen.As[l], rxy[l], (p.zen.Bs[l] * gs) * e);
+                            sr += rxy[l] + n_;
+                            p.r[2][l * p.grid_elems + i] = n_;
+                        }
+                    u = fmaf(0.5f * Ms, sr, u);
+                }
+                if (FEAT) p.feat[kFeatShear * p.grid_elems + i] = fmaf(0.5f, sr, e);
+                p.s[3][i] = sxy + u;
+            }
+        }
+        if (t + 1 < TX) {
+            shift_window<ORD>(wvx, vx, x + ORD + 1, nx, P, y);
+            shift_window<ORD>(wvy, vy, x + ORD, nx, P, y);
+        }
+    }
+    pdl_trigger();
+}
+
+template <int ORD, int FAM, int TX, bool FEAT = false>
+__global__ void __launch_bounds__(kBX2 *kBY2) k_velocity2d(const StepParams p, const int j) {
+    const int y = blockIdx.x * kBX2 + threadIdx.x;
+    const int x0 = (blockIdx.y * kBY2 + threadIdx.y) * TX;
+    const int tid = threadIdx.y * kBX2 + threadIdx.x;
+    const int blk = blockIdx.y * gridDim.x + blockIdx.x;
+    const int P = p.pitch, nx = p.nx;
+    const bool live_col = y < p.ny;
+    const float *__restrict__ sxx = p.s[0];
+    const float *__restrict__ syy = p.s[1];
+    const float *__restrict__ sxy = p.s[3];
+    const int sy = live_col ? strip_index(p.strip[1], y) : -1;
+    // y-part of the regions
+    const bool yvy = y >= ORD - 1 && y < p.ny - ORD;
+    const bool yvx = FAM == kTaichi ? (y >= ORD && y < p.ny - ORD + 1) : (yvy && y >= ORD);
+    const int q0 = __ldg(p.src_block_start + blk), q1 = __ldg(p.src_block_start + blk + 1);
+    pdl_wait();
+    const int k = *p.step_base + j;
+    float vmax = 0.f;
+    bool bad = false;
+
+    if (live_col && x0 < nx) {
+        // sxx rows [x-ORD, x+ORD-1] (vx), sxy rows [x-ORD+1, x+ORD] (vy; row x also feeds vx's y-derivative)
+        float wxx[2 * ORD], wxy[2 * ORD];
+        load_window<ORD>(wxx, sxx, x0 - ORD, nx, P, y);
+        load_window<ORD>(wxy, sxy, x0 - ORD + 1, nx, P, y);
+#pragma unroll
+        for (int t = 0; t < TX; ++t) {
+            const int x = x0 + t;
+            if (x >= nx) break;
+            const int64_t i = (int64_t)x * P + y;
+            const bool in_vy = yvy && x >= ORD - 1 && x < nx - ORD;
+            const bool in_vx = FAM == kTaichi ? (yvx && x >= ORD && x < nx - ORD + 1) : (yvx && in_vy && x >= ORD);
+            const int sx = strip_index(p.strip[0], x);
+            const int64_t ix = (int64_t)sx * P + y, iy = (int64_t)x * p.strip[1].width + sy;
+            // ---- loads ----
+            float bx_lo[ORD], bx_hi[ORD - 1 > 0 ? ORD - 1 : 1], by[2 * ORD];
+            float vx0 = 0.f, vy0 = 0.f, dx0 = 0.f, dy0 = 0.f, pxa = 0.f, pxb = 0.f, pya = 0.f, pyb = 0.f;
+            if (in_vx) {
+#pragma unroll
+                for (int c = 0; c < ORD; ++c) bx_lo[c] = ldg(sxy + i - c - 1);   // sxy[y-c-1]
+#pragma unroll
+                for (int c = 1; c < ORD; ++c) bx_hi[c - 1] = ldg(sxy + i + c);   // sxy[y+c], c >= 1
+                vx0 = p.v[0][i];
+                dx0 = ldg(p.dtr[0] + i);
+                if (sx >= 0) pxa = p.psi[4][ix];
+                if (sy >= 0) pxb = p.psi[6][iy];
+            }
+            if (in_vy) {
+#pragma unroll
+                for (int c = 0; c < 2 * ORD; ++c) by[c] = ldg(syy + i - ORD + 1 + c);   // syy[y-ORD+1 .. y+ORD]
+                vy0 = p.v[1][i];
+                dy0 = ldg(p.dtr[1] + i);
+                if (sx >= 0) pya = p.psi[5][ix];
+                if (sy >= 0) pyb = p.psi[7][iy];
+            }
+            // ---- update ----
+            float vxn = 0.f, vyn = 0.f, np_, fax = 0.f, fay = 0.f;
+            if (in_vx) {
+                float a = 0.f, b = 0.f;
+#pragma unroll
+                for (int c = 0; c < ORD; ++c) {
+                    a = fmaf(p.cd[0][c], wxx[c + ORD] - wxx[ORD - 1 - c], a);
+                    const float hi = c == 0 ? wxy[ORD - 1] : bx_hi[c > 0 ? c - 1 : 0];
+                    b = fmaf(p.cd[1][c], hi - bx_lo[c], b);
+                }
+                if (sx >= 0) {
+                    a = cpml(a, pxa, np_, p.tab_f[0][x]);
+                    p.psi[4][ix] = np_;
+                }
+                if (sy >= 0) {
+                    b = cpml(b, pxb, np_, p.tab_f[1][y]);
+                    p.psi[6][iy] = np_;
+                }
+                fax = a + b;
+                vxn = fmaf(fax, dx0, vx0);
+            }
+            if (in_vy) {
+                float a = 0.f, b = 0.f;
+#pragma unroll
+                for (int c = 0; c < ORD; ++c) {
+                    a = fmaf(p.cd[0][c], wxy[c + ORD] - wxy[ORD - 1 - c], a);
+                    b = fmaf(p.cd[1][c], by[ORD + c] - by[ORD - 1 - c], b);
+                }
+                if (sx >= 0) {
+                    a = cpml(a, pya, np_, p.tab_h[0][x]);
+                    p.psi[5][ix] = np_;
+                }
+                if (sy >= 0) {
+                    b = cpml(b, pyb, np_, p.tab_h[1][y]);
+                    p.psi[7][iy] = np_;
+                }
+                fay = a + b;
+                vyn = fmaf(fay, dy0, vy0);
+            }
+            for (int q = q0; q < q1; ++q) {
+                const Source s = p.src[q];
+                if (s.cell == i && k < p.src_rows)
+                    vyn = fmaf(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), s.scale, vyn);
+            }
+            p.v[0][i] = vxn;
+            p.v[1][i] = vyn;
+            if (FEAT) {
+                p.feat[kFeatVx * p.grid_elems + i] = fax;
+                p.feat[kFeatVy * p.grid_elems + i] = fay;
+            }
+            const float v2 = fmaf(vxn, vxn, vyn * vyn);
+            bad |= !(v2 <= p.v2_threshold);
+            vmax = fmaxf(vmax, v2);
+            if (v2 != v2) vmax = v2;  // keep a NaN visible
+            if (t + 1 < TX) {
+                shift_window<ORD>(wxx, sxx, x + ORD, nx, P, y);
+                shift_window<ORD>(wxy, sxy, x + ORD + 1, nx, P, y);
+            }
+        }
+    }
+
+    // receivers: global thread g samples receiver g (syy is final for step k)
+    const int g = blk * (kBX2 * kBY2) + tid;
+    if (g < p.n_rec && k >= __ldg(p.rec_first_step + g)) {
+        float acc = 0.f;
+        for (int q = __ldg(p.rec_start + g); q < __ldg(p.rec_start + g + 1); ++q) acc += syy[__ldg(p.rec_cell + q)];
+        p.traces[(int64_t)k * p.n_rec + g] = acc;
+    }
+    warp_stability(vmax, bad, reinterpret_cast<unsigned *>(p.block_max) + blk, p.first_bad, k);
+    pdl_trigger();
+}
+
+}  // namespace
+}  // namespace ts

@@ -1,0 +1,36 @@
+// Instantiations of the 2D step kernels that record the adjoint's per-node
+// quantities (family TS_WGSL2D, two nodes per thread), in their own
+// translation unit so that they compile in parallel with the plain ones.
+#include <cuda_runtime.h>
+#include "ts_kernels2d.cuh"
+
+namespace ts {
+namespace {
+
+template <int ORD>
+void launch_feat(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
+    constexpr int TX = 2;
+    const dim3 block(kBX2, kBY2), grid((p.ny + kBX2 - 1) / kBX2, (p.nx + kBY2 * TX - 1) / (kBY2 * TX));
+    const bool three = p.zen.n == 3;
+    if (zen_mode == 0) launch_pdl(k_stress2d<ORD, 1, 0, 0, TX, true>, grid, block, st, p);
+    else if (zen_mode == 1 && three) launch_pdl(k_stress2d<ORD, 1, 1, 3, TX, true>, grid, block, st, p);
+    else if (zen_mode == 1) launch_pdl(k_stress2d<ORD, 1, 1, kMaxSls, TX, true>, grid, block, st, p);
+    else if (three) launch_pdl(k_stress2d<ORD, 1, 2, 3, TX, true>, grid, block, st, p);
+    else launch_pdl(k_stress2d<ORD, 1, 2, kMaxSls, TX, true>, grid, block, st, p);
+    launch_pdl(k_velocity2d<ORD, 1, TX, true>, grid, block, st, p, j);
+}
+
+}  // namespace
+
+void launch_step_2d_feat(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st) {
+    switch (ord) {
+    case 2: launch_feat<2>(p, zen_mode, j, st); break;
+    case 3: launch_feat<3>(p, zen_mode, j, st); break;
+    case 4: launch_feat<4>(p, zen_mode, j, st); break;
+    case 5: launch_feat<5>(p, zen_mode, j, st); break;
+    case 6: launch_feat<6>(p, zen_mode, j, st); break;
+    default: break;  // rejected at creation
+    }
+}
+
+}  // namespace ts
