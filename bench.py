@@ -150,6 +150,11 @@ def run_reference(args):
     if rank != 0:
         return
     name = args.workload
+    if name == "adjoint2d":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference computes no gradients"}))
+        return
+    if name == "fmc2d":
+        name = "visco2d"   # the reference runs one shot at a time: its per-shot path
     sim = build_model(name, args.time_steps)
     from oracle import oracle
     fam = {"elastic2d": oracle.TAICHI2D, "visco2d": oracle.WGSL2D, "visco3d": oracle.WGSL3D}[name]
@@ -263,12 +268,176 @@ def run_fmc(args):
     print(json.dumps(line))
 
 
+ADJ_BYTES = {
+    # adjoint step per cell (float32, L = 3 global relaxation times):
+    # velocity kernel: vbar r/w 16, stress-node adjoints gathered 16, Bx By 8,
+    # record 8, gBx gBy r/w 16, velocity-node adjoints written 16;
+    # stress kernel: velocity-node adjoints 16, sbar r/w 24, L M Ms 12,
+    # record 16, gL gM gMs r/w 24, Zener adjoints r/w 72, stress-node adjoints 16
+    "adjoint_step": 80 + 180,
+    # forward step of the same model (its algorithmic bytes) and the record it writes when recomputing
+    "forward_step": 127.75, "record": 24,
+}
+
+
+def run_adjoint(args):
+    """Adjoint gradient: 16 shots of a 512 x 1024 viscoelastic model (3000
+    steps, 256 receivers), gradient of the L2 trace misfit w.r.t. per-cell
+    lambda, mu, rho summed over shots, checkpointing every ceil(sqrt(3000))
+    = 55 steps; one bench step = the whole 16-shot gradient.  Reported next
+    to one plain forward per shot (the regular stepper) as t_grad / t_forward."""
+    import torch
+    from taichi_sim_gb300 import engine
+    from taichi_sim_gb300.adjoint import AdjointProblem, l2_misfit
+    from taichi_sim_gb300.batch import fmc_shot_sources
+    from taichi_sim_gb300.sim_support.simulator import Simulator
+
+    n_t = args.time_steps or 3000
+    true = Simulator(workloads.adjoint2d_512x1024(n_steps=n_t))
+    start = Simulator(workloads.adjoint2d_512x1024(n_steps=n_t, true_model=False))
+    shots = fmc_shot_sources(start)
+    n_shots = shots.shape[0]
+    cells = int(np.prod(start.grid_shape()))
+    stream = torch.cuda.Stream()
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    # observed data: the true model through the same forward (untimed)
+    with torch.cuda.stream(stream), AdjointProblem(true, checkpoint_every=64) as pt, torch.no_grad():
+        obs = []
+        for s in range(n_shots):
+            pt.set_source_term(shots[s])
+            obs.append(pt.traces(*pt.material()).clone())
+
+    # t_forward: the plain stepper, one simulation per shot
+    with engine.Stepper(start, family=engine.WGSL2D) as st:
+        h = stream.cuda_stream
+
+        def forward_all():
+            for s in range(n_shots):
+                st.set_sources(shots[s])
+                st.reset(stream=h, wait=False)
+                st.run(n_t, stream=h)
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+
+        forward_all()
+        torch.cuda.synchronize()
+        a, b = ev(), ev()
+        a.record(stream)
+        forward_all()
+        b.record(stream)
+        torch.cuda.synchronize()
+        t_fwd_ms = a.elapsed_time(b) / n_shots
+
+    def gradient(prob, m):
+        for t in m:
+            t.grad = None
+        for s in range(n_shots):
+            prob.set_source_term(shots[s])
+            l2_misfit(prob.traces(*m), obs[s]).backward()
+            with torch.cuda.stream(stream):
+                flush.zero_()
+
+    ckpt = int(np.ceil(np.sqrt(n_t)))
+    with torch.cuda.stream(stream), AdjointProblem(start, checkpoint_every=ckpt) as prob:
+        m = [t.clone().requires_grad_(True) for t in prob.material()]
+        for _ in range(args.warmup):
+            gradient(prob, m)
+        torch.cuda.synchronize()
+        l0 = prob.launch_count()
+        start_ev, end_ev = ev(), ev()
+        with ClockSampler(0) as clk:
+            start_ev.record(stream)
+            for _ in range(args.steps):
+                gradient(prob, m)
+            end_ev.record(stream)
+            torch.cuda.synchronize()
+        ms = start_ev.elapsed_time(end_ev)
+        launches = prob.launch_count() - l0
+        grad_ref = [t.grad.detach().clone() for t in m]
+
+        # end to end: material and observed traces from host memory, gradient back to host
+        host_m = [t.detach().cpu().pin_memory() for t in m]
+        host_obs = [o.cpu().pin_memory() for o in obs]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        md = [t.to("cuda", non_blocking=True).requires_grad_(True) for t in host_m]
+        for s in range(n_shots):
+            prob.set_source_term(shots[s])
+            l2_misfit(prob.traces(*md), host_obs[s].to("cuda", non_blocking=True)).backward()
+        g_host = [t.grad.cpu() for t in md]
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        h2d = sum(t.numel() * 4 for t in host_m) + sum(o.numel() * 4 for o in host_obs)
+        d2h = sum(t.numel() * 4 for t in g_host)
+
+    # the same gradient with the whole record kept in HBM (no recomputation)
+    with torch.cuda.stream(stream), AdjointProblem(start, checkpoint_every=0) as prob0:
+        m0 = [t.detach().clone().requires_grad_(True) for t in m]
+        gradient(prob0, m0)
+        torch.cuda.synchronize()
+        a, b = ev(), ev()
+        a.record(stream)
+        gradient(prob0, m0)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms_keep = a.elapsed_time(b)
+        agree = max(float((x.grad - y).norm() / y.norm()) for x, y in zip(m0, grad_ref))
+        # one adjoint sweep alone (the record kept): backward of one shot
+        prob0.set_source_term(shots[0])
+        tr = prob0.traces(*m0)
+        loss = l2_misfit(tr, obs[0])
+        torch.cuda.synchronize()
+        a.record(stream)
+        loss.backward()
+        b.record(stream)
+        torch.cuda.synchronize()
+        sweep_ms = a.elapsed_time(b)
+
+    t_grad_ms = ms / args.steps / n_shots
+    ratio = t_grad_ms / t_fwd_ms
+    value = cells * n_t * n_shots * args.steps / (ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    adj_bytes = cells * ADJ_BYTES["adjoint_step"]
+    achieved = adj_bytes / (sweep_ms / n_t / 1e3) / 1e9
+    cpu = None if args.no_cpu_baseline else cpu_baseline(start, "visco2d")
+    if cpu:
+        cpu["sample"] += "; the reference computes no gradient: this is its forward on the same grid"
+    line = {"metric": "Gcell-updates/s", "value": round(value, 3), "unit": "Gcell/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded numpy default_rng(0); no public dataset exists)",
+            "config": {"workload": "adjoint2d", "grid": list(start.grid_shape()), "time_steps": n_t,
+                       "shots_per_step": n_shots, "receivers": int(start._n_rec), "checkpoint_every": ckpt,
+                       "zener": "L=3, fixed relaxation times",
+                       "value_is": "forward cell-updates of the 16 shots per second of gradient time",
+                       "l2": "256 MiB flush written after every shot (inside the timed region)"},
+            "adjoint": {"t_grad_over_t_forward": round(ratio, 3), "t_forward_ms_per_shot": round(t_fwd_ms, 3),
+                        "t_grad_ms_per_shot": round(t_grad_ms, 3),
+                        "record_kept": {"t_grad_over_t_forward": round(ms_keep / n_shots / t_fwd_ms, 3),
+                                        "record_gb": round(cells * n_t * 24 / 1e9, 1),
+                                        "gradient_rel_diff_vs_checkpointed": agree},
+                        "adjoint_step_ms": round(sweep_ms / n_t, 5)},
+            "roofline": {"kernel": "adjoint step (k_adj_velocity + k_adj_stress)", "bound": "hbm",
+                         "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
+                         "bytes_per_launch_pair": int(adj_bytes)},
+            "cpu_baseline": cpu,
+            "e2e": {"value": cells * n_t * n_shots / e2e_s / 1e9, "unit": "Gcell/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "seconds_per_step": round(e2e_s, 4),
+                    "path": "material + observed traces from pinned host memory, 16 x (traces, misfit, "
+                            "backward), gradient to host"},
+            "gpu_launches": int(launches), "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="visco2d", choices=sorted(workloads.WORKLOADS) + ["fmc2d"])
+    ap.add_argument("--workload", default="visco2d", choices=sorted(workloads.WORKLOADS) + ["fmc2d", "adjoint2d"])
     ap.add_argument("--loop-shots", type=int, default=4, help="fmc2d: shots per phantom timed in the per-shot loop")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ref-sample-steps", type=int, default=200)
@@ -285,6 +454,8 @@ def main():
         return run_reference(args)
     if args.workload == "fmc2d":
         return run_fmc(args)
+    if args.workload == "adjoint2d":
+        return run_adjoint(args)
 
     import torch
     from taichi_sim_gb300 import engine

@@ -52,7 +52,8 @@
 namespace ts {
 namespace {
 
-constexpr int kTX = 2;  // nodes per thread along x, forward and adjoint
+constexpr int kTX = 2;     // nodes per thread along x of the forward kernels
+constexpr int kAdjTx = 1;  // and of the adjoint kernels
 
 // Everything the adjoint kernels read, passed by value.
 struct AdjState {
@@ -97,8 +98,8 @@ __device__ __forceinline__ float ld_y(const float *f, int64_t row, int yy, int n
     return (yy >= 0 && yy < ny) ? __ldg(f + row + yy) : 0.f;
 }
 
-template <int ORD, int TX>
-__global__ void __launch_bounds__(kBX2 *kBY2) k_adj_velocity(const AdjState a, const float *__restrict__ rec, int k) {
+template <int ORD, int TX, int MINB>
+__global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_velocity(const AdjState a, const float *__restrict__ rec, int k) {
     const int y = blockIdx.x * kBX2 + threadIdx.x;
     const int x0 = (blockIdx.y * kBY2 + threadIdx.y) * TX;
     const int tid = threadIdx.y * kBX2 + threadIdx.x;
@@ -220,8 +221,8 @@ __global__ void __launch_bounds__(kBX2 *kBY2) k_adj_velocity(const AdjState a, c
     pdl_trigger();
 }
 
-template <int ORD, int ZM, int NS, int TX>
-__global__ void __launch_bounds__(kBX2 *kBY2) k_adj_stress(const AdjState a, const float *__restrict__ rec) {
+template <int ORD, int ZM, int NS, int TX, int MINB>
+__global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_stress(const AdjState a, const float *__restrict__ rec) {
     const int y = blockIdx.x * kBX2 + threadIdx.x;
     const int x0 = (blockIdx.y * kBY2 + threadIdx.y) * TX;
     if (y >= a.ny || x0 >= a.nx) return;
@@ -369,16 +370,25 @@ __global__ void __launch_bounds__(kBX2 *kBY2) k_adj_stress(const AdjState a, con
     pdl_trigger();
 }
 
+template <int ORD, int TX, int MINB>
+void launch_adj_shape(const AdjState &a, int zm, const float *rec, int k, cudaStream_t st) {
+    const dim3 block(kBX2, kBY2), grid((a.ny + kBX2 - 1) / kBX2, (a.nx + kBY2 * TX - 1) / (kBY2 * TX));
+    launch_pdl(k_adj_velocity<ORD, TX, MINB>, grid, block, st, a, rec, k);
+    const bool three = a.zen.n == 3;
+    if (zm == 0) launch_pdl(k_adj_stress<ORD, 0, 0, TX, MINB>, grid, block, st, a, rec);
+    else if (zm == 1 && three) launch_pdl(k_adj_stress<ORD, 1, 3, TX, MINB>, grid, block, st, a, rec);
+    else if (zm == 1) launch_pdl(k_adj_stress<ORD, 1, kMaxSls, TX, MINB>, grid, block, st, a, rec);
+    else if (three) launch_pdl(k_adj_stress<ORD, 2, 3, TX, MINB>, grid, block, st, a, rec);
+    else launch_pdl(k_adj_stress<ORD, 2, kMaxSls, TX, MINB>, grid, block, st, a, rec);
+}
+
+// Block shape of the adjoint kernels: one node per thread, and a register
+// budget that keeps 4 (ord 2) or 3 blocks resident per SM without spills
+// (measured on the 512 x 1024 three-mechanism case: about 1.3x the speed of
+// two nodes per thread with an unconstrained budget).
 template <int ORD>
 void launch_adj_ord(const AdjState &a, int zm, const float *rec, int k, cudaStream_t st) {
-    const dim3 block(kBX2, kBY2), grid((a.ny + kBX2 - 1) / kBX2, (a.nx + kBY2 * kTX - 1) / (kBY2 * kTX));
-    launch_pdl(k_adj_velocity<ORD, kTX>, grid, block, st, a, rec, k);
-    const bool three = a.zen.n == 3;
-    if (zm == 0) launch_pdl(k_adj_stress<ORD, 0, 0, kTX>, grid, block, st, a, rec);
-    else if (zm == 1 && three) launch_pdl(k_adj_stress<ORD, 1, 3, kTX>, grid, block, st, a, rec);
-    else if (zm == 1) launch_pdl(k_adj_stress<ORD, 1, kMaxSls, kTX>, grid, block, st, a, rec);
-    else if (three) launch_pdl(k_adj_stress<ORD, 2, 3, kTX>, grid, block, st, a, rec);
-    else launch_pdl(k_adj_stress<ORD, 2, kMaxSls, kTX>, grid, block, st, a, rec);
+    launch_adj_shape<ORD, kAdjTx, ORD == 2 ? 4 : 3>(a, zm, rec, k, st);
 }
 
 void launch_adjoint_step(const AdjState &a, int ord, int zm, const float *rec, int k, cudaStream_t st) {
@@ -421,6 +431,7 @@ struct ts_adj {
     float *coefs = nullptr;     // own copy of L, M, Ms, Bx, By, g_p, g_s
     float *record = nullptr;    // [n_record_steps][kFeat][G]
     int n_record_steps = 0;
+
     float *checkpoints = nullptr;  // [n_ckpt][state_floats]
     Source *src = nullptr;
     float *src_tab = nullptr;
@@ -445,6 +456,17 @@ struct ts_adj {
         return TS_OK;
     }
     float *record_of(int k_in_segment) const { return record + (int64_t)k_in_segment * kFeat * G; }
+    int recompute(int s, cudaStream_t st) {
+        const int k0 = s * ckpt, k1 = std::min(rows, k0 + ckpt);
+        const int rc = copy_state(checkpoints + (int64_t)s * state_floats, false, st);
+        if (rc) return rc;
+        for (int k = k0; k < k1; ++k) forward_step(k, record_of(k - k0), st);
+        return TS_OK;
+    }
+    void sweep(int s, cudaStream_t st) {
+        const int k0 = s * ckpt, k1 = std::min(rows, k0 + ckpt);
+        for (int k = k1 - 1; k >= k0; --k) adjoint_step(k, record_of(k - k0), st);
+    }
     void forward_step(int k, float *rec, cudaStream_t st) {
         sp.feat = rec;
         if (rec) launch_step_2d_feat(sp, ord, zm, k, st);
@@ -590,36 +612,52 @@ int ts_adj_create(const ts_desc *d, int32_t checkpoint_every, ts_adj **out) {
     sp.dtr[1] = as.By = a->coefs + 4 * G;
     sp.g_p = as.gp = a->coefs + 5 * G;
     sp.g_s = as.gs = a->coefs + 6 * G;
-    // sources: every node of the source map, binned by block, column = its
-    // source index; scales (= By at the node) are set by each forward
+    // sources: every node of the source map, column = its source index,
+    // binned by the block that updates it (forward and adjoint block shapes);
+    // scales (= By at the node) are set by each forward
     a->n_blocks = blocks_2d(sp);
+    const int gx = (a->ny + kBX2 - 1) / kBX2;
+    const int n_blocks_adj = gx * ((a->nx + kBY2 * kAdjTx - 1) / (kBY2 * kAdjTx));
     {
-        struct Cand {
-            int blk;
-            Source s;
-        };
-        std::vector<Cand> cands;
+        std::vector<std::pair<int64_t, int>> nodes;   // (cell, column) in (x, y) order
         int ncol = 0;
         for (int x = 0; x < a->nx; ++x)
             for (int y = 0; y < a->ny; ++y) {
                 const int idx = d->pos_sources[(int64_t)x * a->ny + y];
                 if (idx < 0) continue;
-                cands.push_back({block_of_2d(sp, x, y), Source{(int64_t)x * a->P + y, idx, 0.f}});
+                nodes.push_back({(int64_t)x * a->P + y, idx});
                 ncol = std::max(ncol, idx + 1);
             }
-        std::stable_sort(cands.begin(), cands.end(), [](const Cand &p, const Cand &q) { return p.blk < q.blk; });
-        std::vector<Source> list;
-        std::vector<int> start(a->n_blocks + 1, 0);
-        for (const Cand &c : cands) {
-            list.push_back(c.s);
-            start[c.blk + 1]++;
-        }
-        for (int b = 0; b < a->n_blocks; ++b) start[b + 1] += start[b];
-        int *dstart = nullptr;
-        if ((rc = a->upload(&a->src, list)) || (rc = a->upload(&dstart, start))) return bail(rc);
-        a->n_src = (int)list.size();
-        sp.src = as.src = a->src;
-        sp.src_block_start = as.src_block_start = dstart;
+        auto binned = [&](int tx, int n_blocks, Source **dsrc, int **dstart) {
+            struct Cand {
+                int blk;
+                Source s;
+            };
+            std::vector<Cand> cands;
+            for (const auto &nd : nodes) {
+                const int x = (int)(nd.first / a->P), y = (int)(nd.first % a->P);
+                cands.push_back({(x / (kBY2 * tx)) * gx + y / kBX2, Source{nd.first, nd.second, 0.f}});
+            }
+            std::stable_sort(cands.begin(), cands.end(), [](const Cand &p, const Cand &q) { return p.blk < q.blk; });
+            std::vector<Source> list;
+            std::vector<int> start(n_blocks + 1, 0);
+            for (const Cand &c : cands) {
+                list.push_back(c.s);
+                start[c.blk + 1]++;
+            }
+            for (int b = 0; b < n_blocks; ++b) start[b + 1] += start[b];
+            int r = a->upload(dsrc, list);
+            return r ? r : a->upload(dstart, start);
+        };
+        int *dstart = nullptr, *astart = nullptr;
+        Source *asrc = nullptr;
+        if ((rc = binned(kTX, a->n_blocks, &a->src, &dstart)) || (rc = binned(kAdjTx, n_blocks_adj, &asrc, &astart)))
+            return bail(rc);
+        a->n_src = (int)nodes.size();
+        sp.src = a->src;
+        sp.src_block_start = dstart;
+        as.src = asrc;
+        as.src_block_start = astart;
         sp.src_rows = as.src_rows = a->rows;
         sp.src_ncol = as.src_ncol = std::max(1, ncol);
         if ((rc = a->alloc(&a->src_tab, (size_t)a->rows * sp.src_ncol))) return bail(rc);
@@ -632,7 +670,7 @@ int ts_adj_create(const ts_desc *d, int32_t checkpoint_every, ts_adj **out) {
     }
     // receivers: nodes of each receiver in info_rec_pt order (shader_webgpu_viscoelastic.wgsl:1118-1134)
     {
-        if ((int64_t)d->n_rec > (int64_t)a->n_blocks * kBX2 * kBY2)
+        if ((int64_t)d->n_rec > (int64_t)std::min(a->n_blocks, n_blocks_adj) * kBX2 * kBY2)
             return bail(afail(TS_E_ARG, "more receivers than threads of a step launch"));
         std::vector<int> start(1, 0), first(std::max(1, d->n_rec), 0);
         std::vector<int64_t> cells;
@@ -765,12 +803,11 @@ int ts_adj_backward(ts_adj *a, const float *residual, const ts_adj_grads *g, voi
     if (a->ckpt <= 0) {
         for (int k = a->rows - 1; k >= 0; --k) a->adjoint_step(k, a->record_of(k), st);
     } else {
+        // (recomputing segment s-1 on a second stream while segment s is swept
+        // was measured no faster: both passes share the same memory system)
         for (int s = a->n_ckpt - 1; s >= 0; --s) {
-            const int k0 = s * a->ckpt, k1 = std::min(a->rows, k0 + a->ckpt);
-            // recompute the segment from its checkpoint, recording it
-            if ((rc = a->copy_state(a->checkpoints + (int64_t)s * a->state_floats, false, st))) return rc;
-            for (int k = k0; k < k1; ++k) a->forward_step(k, a->record_of(k - k0), st);
-            for (int k = k1 - 1; k >= k0; --k) a->adjoint_step(k, a->record_of(k - k0), st);
+            if ((rc = a->recompute(s, st))) return rc;
+            a->sweep(s, st);
         }
     }
     const cudaError_t e = cudaGetLastError();

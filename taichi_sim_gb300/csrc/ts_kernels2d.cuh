@@ -65,8 +65,8 @@ __device__ __forceinline__ void shift_window(float (&w)[2 * ORD], const float *f
     w[2 * ORD - 1] = (r_new >= 0 && r_new < nx) ? ldg(f + (int64_t)r_new * P + y) : 0.f;
 }
 
-template <int ORD, int FAM, int ZM, int NS, int TX, bool FEAT = false>
-__global__ void __launch_bounds__(kBX2 *kBY2) k_stress2d(const StepParams p) {
+template <int ORD, int FAM, int ZM, int NS, int TX, bool FEAT = false, int MINB = 1>
+__global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams p) {
     const int y = blockIdx.x * kBX2 + threadIdx.x;
     const int x0 = (blockIdx.y * kBY2 + threadIdx.y) * TX;
     if (y >= p.ny || x0 >= p.nx) return;
@@ -230,8 +230,8 @@ __global__ void __launch_bounds__(kBX2 *kBY2) k_stress2d(const StepParams p) {
     pdl_trigger();
 }
 
-template <int ORD, int FAM, int TX, bool FEAT = false>
-__global__ void __launch_bounds__(kBX2 *kBY2) k_velocity2d(const StepParams p, const int j) {
+template <int ORD, int FAM, int TX, bool FEAT = false, int MINB = 1>
+__global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParams p, const int j) {
     const int y = blockIdx.x * kBX2 + threadIdx.x;
     const int x0 = (blockIdx.y * kBY2 + threadIdx.y) * TX;
     const int tid = threadIdx.y * kBX2 + threadIdx.x;

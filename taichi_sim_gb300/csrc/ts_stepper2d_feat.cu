@@ -7,17 +7,25 @@
 namespace ts {
 namespace {
 
-template <int ORD>
-void launch_feat(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
+template <int ORD, int MINB>
+void launch_feat_mb(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
     constexpr int TX = 2;
     const dim3 block(kBX2, kBY2), grid((p.ny + kBX2 - 1) / kBX2, (p.nx + kBY2 * TX - 1) / (kBY2 * TX));
     const bool three = p.zen.n == 3;
-    if (zen_mode == 0) launch_pdl(k_stress2d<ORD, 1, 0, 0, TX, true>, grid, block, st, p);
-    else if (zen_mode == 1 && three) launch_pdl(k_stress2d<ORD, 1, 1, 3, TX, true>, grid, block, st, p);
-    else if (zen_mode == 1) launch_pdl(k_stress2d<ORD, 1, 1, kMaxSls, TX, true>, grid, block, st, p);
-    else if (three) launch_pdl(k_stress2d<ORD, 1, 2, 3, TX, true>, grid, block, st, p);
-    else launch_pdl(k_stress2d<ORD, 1, 2, kMaxSls, TX, true>, grid, block, st, p);
-    launch_pdl(k_velocity2d<ORD, 1, TX, true>, grid, block, st, p, j);
+    if (zen_mode == 0) launch_pdl(k_stress2d<ORD, 1, 0, 0, TX, true, MINB>, grid, block, st, p);
+    else if (zen_mode == 1 && three) launch_pdl(k_stress2d<ORD, 1, 1, 3, TX, true, MINB>, grid, block, st, p);
+    else if (zen_mode == 1) launch_pdl(k_stress2d<ORD, 1, 1, kMaxSls, TX, true, MINB>, grid, block, st, p);
+    else if (three) launch_pdl(k_stress2d<ORD, 1, 2, 3, TX, true, MINB>, grid, block, st, p);
+    else launch_pdl(k_stress2d<ORD, 1, 2, kMaxSls, TX, true, MINB>, grid, block, st, p);
+    launch_pdl(k_velocity2d<ORD, 1, TX, true, MINB>, grid, block, st, p, j);
+}
+
+// Register budget: 4 (ord 2) or 3 (ord 3, 4) resident blocks per SM where
+// that spills nothing (ord 2: about 10 % faster than an unconstrained
+// budget); ord 5, 6 keep the compiler's choice.
+template <int ORD>
+void launch_feat(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
+    launch_feat_mb<ORD, ORD == 2 ? 4 : (ORD <= 4 ? 3 : 1)>(p, zen_mode, j, st);
 }
 
 }  // namespace
