@@ -178,8 +178,10 @@ const char *ts_last_error(void);
  * the attenuation model) plus n_shots[p] shots; shot s of phantom p injects,
  * at every node of the phantom's source map, column idx of its own table
  * shot_sources[p][s][n_steps][src_cols] (idx = the map's value).  Traces
- * are [n_shots][n_steps][n_rec] per phantom.  block_cells (0 = 8) sets the
- * block shape, 32 shots x block_cells nodes; it is fixed at creation.
+ * are [n_shots][n_steps][n_rec] per phantom.  block_cells (0 = 8) and
+ * nodes_per_thread (0 = 2) set the launch shape, blocks of 32 shots x
+ * block_cells nodes along y with each thread updating nodes_per_thread
+ * nodes along x; both are fixed at creation.
  */
 typedef struct ts_batch ts_batch;
 
@@ -189,7 +191,8 @@ typedef struct ts_batch_desc {
     const ts_desc *phantoms;          /* [n_phantoms] */
     const int32_t *n_shots;           /* [n_phantoms] */
     const float *const *shot_sources; /* [n_phantoms] -> [n_shots][n_steps][src_cols] */
-    int32_t block_cells;              /* 0, 4, 8 or 16 */
+    int32_t block_cells;              /* 0, 4 or 8 */
+    int32_t nodes_per_thread;         /* 0, 1, 2 or 4 */
 } ts_batch_desc;
 
 int ts_batch_create(const ts_batch_desc *desc, ts_batch **out);

@@ -1,9 +1,10 @@
 // Batched 2D (visco)elastic stepping: many shots of several phantoms (grids
 // of uneven sizes) advanced together, one launch per kernel per time step.
 //
-// Layout: per phantom every field is [nx][ny][S] with the shot index
-// innermost (S = shots rounded up to 32).  A warp is 32 shots of one grid
-// node, so every load and store is one contiguous 128-byte row, the
+// Layout: per phantom every field is [S/32][nx][ny][32]: blocks of 32 shots
+// (S = shots rounded up to 32), the shot index innermost.  A warp is 32
+// shots of one grid node, so every load and store is one contiguous 128-byte
+// row, neighbouring nodes along y are 128 bytes apart (immediate offsets), the
 // per-node coefficients (lambda*dt, mu*dt, dt/rho, Q scale) are one
 // broadcast load shared by all shots, and the region and CPML-strip tests
 // are uniform across the warp.  Blocks are 32 shots x CY nodes along y;
@@ -40,8 +41,8 @@ struct BSrc {
 
 struct BPh {
     int nx, ny, S, n_shots;
-    int64_t G;  // nx * ny * S
-    int block0, yblocks, sblocks;
+    int G;      // nx * ny * S (checked < 2^31 with the memory variables)
+    int block0, xchunks, yblocks, sblocks;
     float cd[2][kMaxOrd];
     float *v[2], *s[3], *r[3], *psi[8];
     const Cpml *tab_f[2], *tab_h[2];
@@ -57,9 +58,11 @@ struct BPh {
     int rec_work0;
 };
 
+// Passed as a __grid_constant__ kernel parameter: the phantom records are read
+// through the constant cache and cannot alias the fields the kernels write.
 struct BParams {
     int n_ph;
-    const BPh *ph;
+    BPh ph[kMaxPhantoms];
     int block_end[kMaxPhantoms];  // exclusive flat block end per phantom
     Zener zen;
     int rows;
@@ -77,12 +80,13 @@ __device__ __forceinline__ float cpml(float d, float psi_old, float &psi_new, co
 
 struct Loc {
     const BPh *ph;
-    int x, y, s, cell;
-    int64_t i;
+    int x0, y, s, lane, cell0;
+    int i0;
     bool live;
 };
 
-template <int CY>
+// Block b of a launch: phantom, then (x-chunk, y-block, shot-block) within it.
+template <int CY, int TX>
 __device__ __forceinline__ Loc locate(const BParams &p) {
     const int b = blockIdx.x;
     int q = 0;
@@ -94,239 +98,308 @@ __device__ __forceinline__ Loc locate(const BParams &p) {
     const int local = b - h.block0;
     const int sb = local % h.sblocks, t = local / h.sblocks;
     const int yb = t % h.yblocks;
-    L.x = t / h.yblocks;
+    L.x0 = (t / h.yblocks) * TX;
     L.y = yb * CY + threadIdx.y;
-    L.s = sb * 32 + threadIdx.x;
-    L.live = L.y < h.ny;
-    L.cell = L.x * h.ny + L.y;
-    L.i = (int64_t)L.cell * h.S + L.s;
+    L.lane = threadIdx.x;
+    L.s = sb * 32 + L.lane;
+    L.live = L.y < h.ny && L.x0 < h.nx;
+    L.cell0 = L.x0 * h.ny + L.y;
+    L.i0 = ((sb * h.nx + L.x0) * h.ny + L.y) * 32 + L.lane;
     return L;
 }
 
-template <int ORD, int ZM, int NS, int CY>
-__global__ void __launch_bounds__(32 * CY) k_bstress(const BParams p) {
-    const Loc at = locate<CY>(p);
+// Rows r0 .. r0+2*ORD-1 of one field at (y, shot), zero outside the grid.
+template <int ORD>
+__device__ __forceinline__ void bwindow(float (&w)[2 * ORD], const float *f, int r0, int nx, int X, int col) {
+#pragma unroll
+    for (int j = 0; j < 2 * ORD; ++j) {
+        const int r = r0 + j;
+        w[j] = (r >= 0 && r < nx) ? __ldg(f + r * X + col) : 0.f;
+    }
+}
+
+template <int ORD>
+__device__ __forceinline__ void bshift(float (&w)[2 * ORD], const float *f, int r_new, int nx, int X, int col) {
+#pragma unroll
+    for (int j = 0; j < 2 * ORD - 1; ++j) w[j] = w[j + 1];
+    w[2 * ORD - 1] = (r_new >= 0 && r_new < nx) ? __ldg(f + r_new * X + col) : 0.f;
+}
+
+template <int ORD, int ZM, int NS, int CY, int TX>
+__global__ void __launch_bounds__(32 * CY, 32 / CY) k_bstress(const __grid_constant__ BParams p) {
+    const Loc at = locate<CY, TX>(p);
+    if (!at.live) return;
     const BPh &h = *at.ph;
-    const int x = at.x, y = at.y;
-    const bool in_n = at.live && x >= ORD - 1 && x < h.nx - ORD && y >= ORD && y < h.ny - ORD + 1;
-    const bool in_s = at.live && x >= ORD && x < h.nx - ORD + 1 && y >= ORD - 1 && y < h.ny - ORD;
-    if (!in_n && !in_s) return;
-    const int64_t i = at.i, X = (int64_t)h.ny * h.S, Y = h.S;
-    const int sx = strip_index(h.strip[0], x), sy = strip_index(h.strip[1], y);
-    const int64_t ix = ((int64_t)sx * h.ny + y) * h.S + at.s, iy = ((int64_t)x * h.strip[1].width + sy) * h.S + at.s;
+    const int y = at.y, nx = h.nx;
+    constexpr int Y = 32;
+    const int X = h.ny * 32, sb = at.s >> 5, col = (sb * h.nx * h.ny + y) * 32 + at.lane;
+    const bool yn = y >= ORD && y < h.ny - ORD + 1;
+    const bool ys = y >= ORD - 1 && y < h.ny - ORD;
+    const int sy = strip_index(h.strip[1], y);
     const int n_mech = NS == 3 ? 3 : p.zen.n;
     constexpr int R = NS > 0 ? NS : 1;
-
-    float L = 0.f, M = 0.f, Ms = 0.f, gp = 1.f, gs = 1.f;
-    if (in_n) {
-        L = __ldg(h.lam + at.cell);
-        M = __ldg(h.mu + at.cell);
-        if (ZM == 2) gp = __ldg(h.gp + at.cell);
-    }
-    if (in_s) Ms = __ldg(h.mus + at.cell);
-    if (ZM == 2) gs = __ldg(h.gs + at.cell);
+    const float *__restrict__ vx = h.v[0];
+    const float *__restrict__ vy = h.v[1];
+    float *__restrict__ s0 = h.s[0];
+    float *__restrict__ s1 = h.s[1];
+    float *__restrict__ s2 = h.s[2];
+    float *__restrict__ r0 = h.r[0];
+    float *__restrict__ r1 = h.r[1];
+    float *__restrict__ r2 = h.r[2];
     pdl_wait();
-    const float *vx = h.v[0], *vy = h.v[1];
-    float nvx[ORD][2], nvy[ORD][2], svy[ORD][2], svx[ORD][2];
-    float sxx = 0.f, syy = 0.f, sxy = 0.f, pn0 = 0.f, pn1 = 0.f, ps0 = 0.f, ps1 = 0.f;
-    float rxx[R], ryy[R], rxy[R];
-    if (in_n) {
+    // vx rows [x-ORD+1, x+ORD] (normal x-derivative), vy rows [x-ORD, x+ORD-1] (shear)
+    float wvx[2 * ORD], wvy[2 * ORD];
+    bwindow<ORD>(wvx, vx, at.x0 - ORD + 1, nx, X, col);
+    bwindow<ORD>(wvy, vy, at.x0 - ORD, nx, X, col);
 #pragma unroll
-        for (int c = 0; c < ORD; ++c) {
-            nvx[c][0] = __ldg(vx + i + (c + 1) * X);
-            nvx[c][1] = __ldg(vx + i - c * X);
-            nvy[c][0] = __ldg(vy + i + c * Y);
-            nvy[c][1] = __ldg(vy + i - (c + 1) * Y);
-        }
-        sxx = h.s[0][i];
-        syy = h.s[1][i];
-        if (sx >= 0) pn0 = h.psi[0][ix];
-        if (sy >= 0) pn1 = h.psi[2][iy];
-        if (ZM != 0) {
+    for (int t = 0; t < TX; ++t) {
+        const int x = at.x0 + t;
+        if (x >= nx) break;
+        const int cell = at.cell0 + t * h.ny;
+        const int i = at.i0 + t * X;
+        const bool in_n = yn && x >= ORD - 1 && x < nx - ORD;
+        const bool in_s = ys && x >= ORD && x < nx - ORD + 1;
+        if (in_n || in_s) {
+            const int sx = strip_index(h.strip[0], x);
+            const int ix = ((sb * h.strip[0].width + sx) * h.ny + y) * 32 + at.lane;
+            const int iy = ((sb * h.nx + x) * h.strip[1].width + sy) * 32 + at.lane;
+            // ---- loads ----
+            float L = 0.f, M = 0.f, Ms = 0.f, gp = 1.f, gs = 1.f, sxx = 0.f, syy = 0.f, sxy = 0.f;
+            float ny_lo[ORD], ny_hi[ORD], sx_lo[ORD], sx_hi[ORD];
+            float rxx[R], ryy[R], rxy[R];
+            float pn0 = 0.f, pn1 = 0.f, ps0 = 0.f, ps1 = 0.f;
+            if (in_n) {
+                L = __ldg(h.lam + cell);
+                M = __ldg(h.mu + cell);
+                if (ZM == 2) gp = __ldg(h.gp + cell);
 #pragma unroll
-            for (int l = 0; l < R; ++l)
-                if (l < n_mech) {
-                    rxx[l] = h.r[0][l * h.G + i];
-                    ryy[l] = h.r[1][l * h.G + i];
+                for (int c = 0; c < ORD; ++c) {
+                    ny_hi[c] = __ldg(vy + i + c * Y);         // vy[y+c]
+                    ny_lo[c] = __ldg(vy + i - (c + 1) * Y);   // vy[y-c-1]
                 }
-        }
-    }
-    if (in_s) {
+                sxx = s0[i];
+                syy = s1[i];
+                if (sx >= 0) pn0 = h.psi[0][ix];
+                if (sy >= 0) pn1 = h.psi[2][iy];
+                if (ZM != 0) {
 #pragma unroll
-        for (int c = 0; c < ORD; ++c) {
-            svy[c][0] = __ldg(vy + i + c * X);
-            svy[c][1] = __ldg(vy + i - (c + 1) * X);
-            svx[c][0] = __ldg(vx + i + (c + 1) * Y);
-            svx[c][1] = __ldg(vx + i - c * Y);
-        }
-        sxy = h.s[2][i];
-        if (sx >= 0) ps0 = h.psi[1][ix];
-        if (sy >= 0) ps1 = h.psi[3][iy];
-        if (ZM != 0) {
-#pragma unroll
-            for (int l = 0; l < R; ++l)
-                if (l < n_mech) rxy[l] = h.r[2][l * h.G + i];
-        }
-    }
-    if (in_n) {
-        float ddx = 0.f, ddy = 0.f, np_;
-#pragma unroll
-        for (int c = 0; c < ORD; ++c) {
-            ddx = fmaf(h.cd[0][c], nvx[c][0] - nvx[c][1], ddx);
-            ddy = fmaf(h.cd[1][c], nvy[c][0] - nvy[c][1], ddy);
-        }
-        if (sx >= 0) {
-            ddx = cpml(ddx, pn0, np_, h.tab_h[0][x]);
-            h.psi[0][ix] = np_;
-        }
-        if (sy >= 0) {
-            ddy = cpml(ddy, pn1, np_, h.tab_f[1][y]);
-            h.psi[2][iy] = np_;
-        }
-        const float L2M = fmaf(2.f, M, L);
-        float ux = fmaf(L2M, ddx, L * ddy), uy = fmaf(L, ddx, L2M * ddy);
-        if (ZM != 0) {
-            float srxx = 0.f, sryy = 0.f;
-            const float dsum = ddx + ddy, ddif = 0.5f * (ddx - ddy);
-#pragma unroll
-            for (int l = 0; l < R; ++l)
-                if (l < n_mech) {
-                    const float a = fmaf(p.zen.Ap[l], rxx[l], (p.zen.Bp[l] * gp) * dsum);
-                    const float b = fmaf(p.zen.As[l], ryy[l], (p.zen.Bs[l] * gs) * ddif);
-                    srxx += rxx[l] + a;
-                    sryy += ryy[l] + b;
-                    h.r[0][l * h.G + i] = a;
-                    h.r[1][l * h.G + i] = b;
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) {
+                            rxx[l] = r0[l * h.G + i];
+                            ryy[l] = r1[l * h.G + i];
+                        }
                 }
-            const float hl = 0.5f * (L + M);
-            ux = fmaf(hl, srxx, fmaf(M, sryy, ux));
-            uy = fmaf(hl, srxx, fmaf(-M, sryy, uy));
-        }
-        h.s[0][i] = sxx + ux;
-        h.s[1][i] = syy + uy;
-    }
-    if (in_s) {
-        float a = 0.f, b = 0.f, np_;
+            }
+            if (in_s) {
+                Ms = __ldg(h.mus + cell);
 #pragma unroll
-        for (int c = 0; c < ORD; ++c) {
-            a = fmaf(h.cd[0][c], svy[c][0] - svy[c][1], a);
-            b = fmaf(h.cd[1][c], svx[c][0] - svx[c][1], b);
-        }
-        if (sx >= 0) {
-            a = cpml(a, ps0, np_, h.tab_f[0][x]);
-            h.psi[1][ix] = np_;
-        }
-        if (sy >= 0) {
-            b = cpml(b, ps1, np_, h.tab_h[1][y]);
-            h.psi[3][iy] = np_;
-        }
-        const float e = a + b;
-        float u = Ms * e;
-        if (ZM != 0) {
-            float sr = 0.f;
-#pragma unroll
-            for (int l = 0; l < R; ++l)
-                if (l < n_mech) {
-                    const float n_ = fmaf(p.zen.As[l], rxy[l], (p.zen.Bs[l] * gs) * e);
-                    sr += rxy[l] + n_;
-                    h.r[2][l * h.G + i] = n_;
+                for (int c = 0; c < ORD; ++c) {
+                    sx_hi[c] = __ldg(vx + i + (c + 1) * Y);   // vx[y+c+1]
+                    sx_lo[c] = __ldg(vx + i - c * Y);         // vx[y-c]
                 }
-            u = fmaf(0.5f * Ms, sr, u);
+                sxy = s2[i];
+                if (sx >= 0) ps0 = h.psi[1][ix];
+                if (sy >= 0) ps1 = h.psi[3][iy];
+                if (ZM != 0) {
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) rxy[l] = r2[l * h.G + i];
+                }
+            }
+            if (ZM == 2) gs = __ldg(h.gs + cell);
+            // ---- normal stresses ----
+            if (in_n) {
+                float ddx = 0.f, ddy = 0.f, np_;
+#pragma unroll
+                for (int c = 0; c < ORD; ++c) {
+                    ddx = fmaf(h.cd[0][c], wvx[c + ORD] - wvx[ORD - 1 - c], ddx);
+                    ddy = fmaf(h.cd[1][c], ny_hi[c] - ny_lo[c], ddy);
+                }
+                if (sx >= 0) {
+                    ddx = cpml(ddx, pn0, np_, h.tab_h[0][x]);
+                    h.psi[0][ix] = np_;
+                }
+                if (sy >= 0) {
+                    ddy = cpml(ddy, pn1, np_, h.tab_f[1][y]);
+                    h.psi[2][iy] = np_;
+                }
+                const float L2M = fmaf(2.f, M, L);
+                float ux = fmaf(L2M, ddx, L * ddy), uy = fmaf(L, ddx, L2M * ddy);
+                if (ZM != 0) {
+                    float srxx = 0.f, sryy = 0.f;
+                    const float dsum = ddx + ddy, ddif = 0.5f * (ddx - ddy);
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) {
+                            const float a = fmaf(p.zen.Ap[l], rxx[l], (p.zen.Bp[l] * gp) * dsum);
+                            const float b = fmaf(p.zen.As[l], ryy[l], (p.zen.Bs[l] * gs) * ddif);
+                            srxx += rxx[l] + a;
+                            sryy += ryy[l] + b;
+                            r0[l * h.G + i] = a;
+                            r1[l * h.G + i] = b;
+                        }
+                    const float hl = 0.5f * (L + M);
+                    ux = fmaf(hl, srxx, fmaf(M, sryy, ux));
+                    uy = fmaf(hl, srxx, fmaf(-M, sryy, uy));
+                }
+                s0[i] = sxx + ux;
+                s1[i] = syy + uy;
+            }
+            // ---- shear stress ----
+            if (in_s) {
+                float a = 0.f, b = 0.f, np_;
+#pragma unroll
+                for (int c = 0; c < ORD; ++c) {
+                    a = fmaf(h.cd[0][c], wvy[c + ORD] - wvy[ORD - 1 - c], a);
+                    b = fmaf(h.cd[1][c], sx_hi[c] - sx_lo[c], b);
+                }
+                if (sx >= 0) {
+                    a = cpml(a, ps0, np_, h.tab_f[0][x]);
+                    h.psi[1][ix] = np_;
+                }
+                if (sy >= 0) {
+                    b = cpml(b, ps1, np_, h.tab_h[1][y]);
+                    h.psi[3][iy] = np_;
+                }
+                const float e = a + b;
+                float u = Ms * e;
+                if (ZM != 0) {
+                    float sr = 0.f;
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) {
+                            const float n_ = fmaf(p.zen.As[l], rxy[l], (p.zen.Bs[l] * gs) * e);
+                            sr += rxy[l] + n_;
+                            r2[l * h.G + i] = n_;
+                        }
+                    u = fmaf(0.5f * Ms, sr, u);
+                }
+                s2[i] = sxy + u;
+            }
         }
-        h.s[2][i] = sxy + u;
+        if (t + 1 < TX) {
+            bshift<ORD>(wvx, vx, x + ORD + 1, nx, X, col);
+            bshift<ORD>(wvy, vy, x + ORD, nx, X, col);
+        }
     }
     pdl_trigger();
 }
 
-template <int ORD, int CY>
-__global__ void __launch_bounds__(32 * CY) k_bvelocity(const BParams p, const int j) {
-    const Loc at = locate<CY>(p);
+template <int ORD, int CY, int TX>
+__global__ void __launch_bounds__(32 * CY, 32 / CY) k_bvelocity(const __grid_constant__ BParams p, const int j) {
+    const Loc at = locate<CY, TX>(p);
     const BPh &h = *at.ph;
-    const int x = at.x, y = at.y;
-    const int64_t i = at.i, X = (int64_t)h.ny * h.S, Y = h.S;
-    const bool in_vy = at.live && x >= ORD - 1 && x < h.nx - ORD && y >= ORD - 1 && y < h.ny - ORD;
-    const bool in_vx = in_vy && x >= ORD && y >= ORD;
-    const int sx = strip_index(h.strip[0], x), sy = strip_index(h.strip[1], y);
-    const int64_t ix = ((int64_t)sx * h.ny + y) * h.S + at.s, iy = ((int64_t)x * h.strip[1].width + sy) * h.S + at.s;
+    const int y = at.y, nx = h.nx;
+    constexpr int Y = 32;
+    const int X = h.ny * 32, sb = at.s >> 5, col = (sb * h.nx * h.ny + y) * 32 + at.lane;
+    const bool yvy = y >= ORD - 1 && y < h.ny - ORD;
+    const bool yvx = yvy && y >= ORD;
+    const int sy = at.live ? strip_index(h.strip[1], y) : -1;
     const int yb = y / CY;
-    const int q0 = __ldg(h.src_start + x * h.yblocks + yb), q1 = __ldg(h.src_start + x * h.yblocks + yb + 1);
-    const float dx0 = in_vx ? __ldg(h.dtr0 + at.cell) : 0.f;
-    const float dy0 = in_vy ? __ldg(h.dtr1 + at.cell) : 0.f;
     pdl_wait();
     const int k = *p.step_base + j;
-    const float *sxx = h.s[0], *syy = h.s[1], *sxy = h.s[2];
-    float ax[ORD][2], bx[ORD][2], ay[ORD][2], by[ORD][2];
-    float vx0 = 0.f, vy0 = 0.f, pxa = 0.f, pxb = 0.f, pya = 0.f, pyb = 0.f;
-    if (in_vx) {
-#pragma unroll
-        for (int c = 0; c < ORD; ++c) {
-            ax[c][0] = __ldg(sxx + i + c * X);
-            ax[c][1] = __ldg(sxx + i - (c + 1) * X);
-            bx[c][0] = __ldg(sxy + i + c * Y);
-            bx[c][1] = __ldg(sxy + i - (c + 1) * Y);
-        }
-        vx0 = h.v[0][i];
-        if (sx >= 0) pxa = h.psi[4][ix];
-        if (sy >= 0) pxb = h.psi[6][iy];
-    }
-    if (in_vy) {
-#pragma unroll
-        for (int c = 0; c < ORD; ++c) {
-            ay[c][0] = __ldg(sxy + i + (c + 1) * X);
-            ay[c][1] = __ldg(sxy + i - c * X);
-            by[c][0] = __ldg(syy + i + (c + 1) * Y);
-            by[c][1] = __ldg(syy + i - c * Y);
-        }
-        vy0 = h.v[1][i];
-        if (sx >= 0) pya = h.psi[5][ix];
-        if (sy >= 0) pyb = h.psi[7][iy];
-    }
-    float v2 = 0.f;
+    const float *__restrict__ sxx = h.s[0];
+    const float *__restrict__ syy = h.s[1];
+    const float *__restrict__ sxy = h.s[2];
+    float *__restrict__ v0 = h.v[0];
+    float *__restrict__ v1 = h.v[1];
+    float vmax = 0.f;
+    bool bad = false;
     if (at.live) {
-        float vxn = 0.f, vyn = 0.f, np_;
-        if (in_vx) {
-            float a = 0.f, b = 0.f;
+        // sxx rows [x-ORD, x+ORD-1] (vx), sxy rows [x-ORD+1, x+ORD] (vy)
+        float wxx[2 * ORD], wxy[2 * ORD];
+        bwindow<ORD>(wxx, sxx, at.x0 - ORD, nx, X, col);
+        bwindow<ORD>(wxy, sxy, at.x0 - ORD + 1, nx, X, col);
 #pragma unroll
-            for (int c = 0; c < ORD; ++c) {
-                a = fmaf(h.cd[0][c], ax[c][0] - ax[c][1], a);
-                b = fmaf(h.cd[1][c], bx[c][0] - bx[c][1], b);
-            }
-            if (sx >= 0) {
-                a = cpml(a, pxa, np_, h.tab_f[0][x]);
-                h.psi[4][ix] = np_;
-            }
-            if (sy >= 0) {
-                b = cpml(b, pxb, np_, h.tab_f[1][y]);
-                h.psi[6][iy] = np_;
-            }
-            vxn = fmaf(a + b, dx0, vx0);
-        }
-        if (in_vy) {
-            float a = 0.f, b = 0.f;
+        for (int t = 0; t < TX; ++t) {
+            const int x = at.x0 + t;
+            if (x >= nx) break;
+            const int cell = at.cell0 + t * h.ny;
+            const int i = at.i0 + t * X;
+            const bool in_vy = yvy && x >= ORD - 1 && x < nx - ORD;
+            const bool in_vx = yvx && in_vy && x >= ORD;
+            const int sx = strip_index(h.strip[0], x);
+            const int ix = ((sb * h.strip[0].width + sx) * h.ny + y) * 32 + at.lane;
+            const int iy = ((sb * h.nx + x) * h.strip[1].width + sy) * 32 + at.lane;
+            // ---- loads ----
+            float bx_hi[ORD], bx_lo[ORD], by_hi[ORD], by_lo[ORD];
+            float vx0 = 0.f, vy0 = 0.f, dx0 = 0.f, dy0 = 0.f, pxa = 0.f, pxb = 0.f, pya = 0.f, pyb = 0.f;
+            if (in_vx) {
 #pragma unroll
-            for (int c = 0; c < ORD; ++c) {
-                a = fmaf(h.cd[0][c], ay[c][0] - ay[c][1], a);
-                b = fmaf(h.cd[1][c], by[c][0] - by[c][1], b);
+                for (int c = 0; c < ORD; ++c) {
+                    bx_hi[c] = __ldg(sxy + i + c * Y);         // sxy[y+c]
+                    bx_lo[c] = __ldg(sxy + i - (c + 1) * Y);   // sxy[y-c-1]
+                }
+                vx0 = v0[i];
+                dx0 = __ldg(h.dtr0 + cell);
+                if (sx >= 0) pxa = h.psi[4][ix];
+                if (sy >= 0) pxb = h.psi[6][iy];
             }
-            if (sx >= 0) {
-                a = cpml(a, pya, np_, h.tab_h[0][x]);
-                h.psi[5][ix] = np_;
+            if (in_vy) {
+#pragma unroll
+                for (int c = 0; c < ORD; ++c) {
+                    by_hi[c] = __ldg(syy + i + (c + 1) * Y);   // syy[y+c+1]
+                    by_lo[c] = __ldg(syy + i - c * Y);         // syy[y-c]
+                }
+                vy0 = v1[i];
+                dy0 = __ldg(h.dtr1 + cell);
+                if (sx >= 0) pya = h.psi[5][ix];
+                if (sy >= 0) pyb = h.psi[7][iy];
             }
-            if (sy >= 0) {
-                b = cpml(b, pyb, np_, h.tab_h[1][y]);
-                h.psi[7][iy] = np_;
+            const int q0 = __ldg(h.src_start + x * h.yblocks + yb), q1 = __ldg(h.src_start + x * h.yblocks + yb + 1);
+            // ---- update ----
+            float vxn = 0.f, vyn = 0.f, np_;
+            if (in_vx) {
+                float a = 0.f, b = 0.f;
+#pragma unroll
+                for (int c = 0; c < ORD; ++c) {
+                    a = fmaf(h.cd[0][c], wxx[c + ORD] - wxx[ORD - 1 - c], a);
+                    b = fmaf(h.cd[1][c], bx_hi[c] - bx_lo[c], b);
+                }
+                if (sx >= 0) {
+                    a = cpml(a, pxa, np_, h.tab_f[0][x]);
+                    h.psi[4][ix] = np_;
+                }
+                if (sy >= 0) {
+                    b = cpml(b, pxb, np_, h.tab_f[1][y]);
+                    h.psi[6][iy] = np_;
+                }
+                vxn = fmaf(a + b, dx0, vx0);
             }
-            vyn = fmaf(a + b, dy0, vy0);
+            if (in_vy) {
+                float a = 0.f, b = 0.f;
+#pragma unroll
+                for (int c = 0; c < ORD; ++c) {
+                    a = fmaf(h.cd[0][c], wxy[c + ORD] - wxy[ORD - 1 - c], a);
+                    b = fmaf(h.cd[1][c], by_hi[c] - by_lo[c], b);
+                }
+                if (sx >= 0) {
+                    a = cpml(a, pya, np_, h.tab_h[0][x]);
+                    h.psi[5][ix] = np_;
+                }
+                if (sy >= 0) {
+                    b = cpml(b, pyb, np_, h.tab_h[1][y]);
+                    h.psi[7][iy] = np_;
+                }
+                vyn = fmaf(a + b, dy0, vy0);
+            }
+            if (at.s < h.n_shots && k < p.rows)
+                for (int q = q0; q < q1; ++q) {
+                    const BSrc s = h.src[q];
+                    if (s.cell == cell)
+                        vyn = fmaf(__ldg(h.shot_tab + ((int64_t)at.s * p.rows + k) * h.ncol + s.col), s.scale, vyn);
+                }
+            v0[i] = vxn;
+            v1[i] = vyn;
+            const float v2 = fmaf(vxn, vxn, vyn * vyn);
+            bad |= !(v2 <= p.v2_threshold);
+            vmax = fmaxf(vmax, v2);
+            if (v2 != v2) vmax = v2;  // keep a NaN visible
+            if (t + 1 < TX) {
+                bshift<ORD>(wxx, sxx, x + ORD, nx, X, col);
+                bshift<ORD>(wxy, sxy, x + ORD + 1, nx, X, col);
+            }
         }
-        if (at.s < h.n_shots && k < p.rows)
-            for (int q = q0; q < q1; ++q) {
-                const BSrc s = h.src[q];
-                if (s.cell == at.cell)
-                    vyn = fmaf(__ldg(h.shot_tab + ((int64_t)at.s * p.rows + k) * h.ncol + s.col), s.scale, vyn);
-            }
-        h.v[0][i] = vxn;
-        h.v[1][i] = vyn;
-        v2 = fmaf(vxn, vxn, vyn * vyn);
     }
     // receivers: flat work item g = (phantom, shot, receiver)
     const int g = blockIdx.x * (32 * CY) + threadIdx.y * 32 + threadIdx.x;
@@ -338,41 +411,45 @@ __global__ void __launch_bounds__(32 * CY) k_bvelocity(const BParams p, const in
         if (k >= __ldg(r.rec_first + rec)) {
             float acc = 0.f;
             for (int t = __ldg(r.rec_start + rec); t < __ldg(r.rec_start + rec + 1); ++t)
-                acc += r.s[1][(int64_t)__ldg(r.rec_cell + t) * r.S + shot];
+                acc += r.s[1][((shot >> 5) * r.nx * r.ny + __ldg(r.rec_cell + t)) * 32 + (shot & 31)];
             r.traces[((int64_t)shot * p.rows + k) * r.n_rec + rec] = acc;
         }
     }
-    warp_stability(v2, at.live && !(v2 <= p.v2_threshold), reinterpret_cast<unsigned *>(p.block_max) + blockIdx.x,
-                   p.first_bad, k);
+    warp_stability(vmax, bad, reinterpret_cast<unsigned *>(p.block_max) + blockIdx.x, p.first_bad, k);
     pdl_trigger();
 }
 
-template <int ORD, int CY>
-void launch_cy(const BParams &p, int n_blocks, int zen_mode, int j, cudaStream_t st, int parts) {
+template <int ORD, int CY, int TX>
+void launch_shape(const BParams &p, int n_blocks, int zen_mode, int j, cudaStream_t st, int parts) {
     const dim3 block(32, CY), grid(n_blocks);
     const bool three = p.zen.n == 3;
+
     if (parts & 1) {
-        if (zen_mode == 0) launch_pdl(k_bstress<ORD, 0, 0, CY>, grid, block, st, p);
-        else if (zen_mode == 1 && three) launch_pdl(k_bstress<ORD, 1, 3, CY>, grid, block, st, p);
-        else if (zen_mode == 1) launch_pdl(k_bstress<ORD, 1, kMaxSls, CY>, grid, block, st, p);
-        else if (three) launch_pdl(k_bstress<ORD, 2, 3, CY>, grid, block, st, p);
-        else launch_pdl(k_bstress<ORD, 2, kMaxSls, CY>, grid, block, st, p);
+        if (zen_mode == 0) launch_pdl(k_bstress<ORD, 0, 0, CY, TX>, grid, block, st, p);
+        else if (zen_mode == 1 && three) launch_pdl(k_bstress<ORD, 1, 3, CY, TX>, grid, block, st, p);
+        else if (zen_mode == 1) launch_pdl(k_bstress<ORD, 1, kMaxSls, CY, TX>, grid, block, st, p);
+        else if (three) launch_pdl(k_bstress<ORD, 2, 3, CY, TX>, grid, block, st, p);
+        else launch_pdl(k_bstress<ORD, 2, kMaxSls, CY, TX>, grid, block, st, p);
     }
-    if (parts & 2) launch_pdl(k_bvelocity<ORD, CY>, grid, block, st, p, j);
+    if (parts & 2) launch_pdl(k_bvelocity<ORD, CY, TX>, grid, block, st, p, j);
 }
 
+// Block shapes: 32 shots x CY nodes along y, TX nodes per thread along x.
 template <int ORD>
-void launch_ord(const BParams &p, int n_blocks, int cy, int zen_mode, int j, cudaStream_t st, int parts) {
-    if (cy == 4) launch_cy<ORD, 4>(p, n_blocks, zen_mode, j, st, parts);
-    else if (cy == 16) launch_cy<ORD, 16>(p, n_blocks, zen_mode, j, st, parts);
-    else launch_cy<ORD, 8>(p, n_blocks, zen_mode, j, st, parts);
+void launch_ord(const BParams &p, int n_blocks, int cy, int tx, int zen_mode, int j, cudaStream_t st, int parts) {
+    if (cy == 4 && tx == 1) launch_shape<ORD, 4, 1>(p, n_blocks, zen_mode, j, st, parts);
+    else if (cy == 4 && tx == 2) launch_shape<ORD, 4, 2>(p, n_blocks, zen_mode, j, st, parts);
+    else if (cy == 4) launch_shape<ORD, 4, 4>(p, n_blocks, zen_mode, j, st, parts);
+    else if (cy == 8 && tx == 1) launch_shape<ORD, 8, 1>(p, n_blocks, zen_mode, j, st, parts);
+    else if (cy == 8 && tx == 2) launch_shape<ORD, 8, 2>(p, n_blocks, zen_mode, j, st, parts);
+    else launch_shape<ORD, 8, 4>(p, n_blocks, zen_mode, j, st, parts);
 }
 
-void launch_batch(const BParams &p, int n_blocks, int ord, int cy, int zen_mode, int j, cudaStream_t st,
+void launch_batch(const BParams &p, int n_blocks, int ord, int cy, int tx, int zen_mode, int j, cudaStream_t st,
                   int parts = 3) {
     switch (ord) {
-    case 2: launch_ord<2>(p, n_blocks, cy, zen_mode, j, st, parts); break;
-    case 4: launch_ord<4>(p, n_blocks, cy, zen_mode, j, st, parts); break;
+    case 2: launch_ord<2>(p, n_blocks, cy, tx, zen_mode, j, st, parts); break;
+    case 4: launch_ord<4>(p, n_blocks, cy, tx, zen_mode, j, st, parts); break;
     default: break;
     }
 }
@@ -390,17 +467,15 @@ int bfail(int code, const std::string &m) {
 using namespace ts;
 
 struct ts_batch {
-    int device = 0, ord = 2, cy = 8, zen_mode = 0, rows = 0;
+    int device = 0, ord = 2, cy = 8, tx = 2, zen_mode = 0, rows = 0;
     int n_blocks = 0, steps_done = 0, n_ph = 0;
     int64_t launches = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     cudaGraphExec_t graph = nullptr;
-    int graph_cy = 0;
     std::vector<void *> allocs;
     std::vector<std::pair<void *, size_t>> state;
     std::vector<BPh> ph;
-    BPh *d_ph = nullptr;
     BParams p{};
     std::vector<int> shots, nrec, ncol, cells;
 
@@ -460,8 +535,11 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
     if (bd->abi_version != TS_ABI_VERSION) return bfail(TS_E_ARG, "abi_version mismatch");
     if (bd->n_phantoms < 1 || bd->n_phantoms > kMaxPhantoms) return bfail(TS_E_ARG, "n_phantoms must be in [1, 8]");
     if (!bd->phantoms || !bd->n_shots || !bd->shot_sources) return bfail(TS_E_ARG, "missing phantom tables");
-    if (!(bd->block_cells == 0 || bd->block_cells == 4 || bd->block_cells == 8 || bd->block_cells == 16))
-        return bfail(TS_E_ARG, "block_cells must be 0 (default), 4, 8 or 16");
+    if (!(bd->block_cells == 0 || bd->block_cells == 4 || bd->block_cells == 8))
+        return bfail(TS_E_ARG, "block_cells must be 0 (default), 4 or 8");
+    if (!(bd->nodes_per_thread == 0 || bd->nodes_per_thread == 1 || bd->nodes_per_thread == 2 ||
+          bd->nodes_per_thread == 4))
+        return bfail(TS_E_ARG, "nodes_per_thread must be 0 (default), 1, 2 or 4");
     const ts_desc *d0 = bd->phantoms;
     for (int q = 0; q < bd->n_phantoms; ++q) {
         const ts_desc *d = bd->phantoms + q;
@@ -496,6 +574,7 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
     b->rows = d0->n_steps;
     b->n_ph = bd->n_phantoms;
     b->cy = bd->block_cells ? bd->block_cells : 8;
+    b->tx = bd->nodes_per_thread ? bd->nodes_per_thread : 2;
     b->zen_mode = !d0->visco ? 0 : (d0->g_p ? 2 : 1);
     b->ph.resize(b->n_ph);
     int block0 = 0, rec0 = 0, rc;
@@ -507,11 +586,14 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
         h.ny = d->ny;
         h.n_shots = bd->n_shots[q];
         h.S = round_up(h.n_shots, 32);
-        h.G = (int64_t)h.nx * h.ny * h.S;
+        if ((int64_t)h.nx * h.ny * h.S * std::max(1, d->visco ? d->n_sls : 1) >= (int64_t)1 << 31)
+            return bail(bfail(TS_E_ARG, "phantom too large for one batch (nodes x shots x mechanisms >= 2^31)"));
+        h.G = h.nx * h.ny * h.S;
         h.yblocks = (h.ny + b->cy - 1) / b->cy;
         h.sblocks = h.S / 32;
+        h.xchunks = (h.nx + b->tx - 1) / b->tx;
         h.block0 = block0;
-        block0 += h.nx * h.yblocks * h.sblocks;
+        block0 += h.xchunks * h.yblocks * h.sblocks;
         const float steps[2] = {d->dx, d->dy};
         for (int a = 0; a < 2; ++a)
             for (int c = 0; c < kMaxOrd; ++c) h.cd[a][c] = c < d->ord ? d->coefs[c] / steps[a] : 0.f;
@@ -534,7 +616,7 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
             if ((rc = b->alloc(&h.psi[k], psz[k], true))) return bail(rc);
         if (d->visco)
             for (int m = 0; m < 3; ++m)
-                if ((rc = b->alloc(&h.r[m], h.G * d->n_sls, true))) return bail(rc);
+                if ((rc = b->alloc(&h.r[m], (size_t)h.G * d->n_sls, true))) return bail(rc);
         // per-node coefficients, shared by every shot
         const int64_t cells = (int64_t)h.nx * h.ny;
         std::vector<float> lam(cells), mu(cells), mus(cells), dtr0(cells), dtr1(cells), rho_vy(cells);
@@ -619,11 +701,13 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
         b->cells.push_back(h.nx * h.ny);
     }
     b->n_blocks = block0;
-    if ((rc = b->upload(&b->d_ph, b->ph))) return bail(rc);
     BParams &p = b->p;
     p.n_ph = b->n_ph;
-    p.ph = b->d_ph;
-    for (int q = 0; q < kMaxPhantoms; ++q) p.block_end[q] = q < b->n_ph ? b->ph[q].block0 + (b->ph[q].nx * b->ph[q].yblocks * b->ph[q].sblocks) : block0;
+    for (int q = 0; q < b->n_ph; ++q) p.ph[q] = b->ph[q];
+    for (int q = 0; q < kMaxPhantoms; ++q)
+        p.block_end[q] = q < b->n_ph ? b->ph[q].block0 + b->ph[q].xchunks * b->ph[q].yblocks * b->ph[q].sblocks : block0;
+    if ((int64_t)rec0 > (int64_t)block0 * 32 * b->cy)
+        return bail(bfail(TS_E_ARG, "more (shot, receiver) pairs than threads of a step launch"));
     p.zen = zener_constants(d0);
     p.rows = b->rows;
     p.v2_threshold = FLT_MAX;
@@ -648,10 +732,10 @@ int ts_batch_run(ts_batch *b, int32_t n_steps, void *stream) {
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : b->stream;
     constexpr int G = 16;
     auto steps = [&](int count, cudaStream_t where) {
-        for (int j = 0; j < count; ++j) launch_batch(b->p, b->n_blocks, b->ord, b->cy, b->zen_mode, j, where);
+        for (int j = 0; j < count; ++j) launch_batch(b->p, b->n_blocks, b->ord, b->cy, b->tx, b->zen_mode, j, where);
         launch_advance(const_cast<int *>(b->p.step_base), count, where);
     };
-    if ((!b->graph || b->graph_cy != b->cy) && n_steps >= G) {
+    if (!b->graph && n_steps >= G) {
         if (b->graph) cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
         cudaGraph_t g = nullptr;
@@ -662,7 +746,6 @@ int ts_batch_run(ts_batch *b, int32_t n_steps, void *stream) {
         cudaError_t e = cudaGraphInstantiate(&b->graph, g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return bfail(TS_E_CUDA, std::string("graph: ") + cudaGetErrorString(e));
-        b->graph_cy = b->cy;
     }
     int left = n_steps;
     while (left >= G && b->graph) {
@@ -722,13 +805,13 @@ int ts_batch_read_field(ts_batch *b, int32_t phantom, int32_t what, void *dst, s
     cudaEventSynchronize(b->done);
     const size_t need = (size_t)h.nx * h.ny * h.n_shots * 4;
     if (bytes < need) return bfail(TS_E_ARG, "destination too small");
-    // device layout [nx][ny][S] -> host [n_shots][nx][ny]
+    // device layout [S/32][nx][ny][32] -> host [n_shots][nx][ny]
     std::vector<float> tmp((size_t)h.G);
     if (cudaMemcpy(tmp.data(), src, tmp.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return bfail(TS_E_CUDA, "cudaMemcpy");
     float *o = static_cast<float *>(dst);
     const int64_t cells = (int64_t)h.nx * h.ny;
     for (int s = 0; s < h.n_shots; ++s)
-        for (int64_t c = 0; c < cells; ++c) o[s * cells + c] = tmp[c * h.S + s];
+        for (int64_t c = 0; c < cells; ++c) o[s * cells + c] = tmp[((s >> 5) * cells + c) * 32 + (s & 31)];
     return TS_OK;
 }
 
@@ -741,7 +824,7 @@ int ts_batch_profile_steps(ts_batch *b, int32_t n_steps, void *stream, float *ms
     cudaEventRecord(ev[0], st);
     for (int j = 0; j < n_steps; ++j)
         for (int part = 0; part < 2; ++part) {
-            launch_batch(b->p, b->n_blocks, b->ord, b->cy, b->zen_mode, j, st, 1 << part);
+            launch_batch(b->p, b->n_blocks, b->ord, b->cy, b->tx, b->zen_mode, j, st, 1 << part);
             cudaEventRecord(ev[2 * j + part + 1], st);
         }
     launch_advance(const_cast<int *>(b->p.step_base), n_steps, st);

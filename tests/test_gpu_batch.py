@@ -38,11 +38,11 @@ def _single_shot(sim, table):
     return st
 
 
-@pytest.mark.parametrize("block_cells", [4, 8, 16])
-def test_batch_matches_single_shots(block_cells):
+@pytest.mark.parametrize("shape", [(4, 1), (4, 2), (8, 2), (8, 4)], ids=lambda s: f"{s[0]}x{s[1]}")
+def test_batch_matches_single_shots(shape):
     sims = _phantoms()
     shots = [fmc_shot_sources(s) for s in sims]
-    with BatchStepper(sims, shots, block_cells=block_cells) as b:
+    with BatchStepper(sims, shots, block_cells=shape[0], nodes_per_thread=shape[1]) as b:
         b.run(sims[0]._n_steps)
         n, vmax, bad = b.status()
         assert n == sims[0]._n_steps and bad == -1
@@ -80,6 +80,6 @@ def test_autotuner_picks_and_caches(tmp_path, monkeypatch):
     sims = _phantoms(steps=40)
     shots = [fmc_shot_sources(s) for s in sims]
     best, timings = autotune(sims, shots, steps=4)
-    assert best in (4, 8, 16) and set(timings) == {4, 8, 16}
+    assert best in batch.SHAPES and set(timings) == {f"{cy}x{tx}" for cy, tx in batch.SHAPES}
     again, _ = autotune(sims, shots, steps=4)
     assert again == best and (tmp_path / "autotune.json").exists()
