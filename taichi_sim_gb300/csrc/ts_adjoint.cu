@@ -93,13 +93,14 @@ __device__ __forceinline__ float cpml_adj(float dt_bar, float &pbar, const Cpml 
     return fmaf(t.ik, dt_bar, t.a * q);
 }
 
-// f[row + yy], zero outside [0, ny) (no wrap into the neighbouring row)
+// f[row + yy], zero outside [0, ny) (no wrap into the neighbouring row); f
+// is written by the previous kernel of the stream: a coherent load
 __device__ __forceinline__ float ld_y(const float *f, int64_t row, int yy, int ny) {
-    return (yy >= 0 && yy < ny) ? __ldg(f + row + yy) : 0.f;
+    return (yy >= 0 && yy < ny) ? __ldca(f + row + yy) : 0.f;
 }
 
 template <int ORD, int TX, int MINB>
-__global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_velocity(const AdjState a, const float *__restrict__ rec, int k) {
+__global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_velocity(const AdjState a, const float *rec, int k) {
     const int y = blockIdx.x * kBX2 + threadIdx.x;
     const int x0 = (blockIdx.y * kBY2 + threadIdx.y) * TX;
     const int tid = threadIdx.y * kBX2 + threadIdx.x;
@@ -137,14 +138,14 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_velocity(const AdjStat
             float pxa = 0.f, pxb = 0.f, pya = 0.f, pyb = 0.f;
             if (in_vx) {
                 bx = __ldg(a.Bx + i);
-                fax = rec[kFeatVx * G + i];
+                fax = __ldca(rec + kFeatVx * G + i);
                 gbx = a.gBx[i];
                 if (sx >= 0) pxa = a.apsi[4][ix];
                 if (sy >= 0) pxb = a.apsi[6][iy];
             }
             if (in_vy) {
                 by = __ldg(a.By + i);
-                fay = rec[kFeatVy * G + i];
+                fay = __ldca(rec + kFeatVy * G + i);
                 if (sx >= 0) pya = a.apsi[5][ix];
                 if (sy >= 0) pyb = a.apsi[7][iy];
             }
@@ -222,7 +223,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_velocity(const AdjStat
 }
 
 template <int ORD, int ZM, int NS, int TX, int MINB>
-__global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_stress(const AdjState a, const float *__restrict__ rec) {
+__global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_stress(const AdjState a, const float *rec) {
     const int y = blockIdx.x * kBX2 + threadIdx.x;
     const int x0 = (blockIdx.y * kBY2 + threadIdx.y) * TX;
     if (y >= a.ny || x0 >= a.nx) return;
@@ -261,9 +262,9 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_stress(const AdjState 
             L = __ldg(a.L + i);
             M = __ldg(a.M + i);
             if (ZM == 2) gp = __ldg(a.gp + i);
-            fl = rec[kFeatLam * G + i];
-            fmx = rec[kFeatMuX * G + i];
-            fmy = rec[kFeatMuY * G + i];
+            fl = __ldca(rec + kFeatLam * G + i);
+            fmx = __ldca(rec + kFeatMuX * G + i);
+            fmy = __ldca(rec + kFeatMuY * G + i);
             gl = a.gL[i];
             gm = a.gM[i];
             if (sx >= 0) pn0 = a.apsi[0][ix];
@@ -279,7 +280,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_stress(const AdjState 
         }
         if (in_s) {
             Ms = __ldg(a.Ms + i);
-            fsh = rec[kFeatShear * G + i];
+            fsh = __ldca(rec + kFeatShear * G + i);
             gms = a.gMs[i];
             if (sx >= 0) ps0 = a.apsi[1][ix];
             if (sy >= 0) ps1 = a.apsi[3][iy];

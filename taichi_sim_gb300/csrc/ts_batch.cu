@@ -109,12 +109,15 @@ __device__ __forceinline__ Loc locate(const BParams &p) {
 }
 
 // Rows r0 .. r0+2*ORD-1 of one field at (y, shot), zero outside the grid.
+// Fields written by the previous kernel of the stream are read with
+// ld.global.ca, never through the non-coherent path: with programmatic
+// dependent launch that kernel overlaps this one's lifetime.
 template <int ORD>
 __device__ __forceinline__ void bwindow(float (&w)[2 * ORD], const float *f, int r0, int nx, int X, int col) {
 #pragma unroll
     for (int j = 0; j < 2 * ORD; ++j) {
         const int r = r0 + j;
-        w[j] = (r >= 0 && r < nx) ? __ldg(f + r * X + col) : 0.f;
+        w[j] = (r >= 0 && r < nx) ? __ldca(f + r * X + col) : 0.f;
     }
 }
 
@@ -122,7 +125,7 @@ template <int ORD>
 __device__ __forceinline__ void bshift(float (&w)[2 * ORD], const float *f, int r_new, int nx, int X, int col) {
 #pragma unroll
     for (int j = 0; j < 2 * ORD - 1; ++j) w[j] = w[j + 1];
-    w[2 * ORD - 1] = (r_new >= 0 && r_new < nx) ? __ldg(f + r_new * X + col) : 0.f;
+    w[2 * ORD - 1] = (r_new >= 0 && r_new < nx) ? __ldca(f + r_new * X + col) : 0.f;
 }
 
 template <int ORD, int ZM, int NS, int CY, int TX>
@@ -138,7 +141,7 @@ __global__ void __launch_bounds__(32 * CY, 32 / CY) k_bstress(const __grid_const
     const int sy = strip_index(h.strip[1], y);
     const int n_mech = NS == 3 ? 3 : p.zen.n;
     constexpr int R = NS > 0 ? NS : 1;
-    const float *__restrict__ vx = h.v[0];
+    const float *__restrict__ vx = h.v[0];   // read with __ldca only
     const float *__restrict__ vy = h.v[1];
     float *__restrict__ s0 = h.s[0];
     float *__restrict__ s1 = h.s[1];
@@ -174,8 +177,8 @@ __global__ void __launch_bounds__(32 * CY, 32 / CY) k_bstress(const __grid_const
                 if (ZM == 2) gp = __ldg(h.gp + cell);
 #pragma unroll
                 for (int c = 0; c < ORD; ++c) {
-                    ny_hi[c] = __ldg(vy + i + c * Y);         // vy[y+c]
-                    ny_lo[c] = __ldg(vy + i - (c + 1) * Y);   // vy[y-c-1]
+                    ny_hi[c] = __ldca(vy + i + c * Y);         // vy[y+c]
+                    ny_lo[c] = __ldca(vy + i - (c + 1) * Y);   // vy[y-c-1]
                 }
                 sxx = s0[i];
                 syy = s1[i];
@@ -194,8 +197,8 @@ __global__ void __launch_bounds__(32 * CY, 32 / CY) k_bstress(const __grid_const
                 Ms = __ldg(h.mus + cell);
 #pragma unroll
                 for (int c = 0; c < ORD; ++c) {
-                    sx_hi[c] = __ldg(vx + i + (c + 1) * Y);   // vx[y+c+1]
-                    sx_lo[c] = __ldg(vx + i - c * Y);         // vx[y-c]
+                    sx_hi[c] = __ldca(vx + i + (c + 1) * Y);   // vx[y+c+1]
+                    sx_lo[c] = __ldca(vx + i - c * Y);         // vx[y-c]
                 }
                 sxy = s2[i];
                 if (sx >= 0) ps0 = h.psi[1][ix];
@@ -298,7 +301,7 @@ __global__ void __launch_bounds__(32 * CY, 32 / CY) k_bvelocity(const __grid_con
     const int yb = y / CY;
     pdl_wait();
     const int k = *p.step_base + j;
-    const float *__restrict__ sxx = h.s[0];
+    const float *__restrict__ sxx = h.s[0];  // read with __ldca only
     const float *__restrict__ syy = h.s[1];
     const float *__restrict__ sxy = h.s[2];
     float *__restrict__ v0 = h.v[0];
@@ -327,8 +330,8 @@ __global__ void __launch_bounds__(32 * CY, 32 / CY) k_bvelocity(const __grid_con
             if (in_vx) {
 #pragma unroll
                 for (int c = 0; c < ORD; ++c) {
-                    bx_hi[c] = __ldg(sxy + i + c * Y);         // sxy[y+c]
-                    bx_lo[c] = __ldg(sxy + i - (c + 1) * Y);   // sxy[y-c-1]
+                    bx_hi[c] = __ldca(sxy + i + c * Y);         // sxy[y+c]
+                    bx_lo[c] = __ldca(sxy + i - (c + 1) * Y);   // sxy[y-c-1]
                 }
                 vx0 = v0[i];
                 dx0 = __ldg(h.dtr0 + cell);
@@ -338,8 +341,8 @@ __global__ void __launch_bounds__(32 * CY, 32 / CY) k_bvelocity(const __grid_con
             if (in_vy) {
 #pragma unroll
                 for (int c = 0; c < ORD; ++c) {
-                    by_hi[c] = __ldg(syy + i + (c + 1) * Y);   // syy[y+c+1]
-                    by_lo[c] = __ldg(syy + i - c * Y);         // syy[y-c]
+                    by_hi[c] = __ldca(syy + i + (c + 1) * Y);   // syy[y+c+1]
+                    by_lo[c] = __ldca(syy + i - c * Y);         // syy[y-c]
                 }
                 vy0 = v1[i];
                 dy0 = __ldg(h.dtr1 + cell);
@@ -411,7 +414,7 @@ __global__ void __launch_bounds__(32 * CY, 32 / CY) k_bvelocity(const __grid_con
         if (k >= __ldg(r.rec_first + rec)) {
             float acc = 0.f;
             for (int t = __ldg(r.rec_start + rec); t < __ldg(r.rec_start + rec + 1); ++t)
-                acc += r.s[1][((shot >> 5) * r.nx * r.ny + __ldg(r.rec_cell + t)) * 32 + (shot & 31)];
+                acc += __ldca(r.s[1] + ((shot >> 5) * r.nx * r.ny + __ldg(r.rec_cell + t)) * 32 + (shot & 31));
             r.traces[((int64_t)shot * p.rows + k) * r.n_rec + rec] = acc;
         }
     }

@@ -151,6 +151,10 @@ using ts::Axis;
 using ts::make_axis;
 using ts::round_up;
 
+// Kernel launches of one time step: 2D stress + velocity; 3D normal stress,
+// shear stress, velocity.
+static int kernels_per_step(const ts_sim *s) { return s->dims == 3 ? 3 : 2; }
+
 extern "C" {
 
 const char *ts_strerror(int code) {
@@ -412,9 +416,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     // ---- launch geometry ----
     s->n_blocks = s->dims == 2 ? ts::blocks_2d(p) : ts::blocks_3d(p);
     auto block_of = [&](int x, int y, int z) -> int {
-        if (s->dims == 2) return ts::block_of_2d(p, x, y);
-        const int gx = (nz + ts::kBX3 - 1) / ts::kBX3, gy = (ny + ts::kBY3 - 1) / ts::kBY3;
-        return ((x / ts::kBZ3) * gy + y / ts::kBY3) * gx + z / ts::kBX3;
+        return s->dims == 2 ? ts::block_of_2d(p, x, y) : ts::block_of_3d(p, x, y, z);
     };
 
     // ---- sources ----
@@ -591,7 +593,7 @@ int ts_profile_steps(ts_sim *s, int32_t n_steps, void *stream, float *ms_per_ker
         }
     }
     ts::launch_advance(s->step_base, n_steps, st);
-    s->launches += 2 * (int64_t)n_steps + 1;
+    s->launches += (int64_t)kernels_per_step(s) * n_steps + 1;
     TS_CUDA(cudaGetLastError());
     TS_CUDA(cudaEventSynchronize(ev.back()));
     double tot[2] = {0.0, 0.0};
@@ -647,12 +649,12 @@ int ts_run(ts_sim *s, int32_t n_steps, void *stream) {
     int left = n_steps;
     while (left >= kGraphSteps && s->graph) {
         TS_CUDA(cudaGraphLaunch(s->graph, st));
-        s->launches += 2 * kGraphSteps + 1;
+        s->launches += kernels_per_step(s) * kGraphSteps + 1;
         left -= kGraphSteps;
     }
     if (left > 0) {
         launch_steps(left, st);
-        s->launches += 2 * left + 1;
+        s->launches += kernels_per_step(s) * left + 1;
     }
     TS_CUDA(cudaGetLastError());
     TS_CUDA(cudaEventRecord(s->done, st));
@@ -719,7 +721,7 @@ int ts_device_buffer(ts_sim *s, int32_t what, void **dev_ptr, size_t *pitch_byte
 
 int ts_launches_per_step(const ts_sim *s, int32_t *launches) {
     if (!s || !launches) return fail(TS_E_ARG, "null argument");
-    *launches = 2;
+    *launches = kernels_per_step(s);
     return TS_OK;
 }
 

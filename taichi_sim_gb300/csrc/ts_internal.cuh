@@ -110,7 +110,10 @@ enum { kFeatLam = 0, kFeatMuX, kFeatMuY, kFeatShear, kFeatVx, kFeatVy, kFeat };
 // Programmatic dependent launch: a step kernel may be scheduled while the
 // previous kernel of the stream drains.  Before the wait it may only read
 // data no earlier kernel writes (coefficients, tables); after it, all
-// writes of the previous kernels are visible.  The trigger lets the next
+// writes of the previous kernels are visible to coherent loads.  Fields an
+// earlier kernel wrote are never read through the non-coherent (read-only)
+// path: that kernel's lifetime overlaps this one's, and such reads returned
+// stale values in a few percent of runs.  The trigger lets the next
 // kernel's launch start once every block of this one has issued it.
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
@@ -160,6 +163,15 @@ inline int block_of_2d(const StepParams &p, int x, int y) {
     const int gx = (p.ny + kBX2 - 1) / kBX2;
     return (x / (kBY2 * p.tx)) * gx + y / kBX2;
 }
-constexpr int kBX3 = 32, kBY3 = 4, kBZ3 = 2;    // 3D block: 32 (z) x 4 (y) x 2 (x)
+// 3D kernels: blocks of 32 (z) x 8 (y) threads, each updating kTX3S (stress
+// kernels) or kTX3 (velocity kernel) consecutive nodes along x (measured on
+// the 256^3 three-mechanism case against 1, 2 and 4).
+constexpr int kBX3 = 32, kBY3 = 8, kTX3 = 2, kTX3S = 4;
+
+// Flat index of the 3D velocity block that updates node (x, y, z).
+inline int block_of_3d(const StepParams &p, int x, int y, int z) {
+    const int gx = (p.nz + kBX3 - 1) / kBX3, gy = (p.ny + kBY3 - 1) / kBY3;
+    return ((x / kTX3) * gy + y / kBY3) * gx + z / kBX3;
+}
 
 }  // namespace ts

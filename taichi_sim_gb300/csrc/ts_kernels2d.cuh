@@ -39,7 +39,14 @@ namespace {
 
 constexpr int kTaichi = 0;
 
+// Loads.  ldg: data no kernel writes (coefficients, tables), through the
+// read-only path.  ldf: fields the previous kernel of the stream wrote.  With
+// programmatic dependent launch that kernel's lifetime overlaps this one's,
+// so its output is not read-only for this kernel's lifetime and must not be
+// read through the non-coherent path (doing so returned stale values):
+// ld.global.ca, cached in L1 and coherent after griddepcontrol.wait.
 __device__ __forceinline__ float ldg(const float *p) { return __ldg(p); }
+__device__ __forceinline__ float ldf(const float *p) { return __ldca(p); }
 
 // b * psi + a * d, then d / k + psi
 __device__ __forceinline__ float cpml(float d, float psi_old, float &psi_new, const Cpml &t) {
@@ -54,7 +61,7 @@ __device__ __forceinline__ void load_window(float (&w)[2 * ORD], const float *f,
 #pragma unroll
     for (int j = 0; j < 2 * ORD; ++j) {
         const int r = r0 + j;
-        w[j] = (r >= 0 && r < nx) ? ldg(f + (int64_t)r * P + y) : 0.f;
+        w[j] = (r >= 0 && r < nx) ? ldf(f + (int64_t)r * P + y) : 0.f;
     }
 }
 
@@ -62,16 +69,16 @@ template <int ORD>
 __device__ __forceinline__ void shift_window(float (&w)[2 * ORD], const float *f, int r_new, int nx, int P, int y) {
 #pragma unroll
     for (int j = 0; j < 2 * ORD - 1; ++j) w[j] = w[j + 1];
-    w[2 * ORD - 1] = (r_new >= 0 && r_new < nx) ? ldg(f + (int64_t)r_new * P + y) : 0.f;
+    w[2 * ORD - 1] = (r_new >= 0 && r_new < nx) ? ldf(f + (int64_t)r_new * P + y) : 0.f;
 }
 
-template <int ORD, int FAM, int ZM, int NS, int TX, bool FEAT = false, int MINB = 1>
+template <int ORD, int FAM, int ZM, int NS, int TX, bool FEAT = false, int MINB = 0>
 __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams p) {
     const int y = blockIdx.x * kBX2 + threadIdx.x;
     const int x0 = (blockIdx.y * kBY2 + threadIdx.y) * TX;
     if (y >= p.ny || x0 >= p.nx) return;
     const int P = p.pitch, nx = p.nx;
-    const float *__restrict__ vx = p.v[0];
+    const float *__restrict__ vx = p.v[0];   // read with ldf only
     const float *__restrict__ vy = p.v[1];
     const int n_mech = NS == 3 ? 3 : p.zen.n;
     constexpr int R = NS > 0 ? NS : 1;
@@ -104,9 +111,9 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
                 M = ldg(p.mu_dt + i);
                 if (ZM == 2) gp = ldg(p.g_p + i);
 #pragma unroll
-                for (int c = 0; c < ORD; ++c) ny_lo[c] = ldg(vy + i - c - 1);   // vy[y-c-1]
+                for (int c = 0; c < ORD; ++c) ny_lo[c] = ldf(vy + i - c - 1);   // vy[y-c-1]
 #pragma unroll
-                for (int c = 1; c < ORD; ++c) ny_hi[c - 1] = ldg(vy + i + c);   // vy[y+c], c >= 1
+                for (int c = 1; c < ORD; ++c) ny_hi[c - 1] = ldf(vy + i + c);   // vy[y+c], c >= 1
                 sxx = p.s[0][i];
                 syy = p.s[1][i];
                 if (sx >= 0) pn0 = p.psi[0][ix];
@@ -123,9 +130,9 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
             if (in_s) {
                 Ms = ldg(p.mus_dt[0] + i);
 #pragma unroll
-                for (int c = 0; c < ORD; ++c) sx_hi[c] = ldg(vx + i + c + 1);   // vx[y+c+1]
+                for (int c = 0; c < ORD; ++c) sx_hi[c] = ldf(vx + i + c + 1);   // vx[y+c+1]
 #pragma unroll
-                for (int c = 1; c < ORD; ++c) sx_lo[c - 1] = ldg(vx + i - c);   // vx[y-c], c >= 1
+                for (int c = 1; c < ORD; ++c) sx_lo[c - 1] = ldf(vx + i - c);   // vx[y-c], c >= 1
                 sxy = p.s[3][i];
                 if (sx >= 0) ps0 = p.psi[1][ix];
                 if (sy >= 0) ps1 = p.psi[3][iy];
@@ -230,7 +237,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
     pdl_trigger();
 }
 
-template <int ORD, int FAM, int TX, bool FEAT = false, int MINB = 1>
+template <int ORD, int FAM, int TX, bool FEAT = false, int MINB = 0>
 __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParams p, const int j) {
     const int y = blockIdx.x * kBX2 + threadIdx.x;
     const int x0 = (blockIdx.y * kBY2 + threadIdx.y) * TX;
@@ -238,7 +245,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
     const int blk = blockIdx.y * gridDim.x + blockIdx.x;
     const int P = p.pitch, nx = p.nx;
     const bool live_col = y < p.ny;
-    const float *__restrict__ sxx = p.s[0];
+    const float *__restrict__ sxx = p.s[0];  // read with ldf only
     const float *__restrict__ syy = p.s[1];
     const float *__restrict__ sxy = p.s[3];
     const int sy = live_col ? strip_index(p.strip[1], y) : -1;
@@ -270,9 +277,9 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             float vx0 = 0.f, vy0 = 0.f, dx0 = 0.f, dy0 = 0.f, pxa = 0.f, pxb = 0.f, pya = 0.f, pyb = 0.f;
             if (in_vx) {
 #pragma unroll
-                for (int c = 0; c < ORD; ++c) bx_lo[c] = ldg(sxy + i - c - 1);   // sxy[y-c-1]
+                for (int c = 0; c < ORD; ++c) bx_lo[c] = ldf(sxy + i - c - 1);   // sxy[y-c-1]
 #pragma unroll
-                for (int c = 1; c < ORD; ++c) bx_hi[c - 1] = ldg(sxy + i + c);   // sxy[y+c], c >= 1
+                for (int c = 1; c < ORD; ++c) bx_hi[c - 1] = ldf(sxy + i + c);   // sxy[y+c], c >= 1
                 vx0 = p.v[0][i];
                 dx0 = ldg(p.dtr[0] + i);
                 if (sx >= 0) pxa = p.psi[4][ix];
@@ -280,7 +287,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             }
             if (in_vy) {
 #pragma unroll
-                for (int c = 0; c < 2 * ORD; ++c) by[c] = ldg(syy + i - ORD + 1 + c);   // syy[y-ORD+1 .. y+ORD]
+                for (int c = 0; c < 2 * ORD; ++c) by[c] = ldf(syy + i - ORD + 1 + c);   // syy[y-ORD+1 .. y+ORD]
                 vy0 = p.v[1][i];
                 dy0 = ldg(p.dtr[1] + i);
                 if (sx >= 0) pya = p.psi[5][ix];
@@ -351,7 +358,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
     const int g = blk * (kBX2 * kBY2) + tid;
     if (g < p.n_rec && k >= __ldg(p.rec_first_step + g)) {
         float acc = 0.f;
-        for (int q = __ldg(p.rec_start + g); q < __ldg(p.rec_start + g + 1); ++q) acc += syy[__ldg(p.rec_cell + q)];
+        for (int q = __ldg(p.rec_start + g); q < __ldg(p.rec_start + g + 1); ++q) acc += ldf(syy + __ldg(p.rec_cell + q));
         p.traces[(int64_t)k * p.n_rec + g] = acc;
     }
     warp_stability(vmax, bad, reinterpret_cast<unsigned *>(p.block_max) + blk, p.first_bad, k);

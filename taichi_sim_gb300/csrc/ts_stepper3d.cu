@@ -1,10 +1,14 @@
 // 3D staggered-grid (visco)elastic time step on sm_103a.
 //
-// One time step = k_stress3d (sxx, syy, szz, sxy, sxz, syz with CPML strips
-// and the Zener update fused) followed by k_velocity3d (vx, vy, vz with
-// CPML, Dirichlet zeroing, source injection, receiver sampling of szz and
-// stability bookkeeping fused).  Thread (tx, ty, tz) owns node
-// (z = 32 bx + tx, y = 4 by + ty, x = 2 bz + tz): z is the contiguous axis.
+// One time step = three launches: k_normal3d (sxx, syy, szz), k_shear3d
+// (sxy, sxz, syz), each with its CPML strips and Zener update fused, then
+// k_velocity3d (vx, vy, vz with CPML, Dirichlet zeroing, source injection,
+// receiver sampling of szz and stability bookkeeping fused).  Splitting the
+// stress update halves the live state of a thread, so more blocks stay
+// resident per SM.  Thread (tx, ty) of a 32 x 8 block owns the column
+// (z = 32 bx + tx, y = 8 by + ty) and updates consecutive nodes along x
+// (z is the contiguous axis); the x-derivatives come from register windows
+// that take one new plane per node, the y- and z-derivatives from loads.
 // As in 2D, every load of a node is issued before its first store so that
 // one memory latency is paid per node.
 //
@@ -24,6 +28,14 @@ __device__ __forceinline__ float cpml(float d, float psi_old, float &psi_new, co
     return fmaf(d, t.ik, psi_new);
 }
 
+// Load of a field value written by an earlier kernel of the stream.  With
+// programmatic dependent launch that kernel's lifetime overlaps this one's,
+// so the field is not read-only for this kernel's lifetime and must not be
+// read through the non-coherent path (measured: stale values, wrong results
+// in a few percent of runs); ld.global.ca is coherent after
+// griddepcontrol.wait and still cached in L1.
+__device__ __forceinline__ float fld(const float *q) { return __ldca(q); }
+
 // Stencil values of one staggered derivative: hi[c] - lo[c] pairs.
 // PLUS: f[i + (c+1) s] - f[i - c s]; otherwise f[i + c s] - f[i - (c+1) s].
 template <int ORD>
@@ -32,12 +44,12 @@ struct Pairs {
 };
 
 template <int ORD, bool PLUS>
-__device__ __forceinline__ Pairs<ORD> load_pairs(const float *__restrict__ f, int64_t i, int64_t s) {
+__device__ __forceinline__ Pairs<ORD> load_pairs(const float *f, int64_t i, int64_t s) {
     Pairs<ORD> r;
 #pragma unroll
     for (int c = 0; c < ORD; ++c) {
-        r.hi[c] = __ldg(f + i + (PLUS ? (c + 1) : c) * s);
-        r.lo[c] = __ldg(f + i - (PLUS ? c : (c + 1)) * s);
+        r.hi[c] = fld(f + i + (PLUS ? (c + 1) : c) * s);
+        r.lo[c] = fld(f + i - (PLUS ? c : (c + 1)) * s);
     }
     return r;
 }
@@ -50,369 +62,479 @@ __device__ __forceinline__ float deriv(const Pairs<ORD> &q, const float *cd) {
     return a;
 }
 
+// Resident blocks per SM the kernels are compiled for (register budget
+// 85 per thread; measured against 1, 2 and 4 on the 256^3 case).
+constexpr int kStressMinBlocks = 3, kVelocityMinBlocks = 3;
+// x window of 2*ORD planes of one field at (y, z), first plane r0; planes
+// outside the grid read 0
+template <int ORD>
+__device__ __forceinline__ void xwindow(float (&w)[2 * ORD], const float *f, int r0, int nx, int64_t X,
+                                        int64_t yz) {
+#pragma unroll
+    for (int j = 0; j < 2 * ORD; ++j) {
+        const int r = r0 + j;
+        w[j] = (r >= 0 && r < nx) ? fld(f + r * X + yz) : 0.f;
+    }
+}
+
+template <int ORD>
+__device__ __forceinline__ void xshift(float (&w)[2 * ORD], const float *f, int r_new, int nx, int64_t X,
+                                       int64_t yz) {
+#pragma unroll
+    for (int j = 0; j < 2 * ORD - 1; ++j) w[j] = w[j + 1];
+    w[2 * ORD - 1] = (r_new >= 0 && r_new < nx) ? fld(f + r_new * X + yz) : 0.f;
+}
+
+// sum_c cd[c] (w[ORD + c] - w[ORD - 1 - c])
+template <int ORD>
+__device__ __forceinline__ float wderiv(const float (&w)[2 * ORD], const float *cd) {
+    float a = 0.f;
+#pragma unroll
+    for (int c = 0; c < ORD; ++c) a = fmaf(cd[c], w[ORD + c] - w[ORD - 1 - c], a);
+    return a;
+}
+
+// Normal stresses (sxx, syy, szz, their Zener memory variables and CPML
+// strips), x-marching: thread (z, y) updates kTX3S consecutive nodes along x,
+// the x-derivative of vx from a register window, the y- and z-derivatives
+// from loads.
 template <int ORD, int ZM, int NS>
-__global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_stress3d(const StepParams p) {
+__global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_normal3d(const StepParams p) {
     const int z = blockIdx.x * kBX3 + threadIdx.x;
     const int y = blockIdx.y * kBY3 + threadIdx.y;
-    const int x = blockIdx.z * kBZ3 + threadIdx.z;
-    const bool in_n = x >= ORD - 1 && x < p.nx - ORD && y >= ORD && y < p.ny - ORD + 1 && z >= ORD && z < p.nz - ORD + 1;
-    const bool in_xy = x >= ORD && x < p.nx - ORD + 1 && y >= ORD - 1 && y < p.ny - ORD && z >= ORD - 1 && z < p.nz - ORD;
-    const bool in_yz = x >= ORD - 1 && x < p.nx - ORD && y >= ORD - 1 && y < p.ny - ORD && z >= ORD - 1 && z < p.nz - ORD;
-    if (!in_n && !in_xy && !in_yz) return;
-    const int64_t X = p.plane, Y = p.pitch;
-    const int64_t i = (int64_t)x * X + y * Y + z;
-    const float *vx = p.v[0], *vy = p.v[1], *vz = p.v[2];
-    const int sx = strip_index(p.strip[0], x), sy = strip_index(p.strip[1], y), sz = strip_index(p.strip[2], z);
-    const int64_t ix = ((int64_t)sx * p.ny + y) * p.pitch + z;
-    const int64_t iy = ((int64_t)x * p.strip[1].width + sy) * p.pitch + z;
-    const int64_t iz = ((int64_t)x * p.ny + y) * p.strip[2].width + sz;
+    const int x0 = blockIdx.z * kTX3S;
+    if (y >= p.ny || z >= p.nz || x0 >= p.nx) return;
+    const int64_t X = p.plane, Y = p.pitch, yz = (int64_t)y * Y + z, G = p.grid_elems;
+    const float *__restrict__ vx = p.v[0];
+    const float *__restrict__ vy = p.v[1];
+    const float *__restrict__ vz = p.v[2];
+    const bool yz_n = y >= ORD && y < p.ny - ORD + 1 && z >= ORD && z < p.nz - ORD + 1;
+    const int sy = strip_index(p.strip[1], y), sz = strip_index(p.strip[2], z);
     const int n_mech = NS == 3 ? 3 : p.zen.n;
-    const int64_t G = p.grid_elems;
     constexpr int R = NS > 0 ? NS : 1;
-
-    // ---------------- loads ----------------
-    // per-node coefficients (never written) before waiting for the previous kernel
-    float L = 0.f, M = 0.f, gp = 1.f, gs = 1.f, Mxy = 0.f, Mxz = 0.f, Myz = 0.f;
-    if (in_n) {
-        L = __ldg(p.lam_dt + i);
-        M = __ldg(p.mu_dt + i);
-        if (ZM == 2) gp = __ldg(p.g_p + i);
-    }
-    if (in_xy) {
-        Mxy = __ldg(p.mus_dt[0] + i);
-        Mxz = __ldg(p.mus_dt[1] + i);
-    }
-    if (in_yz) Myz = __ldg(p.mus_dt[2] + i);
-    if (ZM == 2) gs = __ldg(p.g_s + i);
     pdl_wait();
-    Pairs<ORD> n_x, n_y, n_z, a_vy, a_vx, b_vz, b_vx, c_vz, c_vy;
-    float s_n[3] = {0.f, 0.f, 0.f};
-    float s_xy = 0.f, s_xz = 0.f, s_yz = 0.f;
-    float psi[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    float r0[R], r1[R], r2[R], r3[R], r4[R], r5[R];
-    if (in_n) {
-        n_x = load_pairs<ORD, true>(vx, i, X);
-        n_y = load_pairs<ORD, false>(vy, i, Y);
-        n_z = load_pairs<ORD, false>(vz, i, 1);
-        s_n[0] = p.s[0][i];
-        s_n[1] = p.s[1][i];
-        s_n[2] = p.s[2][i];
-        if (sx >= 0) psi[0] = p.psi[0][ix];
-        if (sy >= 0) psi[1] = p.psi[1][iy];
-        if (sz >= 0) psi[2] = p.psi[2][iz];
-        if (ZM != 0) {
+    float wx[2 * ORD];   // vx planes [x-ORD+1, x+ORD]
+    xwindow<ORD>(wx, vx, x0 - ORD + 1, p.nx, X, yz);
 #pragma unroll
-            for (int l = 0; l < R; ++l)
-                if (l < n_mech) {
-                    r0[l] = p.r[0][l * G + i];
-                    r1[l] = p.r[1][l * G + i];
-                    r2[l] = p.r[2][l * G + i];
-                }
-        }
-    }
-    if (in_xy) {
-        a_vy = load_pairs<ORD, false>(vy, i, X);
-        a_vx = load_pairs<ORD, true>(vx, i, Y);
-        b_vz = load_pairs<ORD, false>(vz, i, X);
-        b_vx = load_pairs<ORD, true>(vx, i, 1);
-        s_xy = p.s[3][i];
-        s_xz = p.s[4][i];
-        if (sx >= 0) {
-            psi[3] = p.psi[3][ix];
-            psi[5] = p.psi[5][ix];
-        }
-        if (sy >= 0) psi[4] = p.psi[4][iy];
-        if (sz >= 0) psi[6] = p.psi[6][iz];
-        if (ZM != 0) {
+    for (int t = 0; t < kTX3S; ++t) {
+        const int x = x0 + t;
+        if (x >= p.nx) break;
+        if (yz_n && x >= ORD - 1 && x < p.nx - ORD) {
+            const int64_t i = (int64_t)x * X + yz;
+            const int sx = strip_index(p.strip[0], x);
+            const int64_t ix = ((int64_t)sx * p.ny + y) * p.pitch + z;
+            const int64_t iy = ((int64_t)x * p.strip[1].width + sy) * p.pitch + z;
+            const int64_t iz = ((int64_t)x * p.ny + y) * p.strip[2].width + sz;
+            // ---- loads ----
+            const Pairs<ORD> n_y = load_pairs<ORD, false>(vy, i, Y);   // vy[y+c]-vy[y-c-1]
+            const Pairs<ORD> n_z = load_pairs<ORD, false>(vz, i, 1);   // vz[z+c]-vz[z-c-1]
+            const float L = __ldg(p.lam_dt + i), M = __ldg(p.mu_dt + i);
+            const float gp = ZM == 2 ? __ldg(p.g_p + i) : 1.f, gs = ZM == 2 ? __ldg(p.g_s + i) : 1.f;
+            const float s0 = p.s[0][i], s1 = p.s[1][i], s2 = p.s[2][i];
+            float pz0 = 0.f, pz1 = 0.f, pz2 = 0.f;
+            if (sx >= 0) pz0 = p.psi[0][ix];
+            if (sy >= 0) pz1 = p.psi[1][iy];
+            if (sz >= 0) pz2 = p.psi[2][iz];
+            float r0[R], r1[R], r2[R];
+            if (ZM != 0) {
 #pragma unroll
-            for (int l = 0; l < R; ++l)
-                if (l < n_mech) {
-                    r3[l] = p.r[3][l * G + i];
-                    r4[l] = p.r[4][l * G + i];
-                }
-        }
-    }
-    if (in_yz) {
-        c_vz = load_pairs<ORD, true>(vz, i, Y);
-        c_vy = load_pairs<ORD, true>(vy, i, 1);
-        s_yz = p.s[5][i];
-        if (sy >= 0) psi[7] = p.psi[7][iy];
-        if (sz >= 0) psi[8] = p.psi[8][iz];
-        if (ZM != 0) {
+                for (int l = 0; l < R; ++l)
+                    if (l < n_mech) {
+                        r0[l] = p.r[0][l * G + i];
+                        r1[l] = p.r[1][l * G + i];
+                        r2[l] = p.r[2][l * G + i];
+                    }
+            }
+            // ---- update: vx[x+c+1]-vx[x-c] from the window ----
+            float ddx = wderiv<ORD>(wx, p.cd[0]), ddy = deriv(n_y, p.cd[1]), ddz = deriv(n_z, p.cd[2]);
+            float np_;
+            if (sx >= 0) {
+                ddx = cpml(ddx, pz0, np_, p.tab_h[0][x]);
+                p.psi[0][ix] = np_;
+            }
+            if (sy >= 0) {
+                ddy = cpml(ddy, pz1, np_, p.tab_f[1][y]);
+                p.psi[1][iy] = np_;
+            }
+            if (sz >= 0) {
+                ddz = cpml(ddz, pz2, np_, p.tab_f[2][z]);
+                p.psi[2][iz] = np_;
+            }
+            const float L2M = fmaf(2.f, M, L);
+            float ux = fmaf(L2M, ddx, L * (ddy + ddz));
+            float uy = fmaf(L2M, ddy, L * (ddx + ddz));
+            float uz = fmaf(L2M, ddz, L * (ddx + ddy));
+            if (ZM != 0) {
+                const float div = ddx + ddy + ddz;
+                const float third = div * (1.f / 3.f);
+                const float dy_ = ddx - third, dz_ = ddy - third;
+                float srxx = 0.f, sryy = 0.f, srzz = 0.f;
 #pragma unroll
-            for (int l = 0; l < R; ++l)
-                if (l < n_mech) r5[l] = p.r[5][l * G + i];
+                for (int l = 0; l < R; ++l)
+                    if (l < n_mech) {
+                        const float a = fmaf(p.zen.Ap[l], r0[l], (p.zen.Bp[l] * gp) * div);
+                        const float b = fmaf(p.zen.As[l], r1[l], (p.zen.Bs[l] * gs) * dy_);
+                        const float c = fmaf(p.zen.As[l], r2[l], (p.zen.Bs[l] * gs) * dz_);
+                        srxx += r0[l] + a;
+                        sryy += r1[l] + b;
+                        srzz += r2[l] + c;
+                        p.r[0][l * G + i] = a;
+                        p.r[1][l * G + i] = b;
+                        p.r[2][l * G + i] = c;
+                    }
+                const float hl23 = 0.5f * fmaf(2.f / 3.f, M, L);
+                ux = fmaf(hl23, srxx, fmaf(M, sryy, ux));
+                uy = fmaf(hl23, srxx, fmaf(M, srzz, uy));
+                uz = fmaf(0.5f * L2M, srxx, fmaf(-M * (1.f / 3.f), sryy + srzz, uz));
+            }
+            p.s[0][i] = s0 + ux;
+            p.s[1][i] = s1 + uy;
+            p.s[2][i] = s2 + uz;
         }
-    }
-
-    // ---------------- normal stresses ----------------
-    if (in_n) {
-        float ddx = deriv(n_x, p.cd[0]), ddy = deriv(n_y, p.cd[1]), ddz = deriv(n_z, p.cd[2]);
-        float np_;
-        if (sx >= 0) {
-            ddx = cpml(ddx, psi[0], np_, p.tab_h[0][x]);
-            p.psi[0][ix] = np_;
-        }
-        if (sy >= 0) {
-            ddy = cpml(ddy, psi[1], np_, p.tab_f[1][y]);
-            p.psi[1][iy] = np_;
-        }
-        if (sz >= 0) {
-            ddz = cpml(ddz, psi[2], np_, p.tab_f[2][z]);
-            p.psi[2][iz] = np_;
-        }
-        const float L2M = fmaf(2.f, M, L);
-        float ux = fmaf(L2M, ddx, L * (ddy + ddz));
-        float uy = fmaf(L2M, ddy, L * (ddx + ddz));
-        float uz = fmaf(L2M, ddz, L * (ddx + ddy));
-        if (ZM != 0) {
-            const float div = ddx + ddy + ddz;
-            const float third = div * (1.f / 3.f);
-            const float dy_ = ddx - third, dz_ = ddy - third;
-            float srxx = 0.f, sryy = 0.f, srzz = 0.f;
-#pragma unroll
-            for (int l = 0; l < R; ++l)
-                if (l < n_mech) {
-                    const float a = fmaf(p.zen.Ap[l], r0[l], (p.zen.Bp[l] * gp) * div);
-                    const float b = fmaf(p.zen.As[l], r1[l], (p.zen.Bs[l] * gs) * dy_);
-                    const float c = fmaf(p.zen.As[l], r2[l], (p.zen.Bs[l] * gs) * dz_);
-                    srxx += r0[l] + a;
-                    sryy += r1[l] + b;
-                    srzz += r2[l] + c;
-                    p.r[0][l * G + i] = a;
-                    p.r[1][l * G + i] = b;
-                    p.r[2][l * G + i] = c;
-                }
-            const float hl23 = 0.5f * fmaf(2.f / 3.f, M, L);
-            ux = fmaf(hl23, srxx, fmaf(M, sryy, ux));
-            uy = fmaf(hl23, srxx, fmaf(M, srzz, uy));
-            uz = fmaf(0.5f * L2M, srxx, fmaf(-M * (1.f / 3.f), sryy + srzz, uz));
-        }
-        p.s[0][i] = s_n[0] + ux;
-        p.s[1][i] = s_n[1] + uy;
-        p.s[2][i] = s_n[2] + uz;
-    }
-    // ---------------- sigma_xy, sigma_xz ----------------
-    if (in_xy) {
-        float a1 = deriv(a_vy, p.cd[0]), a2 = deriv(a_vx, p.cd[1]);
-        float b1 = deriv(b_vz, p.cd[0]), b2 = deriv(b_vx, p.cd[2]);
-        float np_;
-        if (sx >= 0) {
-            a1 = cpml(a1, psi[3], np_, p.tab_f[0][x]);
-            p.psi[3][ix] = np_;
-            b1 = cpml(b1, psi[5], np_, p.tab_f[0][x]);
-            p.psi[5][ix] = np_;
-        }
-        if (sy >= 0) {
-            a2 = cpml(a2, psi[4], np_, p.tab_h[1][y]);
-            p.psi[4][iy] = np_;
-        }
-        if (sz >= 0) {
-            b2 = cpml(b2, psi[6], np_, p.tab_h[2][z]);
-            p.psi[6][iz] = np_;
-        }
-        const float ea = a1 + a2, eb = b1 + b2;
-        float u = Mxy * ea, w = Mxz * eb;
-        if (ZM != 0) {
-            float sa = 0.f, sb = 0.f;
-#pragma unroll
-            for (int l = 0; l < R; ++l)
-                if (l < n_mech) {
-                    const float na = fmaf(p.zen.As[l], r3[l], (p.zen.Bs[l] * gs) * ea);
-                    const float nb = fmaf(p.zen.As[l], r4[l], (p.zen.Bs[l] * gs) * eb);
-                    sa += r3[l] + na;
-                    sb += r4[l] + nb;
-                    p.r[3][l * G + i] = na;
-                    p.r[4][l * G + i] = nb;
-                }
-            u = fmaf(0.5f * Mxy, sa, u);
-            w = fmaf(0.5f * Mxz, sb, w);
-        }
-        p.s[3][i] = s_xy + u;
-        p.s[4][i] = s_xz + w;
-    }
-    // ---------------- sigma_yz ----------------
-    if (in_yz) {
-        float a1 = deriv(c_vz, p.cd[1]), a2 = deriv(c_vy, p.cd[2]);
-        float np_;
-        if (sy >= 0) {
-            a1 = cpml(a1, psi[7], np_, p.tab_h[1][y]);
-            p.psi[7][iy] = np_;
-        }
-        if (sz >= 0) {
-            a2 = cpml(a2, psi[8], np_, p.tab_h[2][z]);
-            p.psi[8][iz] = np_;
-        }
-        const float e = a1 + a2;
-        float u = Myz * e;
-        if (ZM != 0) {
-            float sr = 0.f;
-#pragma unroll
-            for (int l = 0; l < R; ++l)
-                if (l < n_mech) {
-                    const float n_ = fmaf(p.zen.As[l], r5[l], (p.zen.Bs[l] * gs) * e);
-                    sr += r5[l] + n_;
-                    p.r[5][l * G + i] = n_;
-                }
-            u = fmaf(0.5f * Myz, sr, u);
-        }
-        p.s[5][i] = s_yz + u;
+        if (t + 1 < kTX3S) xshift<ORD>(wx, vx, x + ORD + 1, p.nx, X, yz);
     }
     pdl_trigger();
 }
 
-template <int ORD>
-__global__ void __launch_bounds__(kBX3 *kBY3 *kBZ3) k_velocity3d(const StepParams p, const int j) {
+// Shear stresses (sxy, sxz, syz with their Zener memory variables and CPML
+// strips), x-marching as k_normal3d: the x-derivatives of vy and vz from
+// register windows.
+template <int ORD, int ZM, int NS>
+__global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_shear3d(const StepParams p) {
     const int z = blockIdx.x * kBX3 + threadIdx.x;
     const int y = blockIdx.y * kBY3 + threadIdx.y;
-    const int x = blockIdx.z * kBZ3 + threadIdx.z;
-    const int tid = (threadIdx.z * kBY3 + threadIdx.y) * kBX3 + threadIdx.x;
+    const int x0 = blockIdx.z * kTX3S;
+    if (y >= p.ny || z >= p.nz || x0 >= p.nx) return;
+    const int64_t X = p.plane, Y = p.pitch, yz = (int64_t)y * Y + z, G = p.grid_elems;
+    const float *__restrict__ vx = p.v[0];
+    const float *__restrict__ vy = p.v[1];
+    const float *__restrict__ vz = p.v[2];
+    const bool yz_s = y >= ORD - 1 && y < p.ny - ORD && z >= ORD - 1 && z < p.nz - ORD;
+    const int sy = strip_index(p.strip[1], y), sz = strip_index(p.strip[2], z);
+    const int n_mech = NS == 3 ? 3 : p.zen.n;
+    constexpr int R = NS > 0 ? NS : 1;
+    pdl_wait();
+    float wy[2 * ORD], wz[2 * ORD];   // vy and vz planes [x-ORD, x+ORD-1]
+    xwindow<ORD>(wy, vy, x0 - ORD, p.nx, X, yz);
+    xwindow<ORD>(wz, vz, x0 - ORD, p.nx, X, yz);
+#pragma unroll
+    for (int t = 0; t < kTX3S; ++t) {
+        const int x = x0 + t;
+        if (x >= p.nx) break;
+        const bool in_xy = yz_s && x >= ORD && x < p.nx - ORD + 1;
+        const bool in_yz = yz_s && x >= ORD - 1 && x < p.nx - ORD;
+        if (in_xy || in_yz) {
+            const int64_t i = (int64_t)x * X + yz;
+            const int sx = strip_index(p.strip[0], x);
+            const int64_t ix = ((int64_t)sx * p.ny + y) * p.pitch + z;
+            const int64_t iy = ((int64_t)x * p.strip[1].width + sy) * p.pitch + z;
+            const int64_t iz = ((int64_t)x * p.ny + y) * p.strip[2].width + sz;
+            // ---- loads ----
+            Pairs<ORD> a_vx, b_vx, c_vz, c_vy;
+            float Mxy = 0.f, Mxz = 0.f, Myz = 0.f, s_xy = 0.f, s_xz = 0.f, s_yz = 0.f;
+            float psi[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            float r3[R], r4[R], r5[R];
+            const float gs = ZM == 2 ? __ldg(p.g_s + i) : 1.f;
+            if (in_xy) {
+                a_vx = load_pairs<ORD, true>(vx, i, Y);   // vx[y+c+1]-vx[y-c]
+                b_vx = load_pairs<ORD, true>(vx, i, 1);   // vx[z+c+1]-vx[z-c]
+                Mxy = __ldg(p.mus_dt[0] + i);
+                Mxz = __ldg(p.mus_dt[1] + i);
+                s_xy = p.s[3][i];
+                s_xz = p.s[4][i];
+                if (sx >= 0) {
+                    psi[0] = p.psi[3][ix];
+                    psi[2] = p.psi[5][ix];
+                }
+                if (sy >= 0) psi[1] = p.psi[4][iy];
+                if (sz >= 0) psi[3] = p.psi[6][iz];
+                if (ZM != 0) {
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) {
+                            r3[l] = p.r[3][l * G + i];
+                            r4[l] = p.r[4][l * G + i];
+                        }
+                }
+            }
+            if (in_yz) {
+                c_vz = load_pairs<ORD, true>(vz, i, Y);   // vz[y+c+1]-vz[y-c]
+                c_vy = load_pairs<ORD, true>(vy, i, 1);   // vy[z+c+1]-vy[z-c]
+                Myz = __ldg(p.mus_dt[2] + i);
+                s_yz = p.s[5][i];
+                if (sy >= 0) psi[4] = p.psi[7][iy];
+                if (sz >= 0) psi[5] = p.psi[8][iz];
+                if (ZM != 0) {
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) r5[l] = p.r[5][l * G + i];
+                }
+            }
+            float np_;
+            // ---- sigma_xy: vy[x+c]-vy[x-c-1] (window), sigma_xz: vz[x+c]-vz[x-c-1] (window) ----
+            if (in_xy) {
+                float a1 = wderiv<ORD>(wy, p.cd[0]), a2 = deriv(a_vx, p.cd[1]);
+                float b1 = wderiv<ORD>(wz, p.cd[0]), b2 = deriv(b_vx, p.cd[2]);
+                if (sx >= 0) {
+                    a1 = cpml(a1, psi[0], np_, p.tab_f[0][x]);
+                    p.psi[3][ix] = np_;
+                    b1 = cpml(b1, psi[2], np_, p.tab_f[0][x]);
+                    p.psi[5][ix] = np_;
+                }
+                if (sy >= 0) {
+                    a2 = cpml(a2, psi[1], np_, p.tab_h[1][y]);
+                    p.psi[4][iy] = np_;
+                }
+                if (sz >= 0) {
+                    b2 = cpml(b2, psi[3], np_, p.tab_h[2][z]);
+                    p.psi[6][iz] = np_;
+                }
+                const float ea = a1 + a2, eb = b1 + b2;
+                float u = Mxy * ea, w = Mxz * eb;
+                if (ZM != 0) {
+                    float sa = 0.f, sb = 0.f;
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) {
+                            const float na = fmaf(p.zen.As[l], r3[l], (p.zen.Bs[l] * gs) * ea);
+                            const float nb = fmaf(p.zen.As[l], r4[l], (p.zen.Bs[l] * gs) * eb);
+                            sa += r3[l] + na;
+                            sb += r4[l] + nb;
+                            p.r[3][l * G + i] = na;
+                            p.r[4][l * G + i] = nb;
+                        }
+                    u = fmaf(0.5f * Mxy, sa, u);
+                    w = fmaf(0.5f * Mxz, sb, w);
+                }
+                p.s[3][i] = s_xy + u;
+                p.s[4][i] = s_xz + w;
+            }
+            // ---- sigma_yz ----
+            if (in_yz) {
+                float a1 = deriv(c_vz, p.cd[1]), a2 = deriv(c_vy, p.cd[2]);
+                if (sy >= 0) {
+                    a1 = cpml(a1, psi[4], np_, p.tab_h[1][y]);
+                    p.psi[7][iy] = np_;
+                }
+                if (sz >= 0) {
+                    a2 = cpml(a2, psi[5], np_, p.tab_h[2][z]);
+                    p.psi[8][iz] = np_;
+                }
+                const float e = a1 + a2;
+                float u = Myz * e;
+                if (ZM != 0) {
+                    float sr = 0.f;
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) {
+                            const float n_ = fmaf(p.zen.As[l], r5[l], (p.zen.Bs[l] * gs) * e);
+                            sr += r5[l] + n_;
+                            p.r[5][l * G + i] = n_;
+                        }
+                    u = fmaf(0.5f * Myz, sr, u);
+                }
+                p.s[5][i] = s_yz + u;
+            }
+        }
+        if (t + 1 < kTX3S) {
+            xshift<ORD>(wy, vy, x + ORD, p.nx, X, yz);
+            xshift<ORD>(wz, vz, x + ORD, p.nx, X, yz);
+        }
+    }
+    pdl_trigger();
+}
+
+// Velocity update, x-marching: thread (z, y) updates kTX3 consecutive nodes
+// along x; the x-derivatives of sxx, sxy, sxz come from register windows that
+// take one new plane per node, the y- and z-derivatives from loads.
+template <int ORD>
+__global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(const StepParams p, const int j) {
+    const int z = blockIdx.x * kBX3 + threadIdx.x;
+    const int y = blockIdx.y * kBY3 + threadIdx.y;
+    const int x0 = blockIdx.z * kTX3;
+    const int tid = threadIdx.y * kBX3 + threadIdx.x;
     const int blk = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-    const bool live = x < p.nx && y < p.ny && z < p.nz;
-    const int64_t X = p.plane, Y = p.pitch;
-    const int64_t i = (int64_t)x * X + y * Y + z;
-    const float *sxx = p.s[0], *syy = p.s[1], *szz = p.s[2], *sxy = p.s[3], *sxz = p.s[4], *syz = p.s[5];
-    const int sx = strip_index(p.strip[0], x), sy = strip_index(p.strip[1], y), sz = strip_index(p.strip[2], z);
-    const int64_t ix = ((int64_t)sx * p.ny + y) * p.pitch + z;
-    const int64_t iy = ((int64_t)x * p.strip[1].width + sy) * p.pitch + z;
-    const int64_t iz = ((int64_t)x * p.ny + y) * p.strip[2].width + sz;
-    // vz region; outside it all three components are zero (wgsl:1754-1758)
-    const bool in_vz = live && x >= ORD - 1 && x < p.nx - ORD && y >= ORD && y < p.ny - ORD + 1 && z >= ORD - 1 &&
-                       z < p.nz - ORD;
-    const bool in_vx = in_vz && x >= ORD && z >= ORD;        // vx region within the vz region
-    const bool in_vy = in_vz && y < p.ny - ORD && z >= ORD;  // vy region within the vz region
+    const bool col = y < p.ny && z < p.nz;
+    const int64_t X = p.plane, Y = p.pitch, yz = (int64_t)y * Y + z;
+    const float *__restrict__ sxx = p.s[0];
+    const float *__restrict__ syy = p.s[1];
+    const float *__restrict__ szz = p.s[2];
+    const float *__restrict__ sxy = p.s[3];
+    const float *__restrict__ sxz = p.s[4];
+    const float *__restrict__ syz = p.s[5];
+    const int sy = strip_index(p.strip[1], y), sz = strip_index(p.strip[2], z);
+    // vz region in (y, z); outside the vz region all three components are zero (wgsl:1754-1758)
+    const bool yz_vz = col && y >= ORD && y < p.ny - ORD + 1 && z >= ORD - 1 && z < p.nz - ORD;
     const int q0 = __ldg(p.src_block_start + blk), q1 = __ldg(p.src_block_start + blk + 1);
-    const float dtx = in_vx ? __ldg(p.dtr[0] + i) : 0.f;
-    const float dty = in_vz ? __ldg(p.dtr[1] + i) : 0.f;
     pdl_wait();
     const int k = *p.step_base + j;
+    float vmax = 0.f;
+    bool bad = false;
+    if (col && x0 < p.nx) {
+        // sxx planes [x-ORD, x+ORD-1] (vx), sxy and sxz planes [x-ORD+1, x+ORD] (vy, vz)
+        float wa[2 * ORD], wb[2 * ORD], wc[2 * ORD];
+        xwindow<ORD>(wa, sxx, x0 - ORD, p.nx, X, yz);
+        xwindow<ORD>(wb, sxy, x0 - ORD + 1, p.nx, X, yz);
+        xwindow<ORD>(wc, sxz, x0 - ORD + 1, p.nx, X, yz);
+#pragma unroll
+        for (int t = 0; t < kTX3; ++t) {
+            const int x = x0 + t;
+            if (x >= p.nx) break;
+            const int64_t i = (int64_t)x * X + yz;
+            const bool in_vz = yz_vz && x >= ORD - 1 && x < p.nx - ORD;
+            const bool in_vx = in_vz && x >= ORD && z >= ORD;        // vx region within the vz region
+            const bool in_vy = in_vz && y < p.ny - ORD && z >= ORD;  // vy region within the vz region
+            const int sx = strip_index(p.strip[0], x);
+            const int64_t ix = ((int64_t)sx * p.ny + y) * p.pitch + z;
+            const int64_t iy = ((int64_t)x * p.strip[1].width + sy) * p.pitch + z;
+            const int64_t iz = ((int64_t)x * p.ny + y) * p.strip[2].width + sz;
+            // ---- loads ----
+            Pairs<ORD> xb, xe, yb, ye, zb, ze;
+            float v0[3] = {0.f, 0.f, 0.f}, dtx = 0.f, dty = 0.f;
+            float psi[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            if (in_vx) {
+                xb = load_pairs<ORD, false>(sxy, i, Y);
+                xe = load_pairs<ORD, false>(sxz, i, 1);
+                v0[0] = p.v[0][i];
+                dtx = __ldg(p.dtr[0] + i);
+                if (sx >= 0) psi[0] = p.psi[9][ix];
+                if (sy >= 0) psi[1] = p.psi[10][iy];
+                if (sz >= 0) psi[2] = p.psi[11][iz];
+            }
+            if (in_vy) {
+                yb = load_pairs<ORD, true>(syy, i, Y);
+                ye = load_pairs<ORD, false>(syz, i, 1);
+                v0[1] = p.v[1][i];
+                if (sx >= 0) psi[3] = p.psi[12][ix];
+                if (sy >= 0) psi[4] = p.psi[13][iy];
+                if (sz >= 0) psi[5] = p.psi[14][iz];
+            }
+            if (in_vz) {
+                zb = load_pairs<ORD, false>(syz, i, Y);
+                ze = load_pairs<ORD, true>(szz, i, 1);
+                v0[2] = p.v[2][i];
+                dty = __ldg(p.dtr[1] + i);
+                if (sx >= 0) psi[6] = p.psi[15][ix];
+                if (sy >= 0) psi[7] = p.psi[16][iy];
+                if (sz >= 0) psi[8] = p.psi[17][iz];
+            }
+            // ---- update ----
+            float vxn = 0.f, vyn = 0.f, vzn = 0.f, np_;
+            // vx: sxx[x+c]-sxx[x-c-1], sxy[y+c]-sxy[y-c-1], sxz[z+c]-sxz[z-c-1]
+            if (in_vx) {
+                float a = wderiv<ORD>(wa, p.cd[0]), b = deriv(xb, p.cd[1]), e = deriv(xe, p.cd[2]);
+                if (sx >= 0) {
+                    a = cpml(a, psi[0], np_, p.tab_f[0][x]);
+                    p.psi[9][ix] = np_;
+                }
+                if (sy >= 0) {
+                    b = cpml(b, psi[1], np_, p.tab_f[1][y]);
+                    p.psi[10][iy] = np_;
+                }
+                if (sz >= 0) {
+                    e = cpml(e, psi[2], np_, p.tab_f[2][z]);
+                    p.psi[11][iz] = np_;
+                }
+                vxn = fmaf(a + b + e, dtx, v0[0]);
+            }
+            // vy: sxy[x+c+1]-sxy[x-c], syy[y+c+1]-syy[y-c], syz[z+c]-syz[z-c-1]
+            if (in_vy) {
+                float a = wderiv<ORD>(wb, p.cd[0]), b = deriv(yb, p.cd[1]), e = deriv(ye, p.cd[2]);
+                if (sx >= 0) {
+                    a = cpml(a, psi[3], np_, p.tab_h[0][x]);
+                    p.psi[12][ix] = np_;
+                }
+                if (sy >= 0) {
+                    b = cpml(b, psi[4], np_, p.tab_h[1][y]);
+                    p.psi[13][iy] = np_;
+                }
+                if (sz >= 0) {
+                    e = cpml(e, psi[5], np_, p.tab_f[2][z]);
+                    p.psi[14][iz] = np_;
+                }
+                vyn = fmaf(a + b + e, dty, v0[1]);
+            }
+            // vz: sxz[x+c+1]-sxz[x-c], syz[y+c]-syz[y-c-1], szz[z+c+1]-szz[z-c]
+            if (in_vz) {
+                float a = wderiv<ORD>(wc, p.cd[0]), b = deriv(zb, p.cd[1]), e = deriv(ze, p.cd[2]);
+                if (sx >= 0) {
+                    a = cpml(a, psi[6], np_, p.tab_h[0][x]);
+                    p.psi[15][ix] = np_;
+                }
+                if (sy >= 0) {
+                    b = cpml(b, psi[7], np_, p.tab_f[1][y]);
+                    p.psi[16][iy] = np_;
+                }
+                if (sz >= 0) {
+                    e = cpml(e, psi[8], np_, p.tab_h[2][z]);
+                    p.psi[17][iz] = np_;
+                }
+                vzn = fmaf(a + b + e, dty, v0[2]);  // the vy-node density (wgsl3d:1748)
+            }
+            for (int q = q0; q < q1; ++q) {
+                const Source s = p.src[q];
+                if (s.cell == i && k < p.src_rows)
+                    vzn = fmaf(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), s.scale, vzn);
+            }
+            p.v[0][i] = vxn;
+            p.v[1][i] = vyn;
+            p.v[2][i] = vzn;
+            const float v2 = fmaf(vxn, vxn, fmaf(vyn, vyn, vzn * vzn));
+            bad |= !(v2 <= p.v2_threshold);
+            vmax = fmaxf(vmax, v2);
+            if (v2 != v2) vmax = v2;  // keep a NaN visible
+            if (t + 1 < kTX3) {
+                xshift<ORD>(wa, sxx, x + ORD, p.nx, X, yz);
+                xshift<ORD>(wb, sxy, x + ORD + 1, p.nx, X, yz);
+                xshift<ORD>(wc, sxz, x + ORD + 1, p.nx, X, yz);
+            }
+        }
+    }
 
-    // ---------------- loads ----------------
-    Pairs<ORD> xa, xb, xe, ya, yb, ye, za, zb, ze;
-    float v0[3] = {0.f, 0.f, 0.f};
-    float psi[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (in_vx) {
-        xa = load_pairs<ORD, false>(sxx, i, X);
-        xb = load_pairs<ORD, false>(sxy, i, Y);
-        xe = load_pairs<ORD, false>(sxz, i, 1);
-        v0[0] = p.v[0][i];
-        if (sx >= 0) psi[0] = p.psi[9][ix];
-        if (sy >= 0) psi[1] = p.psi[10][iy];
-        if (sz >= 0) psi[2] = p.psi[11][iz];
-    }
-    if (in_vy) {
-        ya = load_pairs<ORD, true>(sxy, i, X);
-        yb = load_pairs<ORD, true>(syy, i, Y);
-        ye = load_pairs<ORD, false>(syz, i, 1);
-        v0[1] = p.v[1][i];
-        if (sx >= 0) psi[3] = p.psi[12][ix];
-        if (sy >= 0) psi[4] = p.psi[13][iy];
-        if (sz >= 0) psi[5] = p.psi[14][iz];
-    }
-    if (in_vz) {
-        za = load_pairs<ORD, true>(sxz, i, X);
-        zb = load_pairs<ORD, false>(syz, i, Y);
-        ze = load_pairs<ORD, true>(szz, i, 1);
-        v0[2] = p.v[2][i];
-        if (sx >= 0) psi[6] = p.psi[15][ix];
-        if (sy >= 0) psi[7] = p.psi[16][iy];
-        if (sz >= 0) psi[8] = p.psi[17][iz];
-    }
-
-    // ---------------- update ----------------
-    float v2 = 0.f;
-    if (live) {
-        float vxn = 0.f, vyn = 0.f, vzn = 0.f, np_;
-        if (in_vx) {
-            float a = deriv(xa, p.cd[0]), b = deriv(xb, p.cd[1]), e = deriv(xe, p.cd[2]);
-            if (sx >= 0) {
-                a = cpml(a, psi[0], np_, p.tab_f[0][x]);
-                p.psi[9][ix] = np_;
-            }
-            if (sy >= 0) {
-                b = cpml(b, psi[1], np_, p.tab_f[1][y]);
-                p.psi[10][iy] = np_;
-            }
-            if (sz >= 0) {
-                e = cpml(e, psi[2], np_, p.tab_f[2][z]);
-                p.psi[11][iz] = np_;
-            }
-            vxn = fmaf(a + b + e, dtx, v0[0]);
-        }
-        if (in_vy) {
-            float a = deriv(ya, p.cd[0]), b = deriv(yb, p.cd[1]), e = deriv(ye, p.cd[2]);
-            if (sx >= 0) {
-                a = cpml(a, psi[3], np_, p.tab_h[0][x]);
-                p.psi[12][ix] = np_;
-            }
-            if (sy >= 0) {
-                b = cpml(b, psi[4], np_, p.tab_h[1][y]);
-                p.psi[13][iy] = np_;
-            }
-            if (sz >= 0) {
-                e = cpml(e, psi[5], np_, p.tab_f[2][z]);
-                p.psi[14][iz] = np_;
-            }
-            vyn = fmaf(a + b + e, dty, v0[1]);
-        }
-        if (in_vz) {
-            float a = deriv(za, p.cd[0]), b = deriv(zb, p.cd[1]), e = deriv(ze, p.cd[2]);
-            if (sx >= 0) {
-                a = cpml(a, psi[6], np_, p.tab_h[0][x]);
-                p.psi[15][ix] = np_;
-            }
-            if (sy >= 0) {
-                b = cpml(b, psi[7], np_, p.tab_f[1][y]);
-                p.psi[16][iy] = np_;
-            }
-            if (sz >= 0) {
-                e = cpml(e, psi[8], np_, p.tab_h[2][z]);
-                p.psi[17][iz] = np_;
-            }
-            vzn = fmaf(a + b + e, dty, v0[2]);  // the vy-node density (wgsl3d:1748)
-        }
-        for (int q = q0; q < q1; ++q) {
-            const Source s = p.src[q];
-            if (s.cell == i && k < p.src_rows)
-                vzn = fmaf(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), s.scale, vzn);
-        }
-        p.v[0][i] = vxn;
-        p.v[1][i] = vyn;
-        p.v[2][i] = vzn;
-        v2 = fmaf(vxn, vxn, fmaf(vyn, vyn, vzn * vzn));
-    }
-
-    const int g = blk * (kBX3 * kBY3 * kBZ3) + tid;
+    // receivers: global thread g samples receiver g (szz is final for step k)
+    const int g = blk * (kBX3 * kBY3) + tid;
     if (g < p.n_rec && k >= __ldg(p.rec_first_step + g)) {
         float acc = 0.f;
-        for (int q = __ldg(p.rec_start + g); q < __ldg(p.rec_start + g + 1); ++q) acc += p.s[2][__ldg(p.rec_cell + q)];
+        for (int q = __ldg(p.rec_start + g); q < __ldg(p.rec_start + g + 1); ++q) acc += fld(szz + __ldg(p.rec_cell + q));
         p.traces[(int64_t)k * p.n_rec + g] = acc;
     }
-
-    warp_stability(v2, live && !(v2 <= p.v2_threshold), reinterpret_cast<unsigned *>(p.block_max) + blk,
-                   p.first_bad, k);
+    warp_stability(vmax, bad, reinterpret_cast<unsigned *>(p.block_max) + blk, p.first_bad, k);
     pdl_trigger();
 }
 
 template <int ORD>
 void launch_ord(const StepParams &p, int zen_mode, int j, cudaStream_t st, int parts) {
-    dim3 block(kBX3, kBY3, kBZ3);
-    dim3 grid((p.nz + kBX3 - 1) / kBX3, (p.ny + kBY3 - 1) / kBY3, (p.nx + kBZ3 - 1) / kBZ3);
+    const dim3 block(kBX3, kBY3);
     const bool three = p.zen.n == 3;
     if (parts & 1) {
-        if (zen_mode == 0) launch_pdl(k_stress3d<ORD, 0, 0>, grid, block, st, p);
-        else if (zen_mode == 1 && three) launch_pdl(k_stress3d<ORD, 1, 3>, grid, block, st, p);
-        else if (zen_mode == 1) launch_pdl(k_stress3d<ORD, 1, kMaxSls>, grid, block, st, p);
-        else if (three) launch_pdl(k_stress3d<ORD, 2, 3>, grid, block, st, p);
-        else launch_pdl(k_stress3d<ORD, 2, kMaxSls>, grid, block, st, p);
+        const dim3 grid((p.nz + kBX3 - 1) / kBX3, (p.ny + kBY3 - 1) / kBY3, (p.nx + kTX3S - 1) / kTX3S);
+        if (zen_mode == 0) {
+            launch_pdl(k_normal3d<ORD, 0, 0>, grid, block, st, p);
+            launch_pdl(k_shear3d<ORD, 0, 0>, grid, block, st, p);
+        } else if (zen_mode == 1 && three) {
+            launch_pdl(k_normal3d<ORD, 1, 3>, grid, block, st, p);
+            launch_pdl(k_shear3d<ORD, 1, 3>, grid, block, st, p);
+        } else if (zen_mode == 1) {
+            launch_pdl(k_normal3d<ORD, 1, kMaxSls>, grid, block, st, p);
+            launch_pdl(k_shear3d<ORD, 1, kMaxSls>, grid, block, st, p);
+        } else if (three) {
+            launch_pdl(k_normal3d<ORD, 2, 3>, grid, block, st, p);
+            launch_pdl(k_shear3d<ORD, 2, 3>, grid, block, st, p);
+        } else {
+            launch_pdl(k_normal3d<ORD, 2, kMaxSls>, grid, block, st, p);
+            launch_pdl(k_shear3d<ORD, 2, kMaxSls>, grid, block, st, p);
+        }
     }
-    if (parts & 2) launch_pdl(k_velocity3d<ORD>, grid, block, st, p, j);
+    if (parts & 2) {
+        const dim3 grid((p.nz + kBX3 - 1) / kBX3, (p.ny + kBY3 - 1) / kBY3, (p.nx + kTX3 - 1) / kTX3);
+        launch_pdl(k_velocity3d<ORD>, grid, block, st, p, j);
+    }
 }
 
 }  // namespace
 
 int blocks_3d(const StepParams &p) {
-    return ((p.nz + kBX3 - 1) / kBX3) * ((p.ny + kBY3 - 1) / kBY3) * ((p.nx + kBZ3 - 1) / kBZ3);
+    return ((p.nz + kBX3 - 1) / kBX3) * ((p.ny + kBY3 - 1) / kBY3) * ((p.nx + kTX3 - 1) / kTX3);
 }
 
 void launch_step_3d(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st, int parts) {
