@@ -43,8 +43,8 @@ struct Pairs {
     float hi[ORD], lo[ORD];
 };
 
-template <int ORD, bool PLUS>
-__device__ __forceinline__ Pairs<ORD> load_pairs(const float *f, int64_t i, int64_t s) {
+template <int ORD, bool PLUS, typename I>
+__device__ __forceinline__ Pairs<ORD> load_pairs(const float *f, I i, I s) {
     Pairs<ORD> r;
 #pragma unroll
     for (int c = 0; c < ORD; ++c) {
@@ -67,9 +67,8 @@ __device__ __forceinline__ float deriv(const Pairs<ORD> &q, const float *cd) {
 constexpr int kStressMinBlocks = 3, kVelocityMinBlocks = 3;
 // x window of 2*ORD planes of one field at (y, z), first plane r0; planes
 // outside the grid read 0
-template <int ORD>
-__device__ __forceinline__ void xwindow(float (&w)[2 * ORD], const float *f, int r0, int nx, int64_t X,
-                                        int64_t yz) {
+template <int ORD, typename I>
+__device__ __forceinline__ void xwindow(float (&w)[2 * ORD], const float *f, int r0, int nx, I X, I yz) {
 #pragma unroll
     for (int j = 0; j < 2 * ORD; ++j) {
         const int r = r0 + j;
@@ -77,9 +76,8 @@ __device__ __forceinline__ void xwindow(float (&w)[2 * ORD], const float *f, int
     }
 }
 
-template <int ORD>
-__device__ __forceinline__ void xshift(float (&w)[2 * ORD], const float *f, int r_new, int nx, int64_t X,
-                                       int64_t yz) {
+template <int ORD, typename I>
+__device__ __forceinline__ void xshift(float (&w)[2 * ORD], const float *f, int r_new, int nx, I X, I yz) {
 #pragma unroll
     for (int j = 0; j < 2 * ORD - 1; ++j) w[j] = w[j + 1];
     w[2 * ORD - 1] = (r_new >= 0 && r_new < nx) ? fld(f + r_new * X + yz) : 0.f;
@@ -98,13 +96,13 @@ __device__ __forceinline__ float wderiv(const float (&w)[2 * ORD], const float *
 // strips), x-marching: thread (z, y) updates kTX3S consecutive nodes along x,
 // the x-derivative of vx from a register window, the y- and z-derivatives
 // from loads.
-template <int ORD, int ZM, int NS>
+template <int ORD, int ZM, int NS, typename I>
 __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_normal3d(const StepParams p) {
     const int z = blockIdx.x * kBX3 + threadIdx.x;
     const int y = blockIdx.y * kBY3 + threadIdx.y;
     const int x0 = blockIdx.z * kTX3S;
     if (y >= p.ny || z >= p.nz || x0 >= p.nx) return;
-    const int64_t X = p.plane, Y = p.pitch, yz = (int64_t)y * Y + z, G = p.grid_elems;
+    const I X = (I)p.plane, Y = (I)p.pitch, yz = (I)y * Y + z, G = (I)p.grid_elems;
     const float *__restrict__ vx = p.v[0];
     const float *__restrict__ vy = p.v[1];
     const float *__restrict__ vz = p.v[2];
@@ -120,14 +118,14 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_normal3d(const
         const int x = x0 + t;
         if (x >= p.nx) break;
         if (yz_n && x >= ORD - 1 && x < p.nx - ORD) {
-            const int64_t i = (int64_t)x * X + yz;
+            const I i = (I)x * X + yz;
             const int sx = strip_index(p.strip[0], x);
-            const int64_t ix = ((int64_t)sx * p.ny + y) * p.pitch + z;
-            const int64_t iy = ((int64_t)x * p.strip[1].width + sy) * p.pitch + z;
-            const int64_t iz = ((int64_t)x * p.ny + y) * p.strip[2].width + sz;
+            const I ix = ((I)sx * p.ny + y) * Y + z;
+            const I iy = ((I)x * p.strip[1].width + sy) * Y + z;
+            const I iz = ((I)x * p.ny + y) * p.strip[2].width + sz;
             // ---- loads ----
             const Pairs<ORD> n_y = load_pairs<ORD, false>(vy, i, Y);   // vy[y+c]-vy[y-c-1]
-            const Pairs<ORD> n_z = load_pairs<ORD, false>(vz, i, 1);   // vz[z+c]-vz[z-c-1]
+            const Pairs<ORD> n_z = load_pairs<ORD, false>(vz, i, (I)1);   // vz[z+c]-vz[z-c-1]
             const float L = __ldg(p.lam_dt + i), M = __ldg(p.mu_dt + i);
             const float gp = ZM == 2 ? __ldg(p.g_p + i) : 1.f, gs = ZM == 2 ? __ldg(p.g_s + i) : 1.f;
             const float s0 = p.s[0][i], s1 = p.s[1][i], s2 = p.s[2][i];
@@ -199,13 +197,13 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_normal3d(const
 // Shear stresses (sxy, sxz, syz with their Zener memory variables and CPML
 // strips), x-marching as k_normal3d: the x-derivatives of vy and vz from
 // register windows.
-template <int ORD, int ZM, int NS>
+template <int ORD, int ZM, int NS, typename I>
 __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_shear3d(const StepParams p) {
     const int z = blockIdx.x * kBX3 + threadIdx.x;
     const int y = blockIdx.y * kBY3 + threadIdx.y;
     const int x0 = blockIdx.z * kTX3S;
     if (y >= p.ny || z >= p.nz || x0 >= p.nx) return;
-    const int64_t X = p.plane, Y = p.pitch, yz = (int64_t)y * Y + z, G = p.grid_elems;
+    const I X = (I)p.plane, Y = (I)p.pitch, yz = (I)y * Y + z, G = (I)p.grid_elems;
     const float *__restrict__ vx = p.v[0];
     const float *__restrict__ vy = p.v[1];
     const float *__restrict__ vz = p.v[2];
@@ -224,11 +222,11 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_shear3d(const 
         const bool in_xy = yz_s && x >= ORD && x < p.nx - ORD + 1;
         const bool in_yz = yz_s && x >= ORD - 1 && x < p.nx - ORD;
         if (in_xy || in_yz) {
-            const int64_t i = (int64_t)x * X + yz;
+            const I i = (I)x * X + yz;
             const int sx = strip_index(p.strip[0], x);
-            const int64_t ix = ((int64_t)sx * p.ny + y) * p.pitch + z;
-            const int64_t iy = ((int64_t)x * p.strip[1].width + sy) * p.pitch + z;
-            const int64_t iz = ((int64_t)x * p.ny + y) * p.strip[2].width + sz;
+            const I ix = ((I)sx * p.ny + y) * Y + z;
+            const I iy = ((I)x * p.strip[1].width + sy) * Y + z;
+            const I iz = ((I)x * p.ny + y) * p.strip[2].width + sz;
             // ---- loads ----
             Pairs<ORD> a_vx, b_vx, c_vz, c_vy;
             float Mxy = 0.f, Mxz = 0.f, Myz = 0.f, s_xy = 0.f, s_xz = 0.f, s_yz = 0.f;
@@ -237,7 +235,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_shear3d(const 
             const float gs = ZM == 2 ? __ldg(p.g_s + i) : 1.f;
             if (in_xy) {
                 a_vx = load_pairs<ORD, true>(vx, i, Y);   // vx[y+c+1]-vx[y-c]
-                b_vx = load_pairs<ORD, true>(vx, i, 1);   // vx[z+c+1]-vx[z-c]
+                b_vx = load_pairs<ORD, true>(vx, i, (I)1);   // vx[z+c+1]-vx[z-c]
                 Mxy = __ldg(p.mus_dt[0] + i);
                 Mxz = __ldg(p.mus_dt[1] + i);
                 s_xy = p.s[3][i];
@@ -259,7 +257,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_shear3d(const 
             }
             if (in_yz) {
                 c_vz = load_pairs<ORD, true>(vz, i, Y);   // vz[y+c+1]-vz[y-c]
-                c_vy = load_pairs<ORD, true>(vy, i, 1);   // vy[z+c+1]-vy[z-c]
+                c_vy = load_pairs<ORD, true>(vy, i, (I)1);   // vy[z+c+1]-vy[z-c]
                 Myz = __ldg(p.mus_dt[2] + i);
                 s_yz = p.s[5][i];
                 if (sy >= 0) psi[4] = p.psi[7][iy];
@@ -347,7 +345,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_shear3d(const 
 // Velocity update, x-marching: thread (z, y) updates kTX3 consecutive nodes
 // along x; the x-derivatives of sxx, sxy, sxz come from register windows that
 // take one new plane per node, the y- and z-derivatives from loads.
-template <int ORD>
+template <int ORD, typename I>
 __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(const StepParams p, const int j) {
     const int z = blockIdx.x * kBX3 + threadIdx.x;
     const int y = blockIdx.y * kBY3 + threadIdx.y;
@@ -355,7 +353,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
     const int tid = threadIdx.y * kBX3 + threadIdx.x;
     const int blk = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
     const bool col = y < p.ny && z < p.nz;
-    const int64_t X = p.plane, Y = p.pitch, yz = (int64_t)y * Y + z;
+    const I X = (I)p.plane, Y = (I)p.pitch, yz = (I)y * Y + z;
     const float *__restrict__ sxx = p.s[0];
     const float *__restrict__ syy = p.s[1];
     const float *__restrict__ szz = p.s[2];
@@ -380,21 +378,21 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
         for (int t = 0; t < kTX3; ++t) {
             const int x = x0 + t;
             if (x >= p.nx) break;
-            const int64_t i = (int64_t)x * X + yz;
+            const I i = (I)x * X + yz;
             const bool in_vz = yz_vz && x >= ORD - 1 && x < p.nx - ORD;
             const bool in_vx = in_vz && x >= ORD && z >= ORD;        // vx region within the vz region
             const bool in_vy = in_vz && y < p.ny - ORD && z >= ORD;  // vy region within the vz region
             const int sx = strip_index(p.strip[0], x);
-            const int64_t ix = ((int64_t)sx * p.ny + y) * p.pitch + z;
-            const int64_t iy = ((int64_t)x * p.strip[1].width + sy) * p.pitch + z;
-            const int64_t iz = ((int64_t)x * p.ny + y) * p.strip[2].width + sz;
+            const I ix = ((I)sx * p.ny + y) * Y + z;
+            const I iy = ((I)x * p.strip[1].width + sy) * Y + z;
+            const I iz = ((I)x * p.ny + y) * p.strip[2].width + sz;
             // ---- loads ----
             Pairs<ORD> xb, xe, yb, ye, zb, ze;
             float v0[3] = {0.f, 0.f, 0.f}, dtx = 0.f, dty = 0.f;
             float psi[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (in_vx) {
                 xb = load_pairs<ORD, false>(sxy, i, Y);
-                xe = load_pairs<ORD, false>(sxz, i, 1);
+                xe = load_pairs<ORD, false>(sxz, i, (I)1);
                 v0[0] = p.v[0][i];
                 dtx = __ldg(p.dtr[0] + i);
                 if (sx >= 0) psi[0] = p.psi[9][ix];
@@ -403,7 +401,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
             }
             if (in_vy) {
                 yb = load_pairs<ORD, true>(syy, i, Y);
-                ye = load_pairs<ORD, false>(syz, i, 1);
+                ye = load_pairs<ORD, false>(syz, i, (I)1);
                 v0[1] = p.v[1][i];
                 if (sx >= 0) psi[3] = p.psi[12][ix];
                 if (sy >= 0) psi[4] = p.psi[13][iy];
@@ -411,7 +409,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
             }
             if (in_vz) {
                 zb = load_pairs<ORD, false>(syz, i, Y);
-                ze = load_pairs<ORD, true>(szz, i, 1);
+                ze = load_pairs<ORD, true>(szz, i, (I)1);
                 v0[2] = p.v[2][i];
                 dty = __ldg(p.dtr[1] + i);
                 if (sx >= 0) psi[6] = p.psi[15][ix];
@@ -502,33 +500,43 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
     pdl_trigger();
 }
 
-template <int ORD>
-void launch_ord(const StepParams &p, int zen_mode, int j, cudaStream_t st, int parts) {
+template <int ORD, typename I>
+void launch_idx(const StepParams &p, int zen_mode, int j, cudaStream_t st, int parts) {
     const dim3 block(kBX3, kBY3);
     const bool three = p.zen.n == 3;
     if (parts & 1) {
         const dim3 grid((p.nz + kBX3 - 1) / kBX3, (p.ny + kBY3 - 1) / kBY3, (p.nx + kTX3S - 1) / kTX3S);
         if (zen_mode == 0) {
-            launch_pdl(k_normal3d<ORD, 0, 0>, grid, block, st, p);
-            launch_pdl(k_shear3d<ORD, 0, 0>, grid, block, st, p);
+            launch_pdl(k_normal3d<ORD, 0, 0, I>, grid, block, st, p);
+            launch_pdl(k_shear3d<ORD, 0, 0, I>, grid, block, st, p);
         } else if (zen_mode == 1 && three) {
-            launch_pdl(k_normal3d<ORD, 1, 3>, grid, block, st, p);
-            launch_pdl(k_shear3d<ORD, 1, 3>, grid, block, st, p);
+            launch_pdl(k_normal3d<ORD, 1, 3, I>, grid, block, st, p);
+            launch_pdl(k_shear3d<ORD, 1, 3, I>, grid, block, st, p);
         } else if (zen_mode == 1) {
-            launch_pdl(k_normal3d<ORD, 1, kMaxSls>, grid, block, st, p);
-            launch_pdl(k_shear3d<ORD, 1, kMaxSls>, grid, block, st, p);
+            launch_pdl(k_normal3d<ORD, 1, kMaxSls, I>, grid, block, st, p);
+            launch_pdl(k_shear3d<ORD, 1, kMaxSls, I>, grid, block, st, p);
         } else if (three) {
-            launch_pdl(k_normal3d<ORD, 2, 3>, grid, block, st, p);
-            launch_pdl(k_shear3d<ORD, 2, 3>, grid, block, st, p);
+            launch_pdl(k_normal3d<ORD, 2, 3, I>, grid, block, st, p);
+            launch_pdl(k_shear3d<ORD, 2, 3, I>, grid, block, st, p);
         } else {
-            launch_pdl(k_normal3d<ORD, 2, kMaxSls>, grid, block, st, p);
-            launch_pdl(k_shear3d<ORD, 2, kMaxSls>, grid, block, st, p);
+            launch_pdl(k_normal3d<ORD, 2, kMaxSls, I>, grid, block, st, p);
+            launch_pdl(k_shear3d<ORD, 2, kMaxSls, I>, grid, block, st, p);
         }
     }
     if (parts & 2) {
         const dim3 grid((p.nz + kBX3 - 1) / kBX3, (p.ny + kBY3 - 1) / kBY3, (p.nx + kTX3 - 1) / kTX3);
-        launch_pdl(k_velocity3d<ORD>, grid, block, st, p, j);
+        launch_pdl(k_velocity3d<ORD, I>, grid, block, st, p, j);
     }
+}
+
+// 32-bit offsets when every array (memory variables included) has fewer
+// than 2^31 elements: fewer integer instructions per load.
+template <int ORD>
+void launch_ord(const StepParams &p, int zen_mode, int j, cudaStream_t st, int parts) {
+    if (p.grid_elems * (int64_t)(p.zen.n > 0 ? p.zen.n : 1) < ((int64_t)1 << 31))
+        launch_idx<ORD, int>(p, zen_mode, j, st, parts);
+    else
+        launch_idx<ORD, int64_t>(p, zen_mode, j, st, parts);
 }
 
 }  // namespace
