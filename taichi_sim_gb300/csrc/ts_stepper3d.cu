@@ -62,9 +62,9 @@ __device__ __forceinline__ float deriv(const Pairs<ORD> &q, const float *cd) {
     return a;
 }
 
-// Resident blocks per SM the kernels are compiled for (register budget
-// 85 per thread; measured against 1, 2 and 4 on the 256^3 case).
-constexpr int kStressMinBlocks = 3, kVelocityMinBlocks = 3;
+// Resident blocks per SM the kernels are compiled for (register budgets 64
+// and 85 per thread; measured against 1 to 4 on the 256^3 case).
+constexpr int kStressMinBlocks = 4, kVelocityMinBlocks = 3;
 // x window of 2*ORD planes of one field at (y, z), first plane r0; planes
 // outside the grid read 0
 template <int ORD, typename I>
