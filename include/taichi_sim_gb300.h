@@ -144,10 +144,10 @@ int ts_reset(ts_sim *sim);
  * state. */
 int ts_reset_async(ts_sim *sim, void *stream);
 
-/* Run n_steps steps launching each kernel between CUDA events on `stream`
- * and return the mean device time per launch of each kernel of a step, in
- * milliseconds (ms_per_kernel[ts_launches_per_step]).  Advances the
- * simulation like ts_run. */
+/* Run n_steps steps, the stress update and the velocity update of each
+ * step between CUDA events on `stream`, and return their mean device times
+ * in milliseconds (ms_per_kernel[2]: stress, velocity; the 3D stress update
+ * is two launches).  Advances the simulation like ts_run. */
 int ts_profile_steps(ts_sim *sim, int32_t n_steps, void *stream, float *ms_per_kernel);
 
 /* Total kernel launches this handle has issued (graph replays count every
@@ -178,10 +178,11 @@ const char *ts_last_error(void);
  * the attenuation model) plus n_shots[p] shots; shot s of phantom p injects,
  * at every node of the phantom's source map, column idx of its own table
  * shot_sources[p][s][n_steps][src_cols] (idx = the map's value).  Traces
- * are [n_shots][n_steps][n_rec] per phantom.  block_cells (0 = 8) and
- * nodes_per_thread (0 = 2) set the launch shape, blocks of 32 shots x
- * block_cells nodes along y with each thread updating nodes_per_thread
- * nodes along x; both are fixed at creation.
+ * are [n_shots][n_steps][n_rec] per phantom.  block_cells (0 = 8),
+ * nodes_per_thread (0 = 2) and shots_per_thread (0 = 1) set the launch
+ * shape: blocks of 32 lanes x block_cells nodes along y, each thread
+ * updating nodes_per_thread nodes along x for shots_per_thread shots; they
+ * are fixed at creation (order-4 batches take the default shape).
  */
 typedef struct ts_batch ts_batch;
 
@@ -192,7 +193,8 @@ typedef struct ts_batch_desc {
     const int32_t *n_shots;           /* [n_phantoms] */
     const float *const *shot_sources; /* [n_phantoms] -> [n_shots][n_steps][src_cols] */
     int32_t block_cells;              /* 0, 4 or 8 */
-    int32_t nodes_per_thread;         /* 0, 1, 2 or 4 */
+    int32_t nodes_per_thread;         /* 0, 1, 2 or 4 (1 or 2 with two shots per thread) */
+    int32_t shots_per_thread;         /* 0, 1 or 2 */
 } ts_batch_desc;
 
 int ts_batch_create(const ts_batch_desc *desc, ts_batch **out);

@@ -27,7 +27,7 @@ class BatchDesc(ctypes.Structure):
     _fields_ = [("abi_version", ctypes.c_int32), ("n_phantoms", ctypes.c_int32),
                 ("phantoms", ctypes.POINTER(engine.TsDesc)), ("n_shots", ctypes.POINTER(ctypes.c_int32)),
                 ("shot_sources", ctypes.POINTER(_f)), ("block_cells", ctypes.c_int32),
-                ("nodes_per_thread", ctypes.c_int32)]
+                ("nodes_per_thread", ctypes.c_int32), ("shots_per_thread", ctypes.c_int32)]
 
 
 def _bind(lib):
@@ -80,7 +80,7 @@ class BatchStepper:
     is ``[n_shots, n_steps, src_cols]`` for phantom p.
     """
 
-    def __init__(self, sims, shot_sources, block_cells=0, nodes_per_thread=0):
+    def __init__(self, sims, shot_sources, block_cells=0, nodes_per_thread=0, shots_per_thread=0):
         self._lib = _bind(engine.load_library())
         self.sims = list(sims)
         self.n_ph = len(self.sims)
@@ -105,7 +105,8 @@ class BatchStepper:
         n_shots = (ctypes.c_int32 * self.n_ph)(*self.n_shots)
         ptrs = (_f * self.n_ph)(*[s.ctypes.data_as(_f) for s in self.shot_sources])
         bd = BatchDesc(abi_version=engine.ABI_VERSION, n_phantoms=self.n_ph, phantoms=descs, n_shots=n_shots,
-                       shot_sources=ptrs, block_cells=int(block_cells), nodes_per_thread=int(nodes_per_thread))
+                       shot_sources=ptrs, block_cells=int(block_cells), nodes_per_thread=int(nodes_per_thread),
+                       shots_per_thread=int(shots_per_thread))
         h = ctypes.c_void_p()
         _check(self._lib, self._lib.ts_batch_create(ctypes.byref(bd), ctypes.byref(h)), "ts_batch_create")
         self._h = h
@@ -182,15 +183,16 @@ def _key(sims, shot_sources):
                       sort_keys=True)
 
 
-SHAPES = ((4, 1), (4, 2), (4, 4), (8, 1), (8, 2), (8, 4))
+SHAPES = ((4, 1, 1), (4, 2, 1), (4, 4, 1), (8, 1, 1), (8, 2, 1), (8, 4, 1), (4, 1, 2), (4, 2, 2), (8, 1, 2), (8, 2, 2))
 
 
 def autotune(sims, shot_sources, candidates=SHAPES, steps=12, use_cache=True):
-    """Pick the launch shape ``(block_cells, nodes_per_thread)`` (blocks of 32
-    shots x block_cells nodes along y, nodes_per_thread nodes along x per
-    thread) with the shortest measured step on this GPU; the choice is cached
-    per problem shape.  Returns ``((block_cells, nodes_per_thread),
-    {"CYxTX": ms_per_step})``."""
+    """Pick the launch shape ``(block_cells, nodes_per_thread, shots_per_thread)``
+    (blocks of 32 lanes x block_cells nodes along y, nodes_per_thread nodes
+    along x and shots_per_thread shots per thread) with the shortest measured
+    step on this GPU; the choice is cached per problem shape.  Order-4 models
+    have the default shape only.  Returns ``((block_cells, nodes_per_thread,
+    shots_per_thread), {"CYxTXxSPT": ms_per_step})``."""
     key = _key(sims, shot_sources)
     path = _cache_path()
     cache = {}
@@ -200,14 +202,16 @@ def autotune(sims, shot_sources, candidates=SHAPES, steps=12, use_cache=True):
                 cache = json.load(f)
         except (OSError, ValueError):
             cache = {}
-        if key in cache and "shape" in cache[key]:
+        if key in cache and len(cache[key].get("shape", ())) == 3:
             return tuple(cache[key]["shape"]), cache[key]["timings"]
     timings = {}
-    for cy, tx in candidates:
-        with BatchStepper(sims, shot_sources, block_cells=cy, nodes_per_thread=tx) as b:
+    if int(sims[0]._coefs.shape[0]) != 2:
+        candidates = ((8, 2, 1),)
+    for cy, tx, spt in candidates:
+        with BatchStepper(sims, shot_sources, block_cells=cy, nodes_per_thread=tx, shots_per_thread=spt) as b:
             b.profile_steps(2)
             ms = b.profile_steps(steps)
-            timings[f"{cy}x{tx}"] = float(sum(ms))
+            timings[f"{cy}x{tx}x{spt}"] = float(sum(ms))
     best_key = min(timings, key=timings.get)
     best = tuple(int(v) for v in best_key.split("x"))
     cache[key] = {"shape": list(best), "timings": timings, "when": time.time()}

@@ -1,15 +1,19 @@
 // Batched 2D (visco)elastic stepping: many shots of several phantoms (grids
 // of uneven sizes) advanced together, one launch per kernel per time step.
 //
-// Layout: per phantom every field is [S/32][nx][ny][32]: blocks of 32 shots
-// (S = shots rounded up to 32), the shot index innermost.  A warp is 32
-// shots of one grid node, so every load and store is one contiguous 128-byte
-// row, neighbouring nodes along y are 128 bytes apart (immediate offsets), the
-// per-node coefficients (lambda*dt, mu*dt, dt/rho, Q scale) are one
-// broadcast load shared by all shots, and the region and CPML-strip tests
-// are uniform across the warp.  Blocks are 32 shots x CY nodes along y;
-// the flat block index runs over (phantom, x, y-block, shot-block), so
-// phantoms of any size share one launch.
+// Layout: per phantom every field is [S/W][nx][ny][W]: blocks of W = 32 or
+// 64 shots (S = shots rounded up to W), the shot index innermost.  A warp
+// covers the W shots of one grid node (one or two per lane), so every load
+// and store is one contiguous 128- or 256-byte row, neighbouring nodes along
+// y are W floats apart (immediate offsets), the per-node coefficients
+// (lambda*dt, mu*dt, dt/rho, Q scale) are one broadcast load shared by all
+// shots, and the region and CPML-strip tests are uniform across the warp.
+// Blocks are 32 lanes x CY nodes along y; each thread updates TX consecutive
+// nodes along x, keeping the x-stencil rows in a register window (one new
+// row per node), for SPT shots.  The flat block index runs over (phantom,
+// x-chunk, y-block, shot-block), so phantoms of any size share one launch.
+// The phantom records are a __grid_constant__ parameter (constant cache, no
+// aliasing with the fields) and offsets are 32-bit (checked at creation).
 //
 // Semantics: the WGSL 2D kernels (shader_webgpu_viscoelastic.wgsl:829-1072
 // and :1118-1134) per shot, except for the source columns: shot s injects
@@ -40,7 +44,7 @@ struct BSrc {
 };
 
 struct BPh {
-    int nx, ny, S, n_shots;
+    int nx, ny, S, W, n_shots;   // S shots padded to a multiple of W (shots per block row: 32 or 64)
     int G;      // nx * ny * S (checked < 2^31 with the memory variables)
     int block0, xchunks, yblocks, sblocks;
     float cd[2][kMaxOrd];
@@ -80,14 +84,16 @@ __device__ __forceinline__ float cpml(float d, float psi_old, float &psi_new, co
 
 struct Loc {
     const BPh *ph;
-    int x0, y, s, lane, cell0;
+    int x0, y, sb, lane, s0, cell0;
     int i0;
     bool live;
 };
 
 // Block b of a launch: phantom, then (x-chunk, y-block, shot-block) within it.
-template <int CY, int TX>
+// W = 32 * SPT shots per shot block: lane l owns shots SPT l .. SPT l + SPT-1.
+template <int CY, int TX, int SPT>
 __device__ __forceinline__ Loc locate(const BParams &p) {
+    constexpr int W = 32 * SPT;
     const int b = blockIdx.x;
     int q = 0;
 #pragma unroll 1
@@ -96,52 +102,94 @@ __device__ __forceinline__ Loc locate(const BParams &p) {
     L.ph = p.ph + q;
     const BPh &h = *L.ph;
     const int local = b - h.block0;
-    const int sb = local % h.sblocks, t = local / h.sblocks;
+    L.sb = local % h.sblocks;
+    const int t = local / h.sblocks;
     const int yb = t % h.yblocks;
     L.x0 = (t / h.yblocks) * TX;
     L.y = yb * CY + threadIdx.y;
     L.lane = threadIdx.x;
-    L.s = sb * 32 + L.lane;
+    L.s0 = L.sb * W + L.lane * SPT;
     L.live = L.y < h.ny && L.x0 < h.nx;
     L.cell0 = L.x0 * h.ny + L.y;
-    L.i0 = ((sb * h.nx + L.x0) * h.ny + L.y) * 32 + L.lane;
+    L.i0 = ((L.sb * h.nx + L.x0) * h.ny + L.y) * W + L.lane * SPT;
     return L;
 }
 
-// Rows r0 .. r0+2*ORD-1 of one field at (y, shot), zero outside the grid.
-// Fields written by the previous kernel of the stream are read with
-// ld.global.ca, never through the non-coherent path: with programmatic
-// dependent launch that kernel overlaps this one's lifetime.
-template <int ORD>
-__device__ __forceinline__ void bwindow(float (&w)[2 * ORD], const float *f, int r0, int nx, int X, int col) {
+// SPT consecutive shots of one node.  ldf: a field the previous kernel of the
+// stream wrote, read with ld.global.ca, never through the non-coherent path
+// (with programmatic dependent launch that kernel overlaps this one's
+// lifetime); ldo / sto: the node's own state.
+template <int SPT>
+__device__ __forceinline__ void ldf(float (&o)[SPT], const float *q) {
+    if constexpr (SPT == 2) {
+        const float2 v = __ldca(reinterpret_cast<const float2 *>(q));
+        o[0] = v.x;
+        o[1] = v.y;
+    } else {
+        o[0] = __ldca(q);
+    }
+}
+template <int SPT>
+__device__ __forceinline__ void ldo(float (&o)[SPT], const float *q) {
+    if constexpr (SPT == 2) {
+        const float2 v = *reinterpret_cast<const float2 *>(q);
+        o[0] = v.x;
+        o[1] = v.y;
+    } else {
+        o[0] = *q;
+    }
+}
+template <int SPT>
+__device__ __forceinline__ void sto(float *q, const float (&v)[SPT]) {
+    if constexpr (SPT == 2) *reinterpret_cast<float2 *>(q) = make_float2(v[0], v[1]);
+    else *q = v[0];
+}
+
+// Rows r0 .. r0+2*ORD-1 of one field at (y, shots), zero outside the grid.
+template <int ORD, int SPT>
+__device__ __forceinline__ void bwindow(float (&w)[2 * ORD][SPT], const float *f, int r0, int nx, int X, int col) {
 #pragma unroll
     for (int j = 0; j < 2 * ORD; ++j) {
         const int r = r0 + j;
-        w[j] = (r >= 0 && r < nx) ? __ldca(f + r * X + col) : 0.f;
+        if (r >= 0 && r < nx) ldf<SPT>(w[j], f + r * X + col);
+        else
+#pragma unroll
+            for (int q = 0; q < SPT; ++q) w[j][q] = 0.f;
     }
 }
 
-template <int ORD>
-__device__ __forceinline__ void bshift(float (&w)[2 * ORD], const float *f, int r_new, int nx, int X, int col) {
+template <int ORD, int SPT>
+__device__ __forceinline__ void bshift(float (&w)[2 * ORD][SPT], const float *f, int r_new, int nx, int X, int col) {
 #pragma unroll
-    for (int j = 0; j < 2 * ORD - 1; ++j) w[j] = w[j + 1];
-    w[2 * ORD - 1] = (r_new >= 0 && r_new < nx) ? __ldca(f + r_new * X + col) : 0.f;
+    for (int j = 0; j < 2 * ORD - 1; ++j)
+#pragma unroll
+        for (int q = 0; q < SPT; ++q) w[j][q] = w[j + 1][q];
+    if (r_new >= 0 && r_new < nx) ldf<SPT>(w[2 * ORD - 1], f + r_new * X + col);
+    else
+#pragma unroll
+        for (int q = 0; q < SPT; ++q) w[2 * ORD - 1][q] = 0.f;
 }
 
-template <int ORD, int ZM, int NS, int CY, int TX>
-__global__ void __launch_bounds__(32 * CY, 32 / CY) k_bstress(const __grid_constant__ BParams p) {
-    const Loc at = locate<CY, TX>(p);
+// Register budget: 64 per thread for one shot per thread, 128 for two.
+template <int CY, int SPT>
+struct MinBlocks {
+    static constexpr int v = (SPT == 1 ? 32 : 16) / CY;
+};
+
+template <int ORD, int ZM, int NS, int CY, int TX, int SPT>
+__global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bstress(const __grid_constant__ BParams p) {
+    constexpr int W = 32 * SPT, Y = W;
+    const Loc at = locate<CY, TX, SPT>(p);
     if (!at.live) return;
     const BPh &h = *at.ph;
     const int y = at.y, nx = h.nx;
-    constexpr int Y = 32;
-    const int X = h.ny * 32, sb = at.s >> 5, col = (sb * h.nx * h.ny + y) * 32 + at.lane;
+    const int X = h.ny * W, col = (at.sb * h.nx * h.ny + y) * W + at.lane * SPT;
     const bool yn = y >= ORD && y < h.ny - ORD + 1;
     const bool ys = y >= ORD - 1 && y < h.ny - ORD;
     const int sy = strip_index(h.strip[1], y);
     const int n_mech = NS == 3 ? 3 : p.zen.n;
     constexpr int R = NS > 0 ? NS : 1;
-    const float *__restrict__ vx = h.v[0];   // read with __ldca only
+    const float *__restrict__ vx = h.v[0];   // read with ldf only
     const float *__restrict__ vy = h.v[1];
     float *__restrict__ s0 = h.s[0];
     float *__restrict__ s1 = h.s[1];
@@ -151,9 +199,9 @@ __global__ void __launch_bounds__(32 * CY, 32 / CY) k_bstress(const __grid_const
     float *__restrict__ r2 = h.r[2];
     pdl_wait();
     // vx rows [x-ORD+1, x+ORD] (normal x-derivative), vy rows [x-ORD, x+ORD-1] (shear)
-    float wvx[2 * ORD], wvy[2 * ORD];
-    bwindow<ORD>(wvx, vx, at.x0 - ORD + 1, nx, X, col);
-    bwindow<ORD>(wvy, vy, at.x0 - ORD, nx, X, col);
+    float wvx[2 * ORD][SPT], wvy[2 * ORD][SPT];
+    bwindow<ORD, SPT>(wvx, vx, at.x0 - ORD + 1, nx, X, col);
+    bwindow<ORD, SPT>(wvy, vy, at.x0 - ORD, nx, X, col);
 #pragma unroll
     for (int t = 0; t < TX; ++t) {
         const int x = at.x0 + t;
@@ -164,32 +212,32 @@ __global__ void __launch_bounds__(32 * CY, 32 / CY) k_bstress(const __grid_const
         const bool in_s = ys && x >= ORD && x < nx - ORD + 1;
         if (in_n || in_s) {
             const int sx = strip_index(h.strip[0], x);
-            const int ix = ((sb * h.strip[0].width + sx) * h.ny + y) * 32 + at.lane;
-            const int iy = ((sb * h.nx + x) * h.strip[1].width + sy) * 32 + at.lane;
+            const int ix = ((at.sb * h.strip[0].width + sx) * h.ny + y) * W + at.lane * SPT;
+            const int iy = ((at.sb * h.nx + x) * h.strip[1].width + sy) * W + at.lane * SPT;
             // ---- loads ----
-            float L = 0.f, M = 0.f, Ms = 0.f, gp = 1.f, gs = 1.f, sxx = 0.f, syy = 0.f, sxy = 0.f;
-            float ny_lo[ORD], ny_hi[ORD], sx_lo[ORD], sx_hi[ORD];
-            float rxx[R], ryy[R], rxy[R];
-            float pn0 = 0.f, pn1 = 0.f, ps0 = 0.f, ps1 = 0.f;
+            float L = 0.f, M = 0.f, Ms = 0.f, gp = 1.f, gs = 1.f;
+            float sxx[SPT], syy[SPT], sxy[SPT], pn0[SPT], pn1[SPT], ps0[SPT], ps1[SPT];
+            float ny_lo[ORD][SPT], ny_hi[ORD][SPT], sx_lo[ORD][SPT], sx_hi[ORD][SPT];
+            float rxx[R][SPT], ryy[R][SPT], rxy[R][SPT];
             if (in_n) {
                 L = __ldg(h.lam + cell);
                 M = __ldg(h.mu + cell);
                 if (ZM == 2) gp = __ldg(h.gp + cell);
 #pragma unroll
                 for (int c = 0; c < ORD; ++c) {
-                    ny_hi[c] = __ldca(vy + i + c * Y);         // vy[y+c]
-                    ny_lo[c] = __ldca(vy + i - (c + 1) * Y);   // vy[y-c-1]
+                    ldf<SPT>(ny_hi[c], vy + i + c * Y);         // vy[y+c]
+                    ldf<SPT>(ny_lo[c], vy + i - (c + 1) * Y);   // vy[y-c-1]
                 }
-                sxx = s0[i];
-                syy = s1[i];
-                if (sx >= 0) pn0 = h.psi[0][ix];
-                if (sy >= 0) pn1 = h.psi[2][iy];
+                ldo<SPT>(sxx, s0 + i);
+                ldo<SPT>(syy, s1 + i);
+                if (sx >= 0) ldo<SPT>(pn0, h.psi[0] + ix);
+                if (sy >= 0) ldo<SPT>(pn1, h.psi[2] + iy);
                 if (ZM != 0) {
 #pragma unroll
                     for (int l = 0; l < R; ++l)
                         if (l < n_mech) {
-                            rxx[l] = r0[l * h.G + i];
-                            ryy[l] = r1[l * h.G + i];
+                            ldo<SPT>(rxx[l], r0 + l * h.G + i);
+                            ldo<SPT>(ryy[l], r1 + l * h.G + i);
                         }
                 }
             }
@@ -197,122 +245,138 @@ __global__ void __launch_bounds__(32 * CY, 32 / CY) k_bstress(const __grid_const
                 Ms = __ldg(h.mus + cell);
 #pragma unroll
                 for (int c = 0; c < ORD; ++c) {
-                    sx_hi[c] = __ldca(vx + i + (c + 1) * Y);   // vx[y+c+1]
-                    sx_lo[c] = __ldca(vx + i - c * Y);         // vx[y-c]
+                    ldf<SPT>(sx_hi[c], vx + i + (c + 1) * Y);   // vx[y+c+1]
+                    ldf<SPT>(sx_lo[c], vx + i - c * Y);         // vx[y-c]
                 }
-                sxy = s2[i];
-                if (sx >= 0) ps0 = h.psi[1][ix];
-                if (sy >= 0) ps1 = h.psi[3][iy];
+                ldo<SPT>(sxy, s2 + i);
+                if (sx >= 0) ldo<SPT>(ps0, h.psi[1] + ix);
+                if (sy >= 0) ldo<SPT>(ps1, h.psi[3] + iy);
                 if (ZM != 0) {
 #pragma unroll
                     for (int l = 0; l < R; ++l)
-                        if (l < n_mech) rxy[l] = r2[l * h.G + i];
+                        if (l < n_mech) ldo<SPT>(rxy[l], r2 + l * h.G + i);
                 }
             }
             if (ZM == 2) gs = __ldg(h.gs + cell);
             // ---- normal stresses ----
             if (in_n) {
-                float ddx = 0.f, ddy = 0.f, np_;
+                float ux[SPT], uy[SPT], pn0n[SPT], pn1n[SPT];
+                float ra[R][SPT], rb[R][SPT];
 #pragma unroll
-                for (int c = 0; c < ORD; ++c) {
-                    ddx = fmaf(h.cd[0][c], wvx[c + ORD] - wvx[ORD - 1 - c], ddx);
-                    ddy = fmaf(h.cd[1][c], ny_hi[c] - ny_lo[c], ddy);
+                for (int q = 0; q < SPT; ++q) {
+                    float ddx = 0.f, ddy = 0.f;
+#pragma unroll
+                    for (int c = 0; c < ORD; ++c) {
+                        ddx = fmaf(h.cd[0][c], wvx[c + ORD][q] - wvx[ORD - 1 - c][q], ddx);
+                        ddy = fmaf(h.cd[1][c], ny_hi[c][q] - ny_lo[c][q], ddy);
+                    }
+                    if (sx >= 0) ddx = cpml(ddx, pn0[q], pn0n[q], h.tab_h[0][x]);
+                    if (sy >= 0) ddy = cpml(ddy, pn1[q], pn1n[q], h.tab_f[1][y]);
+                    const float L2M = fmaf(2.f, M, L);
+                    ux[q] = fmaf(L2M, ddx, L * ddy);
+                    uy[q] = fmaf(L, ddx, L2M * ddy);
+                    if (ZM != 0) {
+                        float srxx = 0.f, sryy = 0.f;
+                        const float dsum = ddx + ddy, ddif = 0.5f * (ddx - ddy);
+#pragma unroll
+                        for (int l = 0; l < R; ++l)
+                            if (l < n_mech) {
+                                ra[l][q] = fmaf(p.zen.Ap[l], rxx[l][q], (p.zen.Bp[l] * gp) * dsum);
+                                rb[l][q] = fmaf(p.zen.As[l], ryy[l][q], (p.zen.Bs[l] * gs) * ddif);
+                                srxx += rxx[l][q] + ra[l][q];
+                                sryy += ryy[l][q] + rb[l][q];
+                            }
+                        const float hl = 0.5f * (L + M);
+                        ux[q] = fmaf(hl, srxx, fmaf(M, sryy, ux[q]));
+                        uy[q] = fmaf(hl, srxx, fmaf(-M, sryy, uy[q]));
+                    }
+                    ux[q] += sxx[q];
+                    uy[q] += syy[q];
                 }
-                if (sx >= 0) {
-                    ddx = cpml(ddx, pn0, np_, h.tab_h[0][x]);
-                    h.psi[0][ix] = np_;
-                }
-                if (sy >= 0) {
-                    ddy = cpml(ddy, pn1, np_, h.tab_f[1][y]);
-                    h.psi[2][iy] = np_;
-                }
-                const float L2M = fmaf(2.f, M, L);
-                float ux = fmaf(L2M, ddx, L * ddy), uy = fmaf(L, ddx, L2M * ddy);
+                if (sx >= 0) sto<SPT>(h.psi[0] + ix, pn0n);
+                if (sy >= 0) sto<SPT>(h.psi[2] + iy, pn1n);
                 if (ZM != 0) {
-                    float srxx = 0.f, sryy = 0.f;
-                    const float dsum = ddx + ddy, ddif = 0.5f * (ddx - ddy);
 #pragma unroll
                     for (int l = 0; l < R; ++l)
                         if (l < n_mech) {
-                            const float a = fmaf(p.zen.Ap[l], rxx[l], (p.zen.Bp[l] * gp) * dsum);
-                            const float b = fmaf(p.zen.As[l], ryy[l], (p.zen.Bs[l] * gs) * ddif);
-                            srxx += rxx[l] + a;
-                            sryy += ryy[l] + b;
-                            r0[l * h.G + i] = a;
-                            r1[l * h.G + i] = b;
+                            sto<SPT>(r0 + l * h.G + i, ra[l]);
+                            sto<SPT>(r1 + l * h.G + i, rb[l]);
                         }
-                    const float hl = 0.5f * (L + M);
-                    ux = fmaf(hl, srxx, fmaf(M, sryy, ux));
-                    uy = fmaf(hl, srxx, fmaf(-M, sryy, uy));
                 }
-                s0[i] = sxx + ux;
-                s1[i] = syy + uy;
+                sto<SPT>(s0 + i, ux);
+                sto<SPT>(s1 + i, uy);
             }
             // ---- shear stress ----
             if (in_s) {
-                float a = 0.f, b = 0.f, np_;
+                float u[SPT], ps0n[SPT], ps1n[SPT], rn[R][SPT];
 #pragma unroll
-                for (int c = 0; c < ORD; ++c) {
-                    a = fmaf(h.cd[0][c], wvy[c + ORD] - wvy[ORD - 1 - c], a);
-                    b = fmaf(h.cd[1][c], sx_hi[c] - sx_lo[c], b);
+                for (int q = 0; q < SPT; ++q) {
+                    float a = 0.f, b = 0.f;
+#pragma unroll
+                    for (int c = 0; c < ORD; ++c) {
+                        a = fmaf(h.cd[0][c], wvy[c + ORD][q] - wvy[ORD - 1 - c][q], a);
+                        b = fmaf(h.cd[1][c], sx_hi[c][q] - sx_lo[c][q], b);
+                    }
+                    if (sx >= 0) a = cpml(a, ps0[q], ps0n[q], h.tab_f[0][x]);
+                    if (sy >= 0) b = cpml(b, ps1[q], ps1n[q], h.tab_h[1][y]);
+                    const float e = a + b;
+                    u[q] = Ms * e;
+                    if (ZM != 0) {
+                        float sr = 0.f;
+#pragma unroll
+                        for (int l = 0; l < R; ++l)
+                            if (l < n_mech) {
+                                rn[l][q] = fmaf(p.zen.As[l], rxy[l][q], (p.zen.Bs[l] * gs) * e);
+                                sr += rxy[l][q] + rn[l][q];
+                            }
+                        u[q] = fmaf(0.5f * Ms, sr, u[q]);
+                    }
+                    u[q] += sxy[q];
                 }
-                if (sx >= 0) {
-                    a = cpml(a, ps0, np_, h.tab_f[0][x]);
-                    h.psi[1][ix] = np_;
-                }
-                if (sy >= 0) {
-                    b = cpml(b, ps1, np_, h.tab_h[1][y]);
-                    h.psi[3][iy] = np_;
-                }
-                const float e = a + b;
-                float u = Ms * e;
+                if (sx >= 0) sto<SPT>(h.psi[1] + ix, ps0n);
+                if (sy >= 0) sto<SPT>(h.psi[3] + iy, ps1n);
                 if (ZM != 0) {
-                    float sr = 0.f;
 #pragma unroll
                     for (int l = 0; l < R; ++l)
-                        if (l < n_mech) {
-                            const float n_ = fmaf(p.zen.As[l], rxy[l], (p.zen.Bs[l] * gs) * e);
-                            sr += rxy[l] + n_;
-                            r2[l * h.G + i] = n_;
-                        }
-                    u = fmaf(0.5f * Ms, sr, u);
+                        if (l < n_mech) sto<SPT>(r2 + l * h.G + i, rn[l]);
                 }
-                s2[i] = sxy + u;
+                sto<SPT>(s2 + i, u);
             }
         }
         if (t + 1 < TX) {
-            bshift<ORD>(wvx, vx, x + ORD + 1, nx, X, col);
-            bshift<ORD>(wvy, vy, x + ORD, nx, X, col);
+            bshift<ORD, SPT>(wvx, vx, x + ORD + 1, nx, X, col);
+            bshift<ORD, SPT>(wvy, vy, x + ORD, nx, X, col);
         }
     }
     pdl_trigger();
 }
 
-template <int ORD, int CY, int TX>
-__global__ void __launch_bounds__(32 * CY, 32 / CY) k_bvelocity(const __grid_constant__ BParams p, const int j) {
-    const Loc at = locate<CY, TX>(p);
+template <int ORD, int CY, int TX, int SPT>
+__global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bvelocity(const __grid_constant__ BParams p,
+                                                                              const int j) {
+    constexpr int W = 32 * SPT, Y = W;
+    const Loc at = locate<CY, TX, SPT>(p);
     const BPh &h = *at.ph;
     const int y = at.y, nx = h.nx;
-    constexpr int Y = 32;
-    const int X = h.ny * 32, sb = at.s >> 5, col = (sb * h.nx * h.ny + y) * 32 + at.lane;
+    const int X = h.ny * W, col = (at.sb * h.nx * h.ny + y) * W + at.lane * SPT;
     const bool yvy = y >= ORD - 1 && y < h.ny - ORD;
     const bool yvx = yvy && y >= ORD;
     const int sy = at.live ? strip_index(h.strip[1], y) : -1;
     const int yb = y / CY;
-    pdl_wait();
-    const int k = *p.step_base + j;
-    const float *__restrict__ sxx = h.s[0];  // read with __ldca only
+    const float *__restrict__ sxx = h.s[0];  // read with ldf only
     const float *__restrict__ syy = h.s[1];
     const float *__restrict__ sxy = h.s[2];
     float *__restrict__ v0 = h.v[0];
     float *__restrict__ v1 = h.v[1];
+    pdl_wait();
+    const int k = *p.step_base + j;
     float vmax = 0.f;
     bool bad = false;
     if (at.live) {
         // sxx rows [x-ORD, x+ORD-1] (vx), sxy rows [x-ORD+1, x+ORD] (vy)
-        float wxx[2 * ORD], wxy[2 * ORD];
-        bwindow<ORD>(wxx, sxx, at.x0 - ORD, nx, X, col);
-        bwindow<ORD>(wxy, sxy, at.x0 - ORD + 1, nx, X, col);
+        float wxx[2 * ORD][SPT], wxy[2 * ORD][SPT];
+        bwindow<ORD, SPT>(wxx, sxx, at.x0 - ORD, nx, X, col);
+        bwindow<ORD, SPT>(wxy, sxy, at.x0 - ORD + 1, nx, X, col);
 #pragma unroll
         for (int t = 0; t < TX; ++t) {
             const int x = at.x0 + t;
@@ -322,85 +386,89 @@ __global__ void __launch_bounds__(32 * CY, 32 / CY) k_bvelocity(const __grid_con
             const bool in_vy = yvy && x >= ORD - 1 && x < nx - ORD;
             const bool in_vx = yvx && in_vy && x >= ORD;
             const int sx = strip_index(h.strip[0], x);
-            const int ix = ((sb * h.strip[0].width + sx) * h.ny + y) * 32 + at.lane;
-            const int iy = ((sb * h.nx + x) * h.strip[1].width + sy) * 32 + at.lane;
+            const int ix = ((at.sb * h.strip[0].width + sx) * h.ny + y) * W + at.lane * SPT;
+            const int iy = ((at.sb * h.nx + x) * h.strip[1].width + sy) * W + at.lane * SPT;
             // ---- loads ----
-            float bx_hi[ORD], bx_lo[ORD], by_hi[ORD], by_lo[ORD];
-            float vx0 = 0.f, vy0 = 0.f, dx0 = 0.f, dy0 = 0.f, pxa = 0.f, pxb = 0.f, pya = 0.f, pyb = 0.f;
+            float bx_hi[ORD][SPT], bx_lo[ORD][SPT], by_hi[ORD][SPT], by_lo[ORD][SPT];
+            float vx0[SPT], vy0[SPT], pxa[SPT], pxb[SPT], pya[SPT], pyb[SPT];
+            float dx0 = 0.f, dy0 = 0.f;
             if (in_vx) {
 #pragma unroll
                 for (int c = 0; c < ORD; ++c) {
-                    bx_hi[c] = __ldca(sxy + i + c * Y);         // sxy[y+c]
-                    bx_lo[c] = __ldca(sxy + i - (c + 1) * Y);   // sxy[y-c-1]
+                    ldf<SPT>(bx_hi[c], sxy + i + c * Y);         // sxy[y+c]
+                    ldf<SPT>(bx_lo[c], sxy + i - (c + 1) * Y);   // sxy[y-c-1]
                 }
-                vx0 = v0[i];
+                ldo<SPT>(vx0, v0 + i);
                 dx0 = __ldg(h.dtr0 + cell);
-                if (sx >= 0) pxa = h.psi[4][ix];
-                if (sy >= 0) pxb = h.psi[6][iy];
+                if (sx >= 0) ldo<SPT>(pxa, h.psi[4] + ix);
+                if (sy >= 0) ldo<SPT>(pxb, h.psi[6] + iy);
             }
             if (in_vy) {
 #pragma unroll
                 for (int c = 0; c < ORD; ++c) {
-                    by_hi[c] = __ldca(syy + i + (c + 1) * Y);   // syy[y+c+1]
-                    by_lo[c] = __ldca(syy + i - c * Y);         // syy[y-c]
+                    ldf<SPT>(by_hi[c], syy + i + (c + 1) * Y);   // syy[y+c+1]
+                    ldf<SPT>(by_lo[c], syy + i - c * Y);         // syy[y-c]
                 }
-                vy0 = v1[i];
+                ldo<SPT>(vy0, v1 + i);
                 dy0 = __ldg(h.dtr1 + cell);
-                if (sx >= 0) pya = h.psi[5][ix];
-                if (sy >= 0) pyb = h.psi[7][iy];
+                if (sx >= 0) ldo<SPT>(pya, h.psi[5] + ix);
+                if (sy >= 0) ldo<SPT>(pyb, h.psi[7] + iy);
             }
             const int q0 = __ldg(h.src_start + x * h.yblocks + yb), q1 = __ldg(h.src_start + x * h.yblocks + yb + 1);
             // ---- update ----
-            float vxn = 0.f, vyn = 0.f, np_;
-            if (in_vx) {
-                float a = 0.f, b = 0.f;
+            float vxn[SPT], vyn[SPT], pxan[SPT], pxbn[SPT], pyan[SPT], pybn[SPT];
 #pragma unroll
-                for (int c = 0; c < ORD; ++c) {
-                    a = fmaf(h.cd[0][c], wxx[c + ORD] - wxx[ORD - 1 - c], a);
-                    b = fmaf(h.cd[1][c], bx_hi[c] - bx_lo[c], b);
+            for (int q = 0; q < SPT; ++q) {
+                vxn[q] = 0.f;
+                vyn[q] = 0.f;
+                if (in_vx) {
+                    float a = 0.f, b = 0.f;
+#pragma unroll
+                    for (int c = 0; c < ORD; ++c) {
+                        a = fmaf(h.cd[0][c], wxx[c + ORD][q] - wxx[ORD - 1 - c][q], a);
+                        b = fmaf(h.cd[1][c], bx_hi[c][q] - bx_lo[c][q], b);
+                    }
+                    if (sx >= 0) a = cpml(a, pxa[q], pxan[q], h.tab_f[0][x]);
+                    if (sy >= 0) b = cpml(b, pxb[q], pxbn[q], h.tab_f[1][y]);
+                    vxn[q] = fmaf(a + b, dx0, vx0[q]);
                 }
-                if (sx >= 0) {
-                    a = cpml(a, pxa, np_, h.tab_f[0][x]);
-                    h.psi[4][ix] = np_;
+                if (in_vy) {
+                    float a = 0.f, b = 0.f;
+#pragma unroll
+                    for (int c = 0; c < ORD; ++c) {
+                        a = fmaf(h.cd[0][c], wxy[c + ORD][q] - wxy[ORD - 1 - c][q], a);
+                        b = fmaf(h.cd[1][c], by_hi[c][q] - by_lo[c][q], b);
+                    }
+                    if (sx >= 0) a = cpml(a, pya[q], pyan[q], h.tab_h[0][x]);
+                    if (sy >= 0) b = cpml(b, pyb[q], pybn[q], h.tab_h[1][y]);
+                    vyn[q] = fmaf(a + b, dy0, vy0[q]);
                 }
-                if (sy >= 0) {
-                    b = cpml(b, pxb, np_, h.tab_f[1][y]);
-                    h.psi[6][iy] = np_;
-                }
-                vxn = fmaf(a + b, dx0, vx0);
+                const int shot = at.s0 + q;
+                if (shot < h.n_shots && k < p.rows)
+                    for (int qq = q0; qq < q1; ++qq) {
+                        const BSrc s = h.src[qq];
+                        if (s.cell == cell)
+                            vyn[q] = fmaf(__ldg(h.shot_tab + ((int64_t)shot * p.rows + k) * h.ncol + s.col), s.scale,
+                                          vyn[q]);
+                    }
+                const float v2 = fmaf(vxn[q], vxn[q], vyn[q] * vyn[q]);
+                bad |= !(v2 <= p.v2_threshold);
+                vmax = fmaxf(vmax, v2);
+                if (v2 != v2) vmax = v2;  // keep a NaN visible
+            }
+            if (in_vx) {
+                if (sx >= 0) sto<SPT>(h.psi[4] + ix, pxan);
+                if (sy >= 0) sto<SPT>(h.psi[6] + iy, pxbn);
             }
             if (in_vy) {
-                float a = 0.f, b = 0.f;
-#pragma unroll
-                for (int c = 0; c < ORD; ++c) {
-                    a = fmaf(h.cd[0][c], wxy[c + ORD] - wxy[ORD - 1 - c], a);
-                    b = fmaf(h.cd[1][c], by_hi[c] - by_lo[c], b);
-                }
-                if (sx >= 0) {
-                    a = cpml(a, pya, np_, h.tab_h[0][x]);
-                    h.psi[5][ix] = np_;
-                }
-                if (sy >= 0) {
-                    b = cpml(b, pyb, np_, h.tab_h[1][y]);
-                    h.psi[7][iy] = np_;
-                }
-                vyn = fmaf(a + b, dy0, vy0);
+                if (sx >= 0) sto<SPT>(h.psi[5] + ix, pyan);
+                if (sy >= 0) sto<SPT>(h.psi[7] + iy, pybn);
             }
-            if (at.s < h.n_shots && k < p.rows)
-                for (int q = q0; q < q1; ++q) {
-                    const BSrc s = h.src[q];
-                    if (s.cell == cell)
-                        vyn = fmaf(__ldg(h.shot_tab + ((int64_t)at.s * p.rows + k) * h.ncol + s.col), s.scale, vyn);
-                }
-            v0[i] = vxn;
-            v1[i] = vyn;
-            const float v2 = fmaf(vxn, vxn, vyn * vyn);
-            bad |= !(v2 <= p.v2_threshold);
-            vmax = fmaxf(vmax, v2);
-            if (v2 != v2) vmax = v2;  // keep a NaN visible
+            sto<SPT>(v0 + i, vxn);
+            sto<SPT>(v1 + i, vyn);
             if (t + 1 < TX) {
-                bshift<ORD>(wxx, sxx, x + ORD, nx, X, col);
-                bshift<ORD>(wxy, sxy, x + ORD + 1, nx, X, col);
+                bshift<ORD, SPT>(wxx, sxx, x + ORD, nx, X, col);
+                bshift<ORD, SPT>(wxy, sxy, x + ORD + 1, nx, X, col);
             }
         }
     }
@@ -414,7 +482,7 @@ __global__ void __launch_bounds__(32 * CY, 32 / CY) k_bvelocity(const __grid_con
         if (k >= __ldg(r.rec_first + rec)) {
             float acc = 0.f;
             for (int t = __ldg(r.rec_start + rec); t < __ldg(r.rec_start + rec + 1); ++t)
-                acc += __ldca(r.s[1] + ((shot >> 5) * r.nx * r.ny + __ldg(r.rec_cell + t)) * 32 + (shot & 31));
+                acc += __ldca(r.s[1] + ((shot / r.W) * r.nx * r.ny + __ldg(r.rec_cell + t)) * r.W + shot % r.W);
             r.traces[((int64_t)shot * p.rows + k) * r.n_rec + rec] = acc;
         }
     }
@@ -422,37 +490,47 @@ __global__ void __launch_bounds__(32 * CY, 32 / CY) k_bvelocity(const __grid_con
     pdl_trigger();
 }
 
-template <int ORD, int CY, int TX>
+template <int ORD, int CY, int TX, int SPT>
 void launch_shape(const BParams &p, int n_blocks, int zen_mode, int j, cudaStream_t st, int parts) {
     const dim3 block(32, CY), grid(n_blocks);
     const bool three = p.zen.n == 3;
-
     if (parts & 1) {
-        if (zen_mode == 0) launch_pdl(k_bstress<ORD, 0, 0, CY, TX>, grid, block, st, p);
-        else if (zen_mode == 1 && three) launch_pdl(k_bstress<ORD, 1, 3, CY, TX>, grid, block, st, p);
-        else if (zen_mode == 1) launch_pdl(k_bstress<ORD, 1, kMaxSls, CY, TX>, grid, block, st, p);
-        else if (three) launch_pdl(k_bstress<ORD, 2, 3, CY, TX>, grid, block, st, p);
-        else launch_pdl(k_bstress<ORD, 2, kMaxSls, CY, TX>, grid, block, st, p);
+        if (zen_mode == 0) launch_pdl(k_bstress<ORD, 0, 0, CY, TX, SPT>, grid, block, st, p);
+        else if (zen_mode == 1 && three) launch_pdl(k_bstress<ORD, 1, 3, CY, TX, SPT>, grid, block, st, p);
+        else if (zen_mode == 1) launch_pdl(k_bstress<ORD, 1, kMaxSls, CY, TX, SPT>, grid, block, st, p);
+        else if (three) launch_pdl(k_bstress<ORD, 2, 3, CY, TX, SPT>, grid, block, st, p);
+        else launch_pdl(k_bstress<ORD, 2, kMaxSls, CY, TX, SPT>, grid, block, st, p);
     }
-    if (parts & 2) launch_pdl(k_bvelocity<ORD, CY, TX>, grid, block, st, p, j);
+    if (parts & 2) launch_pdl(k_bvelocity<ORD, CY, TX, SPT>, grid, block, st, p, j);
 }
 
-// Block shapes: 32 shots x CY nodes along y, TX nodes per thread along x.
+// Launch shapes: blocks of 32 lanes x CY nodes along y, TX nodes per thread
+// along x, SPT shots per lane.  Order 2 has every shape of the autotuner; order
+// 4 has the default shape only.
 template <int ORD>
-void launch_ord(const BParams &p, int n_blocks, int cy, int tx, int zen_mode, int j, cudaStream_t st, int parts) {
-    if (cy == 4 && tx == 1) launch_shape<ORD, 4, 1>(p, n_blocks, zen_mode, j, st, parts);
-    else if (cy == 4 && tx == 2) launch_shape<ORD, 4, 2>(p, n_blocks, zen_mode, j, st, parts);
-    else if (cy == 4) launch_shape<ORD, 4, 4>(p, n_blocks, zen_mode, j, st, parts);
-    else if (cy == 8 && tx == 1) launch_shape<ORD, 8, 1>(p, n_blocks, zen_mode, j, st, parts);
-    else if (cy == 8 && tx == 2) launch_shape<ORD, 8, 2>(p, n_blocks, zen_mode, j, st, parts);
-    else launch_shape<ORD, 8, 4>(p, n_blocks, zen_mode, j, st, parts);
+void launch_ord(const BParams &p, int n_blocks, int cy, int tx, int spt, int zen_mode, int j, cudaStream_t st,
+                int parts) {
+    if constexpr (ORD == 2) {
+        if (spt == 2) {
+            if (cy == 4 && tx == 1) return launch_shape<ORD, 4, 1, 2>(p, n_blocks, zen_mode, j, st, parts);
+            if (cy == 4) return launch_shape<ORD, 4, 2, 2>(p, n_blocks, zen_mode, j, st, parts);
+            if (tx == 1) return launch_shape<ORD, 8, 1, 2>(p, n_blocks, zen_mode, j, st, parts);
+            return launch_shape<ORD, 8, 2, 2>(p, n_blocks, zen_mode, j, st, parts);
+        }
+        if (cy == 4 && tx == 1) return launch_shape<ORD, 4, 1, 1>(p, n_blocks, zen_mode, j, st, parts);
+        if (cy == 4 && tx == 2) return launch_shape<ORD, 4, 2, 1>(p, n_blocks, zen_mode, j, st, parts);
+        if (cy == 4) return launch_shape<ORD, 4, 4, 1>(p, n_blocks, zen_mode, j, st, parts);
+        if (cy == 8 && tx == 1) return launch_shape<ORD, 8, 1, 1>(p, n_blocks, zen_mode, j, st, parts);
+        if (cy == 8 && tx == 4) return launch_shape<ORD, 8, 4, 1>(p, n_blocks, zen_mode, j, st, parts);
+    }
+    launch_shape<ORD, 8, 2, 1>(p, n_blocks, zen_mode, j, st, parts);
 }
 
-void launch_batch(const BParams &p, int n_blocks, int ord, int cy, int tx, int zen_mode, int j, cudaStream_t st,
-                  int parts = 3) {
+void launch_batch(const BParams &p, int n_blocks, int ord, int cy, int tx, int spt, int zen_mode, int j,
+                  cudaStream_t st, int parts = 3) {
     switch (ord) {
-    case 2: launch_ord<2>(p, n_blocks, cy, tx, zen_mode, j, st, parts); break;
-    case 4: launch_ord<4>(p, n_blocks, cy, tx, zen_mode, j, st, parts); break;
+    case 2: launch_ord<2>(p, n_blocks, cy, tx, spt, zen_mode, j, st, parts); break;
+    case 4: launch_ord<4>(p, n_blocks, cy, tx, spt, zen_mode, j, st, parts); break;
     default: break;
     }
 }
@@ -470,7 +548,7 @@ int bfail(int code, const std::string &m) {
 using namespace ts;
 
 struct ts_batch {
-    int device = 0, ord = 2, cy = 8, tx = 2, zen_mode = 0, rows = 0;
+    int device = 0, ord = 2, cy = 8, tx = 2, spt = 1, zen_mode = 0, rows = 0;
     int n_blocks = 0, steps_done = 0, n_ph = 0;
     int64_t launches = 0;
     cudaStream_t stream = nullptr;
@@ -543,6 +621,14 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
     if (!(bd->nodes_per_thread == 0 || bd->nodes_per_thread == 1 || bd->nodes_per_thread == 2 ||
           bd->nodes_per_thread == 4))
         return bfail(TS_E_ARG, "nodes_per_thread must be 0 (default), 1, 2 or 4");
+    if (!(bd->shots_per_thread == 0 || bd->shots_per_thread == 1 || bd->shots_per_thread == 2))
+        return bfail(TS_E_ARG, "shots_per_thread must be 0 (default), 1 or 2");
+    if (bd->shots_per_thread == 2 && bd->nodes_per_thread == 4)
+        return bfail(TS_E_ARG, "two shots per thread take 1 or 2 nodes per thread");
+    if (bd->phantoms && bd->phantoms->ord == 4 &&
+        !((bd->block_cells == 0 || bd->block_cells == 8) && (bd->nodes_per_thread == 0 || bd->nodes_per_thread == 2) &&
+          bd->shots_per_thread <= 1))
+        return bfail(TS_E_ARG, "order-4 batches take the default launch shape (8 cells, 2 nodes, 1 shot per thread)");
     const ts_desc *d0 = bd->phantoms;
     for (int q = 0; q < bd->n_phantoms; ++q) {
         const ts_desc *d = bd->phantoms + q;
@@ -578,6 +664,7 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
     b->n_ph = bd->n_phantoms;
     b->cy = bd->block_cells ? bd->block_cells : 8;
     b->tx = bd->nodes_per_thread ? bd->nodes_per_thread : 2;
+    b->spt = bd->shots_per_thread ? bd->shots_per_thread : 1;
     b->zen_mode = !d0->visco ? 0 : (d0->g_p ? 2 : 1);
     b->ph.resize(b->n_ph);
     int block0 = 0, rec0 = 0, rc;
@@ -588,12 +675,13 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
         h.nx = d->nx;
         h.ny = d->ny;
         h.n_shots = bd->n_shots[q];
-        h.S = round_up(h.n_shots, 32);
+        h.W = 32 * b->spt;
+        h.S = round_up(h.n_shots, h.W);
         if ((int64_t)h.nx * h.ny * h.S * std::max(1, d->visco ? d->n_sls : 1) >= (int64_t)1 << 31)
             return bail(bfail(TS_E_ARG, "phantom too large for one batch (nodes x shots x mechanisms >= 2^31)"));
         h.G = h.nx * h.ny * h.S;
         h.yblocks = (h.ny + b->cy - 1) / b->cy;
-        h.sblocks = h.S / 32;
+        h.sblocks = h.S / h.W;
         h.xchunks = (h.nx + b->tx - 1) / b->tx;
         h.block0 = block0;
         block0 += h.xchunks * h.yblocks * h.sblocks;
@@ -735,7 +823,8 @@ int ts_batch_run(ts_batch *b, int32_t n_steps, void *stream) {
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : b->stream;
     constexpr int G = 16;
     auto steps = [&](int count, cudaStream_t where) {
-        for (int j = 0; j < count; ++j) launch_batch(b->p, b->n_blocks, b->ord, b->cy, b->tx, b->zen_mode, j, where);
+        for (int j = 0; j < count; ++j)
+            launch_batch(b->p, b->n_blocks, b->ord, b->cy, b->tx, b->spt, b->zen_mode, j, where);
         launch_advance(const_cast<int *>(b->p.step_base), count, where);
     };
     if (!b->graph && n_steps >= G) {
@@ -808,13 +897,13 @@ int ts_batch_read_field(ts_batch *b, int32_t phantom, int32_t what, void *dst, s
     cudaEventSynchronize(b->done);
     const size_t need = (size_t)h.nx * h.ny * h.n_shots * 4;
     if (bytes < need) return bfail(TS_E_ARG, "destination too small");
-    // device layout [S/32][nx][ny][32] -> host [n_shots][nx][ny]
+    // device layout [S/W][nx][ny][W] -> host [n_shots][nx][ny]
     std::vector<float> tmp((size_t)h.G);
     if (cudaMemcpy(tmp.data(), src, tmp.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return bfail(TS_E_CUDA, "cudaMemcpy");
     float *o = static_cast<float *>(dst);
     const int64_t cells = (int64_t)h.nx * h.ny;
     for (int s = 0; s < h.n_shots; ++s)
-        for (int64_t c = 0; c < cells; ++c) o[s * cells + c] = tmp[((s >> 5) * cells + c) * 32 + (s & 31)];
+        for (int64_t c = 0; c < cells; ++c) o[s * cells + c] = tmp[((s / h.W) * cells + c) * h.W + (s % h.W)];
     return TS_OK;
 }
 
@@ -827,7 +916,7 @@ int ts_batch_profile_steps(ts_batch *b, int32_t n_steps, void *stream, float *ms
     cudaEventRecord(ev[0], st);
     for (int j = 0; j < n_steps; ++j)
         for (int part = 0; part < 2; ++part) {
-            launch_batch(b->p, b->n_blocks, b->ord, b->cy, b->tx, b->zen_mode, j, st, 1 << part);
+            launch_batch(b->p, b->n_blocks, b->ord, b->cy, b->tx, b->spt, b->zen_mode, j, st, 1 << part);
             cudaEventRecord(ev[2 * j + part + 1], st);
         }
     launch_advance(const_cast<int *>(b->p.step_base), n_steps, st);

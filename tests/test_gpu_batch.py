@@ -38,11 +38,12 @@ def _single_shot(sim, table):
     return st
 
 
-@pytest.mark.parametrize("shape", [(4, 1), (4, 2), (8, 2), (8, 4)], ids=lambda s: f"{s[0]}x{s[1]}")
+@pytest.mark.parametrize("shape", [(4, 1, 1), (4, 2, 1), (8, 2, 1), (8, 4, 1), (4, 1, 2), (8, 2, 2)],
+                         ids=lambda s: f"{s[0]}x{s[1]}x{s[2]}")
 def test_batch_matches_single_shots(shape):
     sims = _phantoms()
     shots = [fmc_shot_sources(s) for s in sims]
-    with BatchStepper(sims, shots, block_cells=shape[0], nodes_per_thread=shape[1]) as b:
+    with BatchStepper(sims, shots, block_cells=shape[0], nodes_per_thread=shape[1], shots_per_thread=shape[2]) as b:
         b.run(sims[0]._n_steps)
         n, vmax, bad = b.status()
         assert n == sims[0]._n_steps and bad == -1
@@ -80,6 +81,6 @@ def test_autotuner_picks_and_caches(tmp_path, monkeypatch):
     sims = _phantoms(steps=40)
     shots = [fmc_shot_sources(s) for s in sims]
     best, timings = autotune(sims, shots, steps=4)
-    assert best in batch.SHAPES and set(timings) == {f"{cy}x{tx}" for cy, tx in batch.SHAPES}
+    assert best in batch.SHAPES and set(timings) == {f"{cy}x{tx}x{spt}" for cy, tx, spt in batch.SHAPES}
     again, _ = autotune(sims, shots, steps=4)
     assert again == best and (tmp_path / "autotune.json").exists()
