@@ -460,7 +460,7 @@ def main():
         return run_adjoint(args)
 
     import torch
-    from taichi_sim_gb300 import engine
+    from taichi_sim_gb300 import engine, shards
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -506,10 +506,7 @@ def main():
         torch.cuda.synchronize()
     launches = st.launch_count() - launches0
     ms = start.elapsed_time(end)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = shards.max_over_ranks(ms, device="cuda")   # the job's time: its slowest replica
     ms_per_step = ms / args.steps
     value = cells * n_t * args.steps * world / (ms / 1e3) / 1e9
     clocks = clk.summary()
