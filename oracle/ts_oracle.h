@@ -18,6 +18,13 @@
  * Built twice from ts_oracle.c: ts_oracle_run_f32 computes in float (the
  * reference's precision) and ts_oracle_run_f64 in double (to measure the
  * float rounding error of either implementation).
+ *
+ * Pinning: the TAICHI2D family reproduces the reference's only known-answer
+ * result (pedro/results/result_teste_aco.npy, relative L2 7.4e-6 over 10000
+ * steps; tests/test_oracle_golden.py).  For the WGSL families parity is
+ * unpinned: the reference ships no WGSL-produced result and its shaders
+ * cannot run here (no graphics API), so they rest on line-by-line review and
+ * the formulas they share with the pinned family.
  */
 #ifndef TS_ORACLE_H
 #define TS_ORACLE_H
