@@ -72,6 +72,32 @@ def fmc_shot_sources(sim):
     return shots
 
 
+def focal_law_shot_sources(sim, laws):
+    """Shots of focal laws (plane-wave or focused transmissions): law k is one
+    emission delay per element (the probes' ``t0_emission`` units), applied
+    with ``set_t0`` as the reference's ``run()`` does
+    (sim_support/simulator.py:328-333) to every emitting array (a point or
+    single-element probe takes the law's first delay), and shot k's table is
+    the source term built with those delays (``EmissionLaw.read_law`` gives
+    such delay rows from a ``.law`` file).  The probes' delays are restored
+    afterwards.  Returns ``[n_laws][n_steps][src_cols]``."""
+    saved = [getattr(p, "_t0_emission", None) for p in sim._probes]
+    tables = []
+    try:
+        for law in laws:
+            row = np.atleast_1d(np.asarray(law, dtype=np.float32))
+            for i in sim._emitting_probes:
+                p = sim._probes[i]
+                p.set_t0(row.copy() if hasattr(p, "num_elem") else np.float32(row[0]))
+            st = np.asarray(sim.build_source_term(), np.float32)
+            tables.append(st[:, None] if st.ndim == 1 else st)
+    finally:
+        for p, t0 in zip(sim._probes, saved):
+            if t0 is not None:
+                p.set_t0(t0)
+    return np.ascontiguousarray(np.stack(tables))
+
+
 class BatchStepper:
     """Every shot of several phantoms advanced together on the GPU.
 

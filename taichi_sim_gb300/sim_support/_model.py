@@ -273,11 +273,13 @@ class ModelBase:
         terms, idx_src, idx_rec = list(), list(), list()
         self._idx_src_offset = 0
         self._idx_rec_offset = 0
+        self._emitting_probes = list()
         for i, pr in enumerate(self._probes):
             st = self._probe_source(i, pr)
             _, owner = pr.get_points_roi(sim_roi=self._roi, simul_type=stype)
             if len(owner) > 0:
                 terms.append(st)
+                self._emitting_probes.append(i)
                 idx_src += [np.array(s) + self._idx_src_offset for s in owner]
                 self._idx_src_offset += len(owner)
             rec_owner = pr.get_idx_rec(sim_roi=self._roi, simul_type=rec_type)
@@ -304,6 +306,13 @@ class ModelBase:
         offsets = [ids[0]] + [int32(i) for i in range(1, len(ids)) if ids[i] != ids[i - 1]]
         self._offset_sensors = np.array(offsets, dtype=int32)
         self._n_pto_rec = int32(len(ids))
+
+    def build_source_term(self):
+        """The source term for the probes' current emission delays, assembled
+        as the constructor assembles it (an extension: the reference builds it
+        once, so a later ``set_t0`` does not reach its kernels)."""
+        terms = [self._probe_source(i, self._probes[i]) for i in self._emitting_probes]
+        return np.concatenate(terms, axis=1) if len(terms) > 1 else terms[0]
 
     def _setup_attenuation(self):
         """Per-cell quality factors (extension); ``None`` keeps global taus."""

@@ -84,3 +84,26 @@ def test_autotuner_picks_and_caches(tmp_path, monkeypatch):
     assert best in batch.SHAPES and set(timings) == {f"{cy}x{tx}x{spt}" for cy, tx, spt in batch.SHAPES}
     again, _ = autotune(sims, shots, steps=4)
     assert again == best and (tmp_path / "autotune.json").exists()
+
+
+def test_focal_law_shots_match_single_shots():
+    """Plane-wave steering laws (one delay per element) batched as shots of
+    one launch: each shot equals the stepper run with that law's table."""
+    from taichi_sim_gb300.batch import focal_law_shot_sources
+    sims = _phantoms(steps=160)
+    dt = float(sims[0]._dt)
+    n_el = sims[0]._probes[0].num_elem
+    ramp = np.arange(n_el, dtype=np.float64)
+    laws = [np.zeros(n_el), ramp * 2 * dt, ramp[::-1] * 2 * dt, np.abs(ramp - (n_el - 1) / 2) * 3 * dt]
+    shots = [focal_law_shot_sources(s, laws) for s in sims]
+    assert not np.array_equal(shots[0][1], shots[0][2])
+    with BatchStepper(sims, shots) as b:
+        b.run(sims[0]._n_steps)
+        assert b.status()[2] == -1
+        for q, sim in enumerate(sims):
+            tr = b.traces(q)
+            for s in range(len(laws)):
+                with _single_shot(sim, shots[q][s]) as one:
+                    one.run(sim._n_steps)
+                    want = one.read("traces")
+                assert rel_l2(tr[s], want) <= TOL, (q, s, rel_l2(tr[s], want))
