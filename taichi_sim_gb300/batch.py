@@ -98,6 +98,27 @@ def focal_law_shot_sources(sim, laws):
     return np.ascontiguousarray(np.stack(tables))
 
 
+def run_emission_laws(sim, laws=None, field="syy"):
+    """Every emission law of a 2D model as shots of one batched launch.
+
+    ``laws`` defaults to the model's ``.law`` file rows (``_emission_laws``,
+    read in the constructor as sim_support/simulator.py:228-230 does); the
+    reference instead runs ``implementation()`` once per law
+    (sim_support/simulator.py:326-337).  Returns ``(traces, fields)``:
+    ``[n_laws, n_steps, n_rec]`` and ``[n_laws, nx, ny]``."""
+    if laws is None:
+        if not hasattr(sim, "_emission_laws"):
+            raise ValueError("the model has no emission laws; pass laws=")
+        laws = list(sim._emission_laws)
+    shots = focal_law_shot_sources(sim, laws)
+    with BatchStepper([sim], [shots]) as b:
+        b.run(sim._n_steps)
+        _, vmax, bad = b.status()
+        if bad >= 0:
+            raise engine.StabilityError("Simulacao tornando-se instavel", float(np.sqrt(np.float32(vmax))))
+        return b.traces(0), b.field(0, field)
+
+
 class BatchStepper:
     """Every shot of several phantoms advanced together on the GPU.
 

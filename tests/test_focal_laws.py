@@ -30,3 +30,11 @@ def test_delays_shift_each_element_and_restore_the_probe():
             assert np.linalg.norm(a - b) <= 1e-3 * np.linalg.norm(b)   # same wavelet, k[e] samples later
     np.testing.assert_array_equal(probe._t0_emission, before)   # restored
     np.testing.assert_array_equal(base, sim._source_term)
+
+
+def test_a_model_without_laws_needs_laws():
+    import pytest
+    from taichi_sim_gb300.batch import run_emission_laws
+    sim = Simulator(case_2d(visco=1, steps=50))
+    with pytest.raises(ValueError):
+        run_emission_laws(sim)

@@ -107,3 +107,26 @@ def test_focal_law_shots_match_single_shots():
                     one.run(sim._n_steps)
                     want = one.read("traces")
                 assert rel_l2(tr[s], want) <= TOL, (q, s, rel_l2(tr[s], want))
+
+
+def test_law_file_runs_as_one_batched_launch(tmp_path):
+    """A ``.law`` file named in the config: every law becomes a shot of one
+    launch, each equal to the stepper run with that law's delays."""
+    from taichi_sim_gb300.batch import focal_law_shot_sources, run_emission_laws
+    from taichi_sim_gb300.sim_support.emission_law import EmissionLaw
+    cfg = workloads.fmc2d_phantoms(n_steps=150, shapes=((80, 84),), n_elem=6, dx=0.1, pml=8)[0]
+    cfg["probes"][0]["linear"].update(dim_a=0.3, inter_elem=0.1)
+    dt = float(Simulator(cfg)._dt)
+    delays = np.stack([np.arange(6) * k * dt for k in (0.0, 1.5, -1.5)]) + 3 * dt
+    EmissionLaw().write_law(str(tmp_path / "steer"), delays)
+    cfg["simul_configs"]["emission_laws"] = str(tmp_path / "steer.law")
+    sim = Simulator(cfg)
+    assert sim._emission_laws.shape == (3, 6)
+    traces, fields = run_emission_laws(sim)
+    assert traces.shape == (3, sim._n_steps, sim._n_rec) and fields.shape == (3,) + tuple(sim.grid_shape())
+    tables = focal_law_shot_sources(sim, list(sim._emission_laws))
+    for k in range(3):
+        with _single_shot(sim, tables[k]) as one:
+            one.run(sim._n_steps)
+            want_tr, want_f = one.read("traces"), one.read("syy")
+        assert rel_l2(traces[k], want_tr) <= TOL and rel_l2(fields[k], want_f) <= TOL
