@@ -192,9 +192,8 @@ def run_fmc(args):
     sims = [Simulator(c) for c in workloads.fmc2d_phantoms(n_steps=n_t)]
     shots = [fmc_shot_sources(s) for s in sims]
     cell_shots = sum(int(np.prod(s.grid_shape())) * sh.shape[0] for s, sh in zip(sims, shots))
-    (block_cells, nodes_per_thread, shots_per_thread), tune = autotune(sims, shots, steps=8)
-    b = BatchStepper(sims, shots, block_cells=block_cells, nodes_per_thread=nodes_per_thread,
-                     shots_per_thread=shots_per_thread)
+    shape, tune = autotune(sims, shots, steps=8)
+    b = BatchStepper(sims, shots, **shape)
     stream = torch.cuda.Stream()
     h = stream.cuda_stream
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -256,8 +255,7 @@ def run_fmc(args):
             "data": "synthetic (seeded numpy default_rng)",
             "config": {"workload": "fmc2d", "phantoms": [list(s.grid_shape()) for s in sims],
                        "shots_per_phantom": [int(sh.shape[0]) for sh in shots], "time_steps_per_step": n_t,
-                       "block_cells": block_cells, "nodes_per_thread": nodes_per_thread,
-                       "shots_per_thread": shots_per_thread, "autotune_ms": tune,
+                       "launch_shape": shape, "autotune_ms": tune,
                        "l2": "256 MiB flush written after every batch (inside the timed region)"},
             "kernel_ms": {"stress": round(k_ms[0], 4), "velocity": round(k_ms[1], 4)},
             "per_shot_loop": {"value": round(loop_value, 3), "unit": "Gcell/s",

@@ -181,7 +181,8 @@ const char *ts_last_error(void);
  * are [n_shots][n_steps][n_rec] per phantom.  block_cells (0 = 8),
  * nodes_per_thread (0 = 2) and shots_per_thread (0 = 1) set the launch
  * shape: blocks of 32 lanes x block_cells nodes along y, each thread
- * updating nodes_per_thread nodes along x for shots_per_thread shots; they
+ * updating nodes_per_thread nodes along x for shots_per_thread shots; the
+ * velocity launch may take its own block_cells and nodes_per_thread.  They
  * are fixed at creation (order-4 batches take the default shape).
  */
 typedef struct ts_batch ts_batch;
@@ -192,9 +193,11 @@ typedef struct ts_batch_desc {
     const ts_desc *phantoms;          /* [n_phantoms] */
     const int32_t *n_shots;           /* [n_phantoms] */
     const float *const *shot_sources; /* [n_phantoms] -> [n_shots][n_steps][src_cols] */
-    int32_t block_cells;              /* 0, 4 or 8 */
-    int32_t nodes_per_thread;         /* 0, 1, 2 or 4 (1 or 2 with two shots per thread) */
-    int32_t shots_per_thread;         /* 0, 1 or 2 */
+    int32_t block_cells;              /* stress launch: nodes along y per block, 0 (= 8), 4 or 8 */
+    int32_t nodes_per_thread;         /* stress launch: nodes along x per thread, 0 (= 2), 1, 2 or 4 */
+    int32_t shots_per_thread;         /* 0 (= 1), 1 or 2; the shot layout, shared by both launches */
+    int32_t velocity_block_cells;     /* velocity launch; 0 = as the stress launch */
+    int32_t velocity_nodes_per_thread;/* velocity launch; 0 = as the stress launch */
 } ts_batch_desc;
 
 int ts_batch_create(const ts_batch_desc *desc, ts_batch **out);

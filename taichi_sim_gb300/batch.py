@@ -27,7 +27,8 @@ class BatchDesc(ctypes.Structure):
     _fields_ = [("abi_version", ctypes.c_int32), ("n_phantoms", ctypes.c_int32),
                 ("phantoms", ctypes.POINTER(engine.TsDesc)), ("n_shots", ctypes.POINTER(ctypes.c_int32)),
                 ("shot_sources", ctypes.POINTER(_f)), ("block_cells", ctypes.c_int32),
-                ("nodes_per_thread", ctypes.c_int32), ("shots_per_thread", ctypes.c_int32)]
+                ("nodes_per_thread", ctypes.c_int32), ("shots_per_thread", ctypes.c_int32),
+                ("velocity_block_cells", ctypes.c_int32), ("velocity_nodes_per_thread", ctypes.c_int32)]
 
 
 def _bind(lib):
@@ -127,7 +128,8 @@ class BatchStepper:
     is ``[n_shots, n_steps, src_cols]`` for phantom p.
     """
 
-    def __init__(self, sims, shot_sources, block_cells=0, nodes_per_thread=0, shots_per_thread=0):
+    def __init__(self, sims, shot_sources, block_cells=0, nodes_per_thread=0, shots_per_thread=0,
+                 velocity_block_cells=0, velocity_nodes_per_thread=0):
         self._lib = _bind(engine.load_library())
         self.sims = list(sims)
         self.n_ph = len(self.sims)
@@ -153,7 +155,8 @@ class BatchStepper:
         ptrs = (_f * self.n_ph)(*[s.ctypes.data_as(_f) for s in self.shot_sources])
         bd = BatchDesc(abi_version=engine.ABI_VERSION, n_phantoms=self.n_ph, phantoms=descs, n_shots=n_shots,
                        shot_sources=ptrs, block_cells=int(block_cells), nodes_per_thread=int(nodes_per_thread),
-                       shots_per_thread=int(shots_per_thread))
+                       shots_per_thread=int(shots_per_thread), velocity_block_cells=int(velocity_block_cells),
+                       velocity_nodes_per_thread=int(velocity_nodes_per_thread))
         h = ctypes.c_void_p()
         _check(self._lib, self._lib.ts_batch_create(ctypes.byref(bd), ctypes.byref(h)), "ts_batch_create")
         self._h = h
@@ -230,16 +233,23 @@ def _key(sims, shot_sources):
                       sort_keys=True)
 
 
-SHAPES = ((4, 1, 1), (4, 2, 1), (4, 4, 1), (8, 1, 1), (8, 2, 1), (8, 4, 1), (4, 1, 2), (4, 2, 2), (8, 1, 2), (8, 2, 2))
+# (block_cells, nodes_per_thread, shots_per_thread) of order-2 batches
+SHAPES = tuple((cy, tx, spt) for spt in (1, 2) for cy in (4, 8) for tx in (1, 2, 4))
 
 
 def autotune(sims, shot_sources, candidates=SHAPES, steps=12, use_cache=True):
-    """Pick the launch shape ``(block_cells, nodes_per_thread, shots_per_thread)``
-    (blocks of 32 lanes x block_cells nodes along y, nodes_per_thread nodes
-    along x and shots_per_thread shots per thread) with the shortest measured
-    step on this GPU; the choice is cached per problem shape.  Order-4 models
-    have the default shape only.  Returns ``((block_cells, nodes_per_thread,
-    shots_per_thread), {"CYxTXxSPT": ms_per_step})``."""
+    """Pick the launch shapes with the shortest measured step on this GPU.
+
+    A shape is ``(block_cells, nodes_per_thread, shots_per_thread)``: blocks
+    of 32 lanes x block_cells nodes along y, nodes_per_thread nodes along x
+    and shots_per_thread shots per thread.  Every candidate is timed with
+    both kernels at that shape; then, per shot layout (shots_per_thread, which
+    the two kernels share), the stress and the velocity launch each take
+    their fastest (block_cells, nodes_per_thread), and the layout with the
+    shortest step wins.  Order-4 models have the default shape only.  The
+    choice is cached per problem shape.  Returns ``(shape, timings)``: shape
+    is a dict of :class:`BatchStepper` keyword arguments, timings
+    ``{"CYxTXxSPT": [stress_ms, velocity_ms]}`` per step."""
     key = _key(sims, shot_sources)
     path = _cache_path()
     cache = {}
@@ -249,20 +259,28 @@ def autotune(sims, shot_sources, candidates=SHAPES, steps=12, use_cache=True):
                 cache = json.load(f)
         except (OSError, ValueError):
             cache = {}
-        if key in cache and len(cache[key].get("shape", ())) == 3:
-            return tuple(cache[key]["shape"]), cache[key]["timings"]
+        if key in cache and isinstance(cache[key].get("shape"), dict):
+            return dict(cache[key]["shape"]), cache[key]["timings"]
     timings = {}
     if int(sims[0]._coefs.shape[0]) != 2:
         candidates = ((8, 2, 1),)
     for cy, tx, spt in candidates:
         with BatchStepper(sims, shot_sources, block_cells=cy, nodes_per_thread=tx, shots_per_thread=spt) as b:
             b.profile_steps(2)
-            ms = b.profile_steps(steps)
-            timings[f"{cy}x{tx}x{spt}"] = float(sum(ms))
-    best_key = min(timings, key=timings.get)
-    best = tuple(int(v) for v in best_key.split("x"))
-    cache[key] = {"shape": list(best), "timings": timings, "when": time.time()}
+            timings[f"{cy}x{tx}x{spt}"] = [float(v) for v in b.profile_steps(steps)]
+    best, best_ms = None, float("inf")
+    for spt in sorted({c[2] for c in candidates}):
+        mine = {k: v for k, v in timings.items() if int(k.split("x")[2]) == spt}
+        ks = min(mine, key=lambda k: mine[k][0])
+        kv = min(mine, key=lambda k: mine[k][1])
+        if mine[ks][0] + mine[kv][1] < best_ms:
+            best_ms = mine[ks][0] + mine[kv][1]
+            cs, ts_, _ = (int(v) for v in ks.split("x"))
+            cv, tv, _ = (int(v) for v in kv.split("x"))
+            best = {"block_cells": cs, "nodes_per_thread": ts_, "shots_per_thread": spt,
+                    "velocity_block_cells": cv, "velocity_nodes_per_thread": tv}
+    cache[key] = {"shape": best, "timings": timings, "when": time.time()}
     os.makedirs(os.path.dirname(path), exist_ok=True)
     with open(path, "w") as f:
         json.dump(cache, f, indent=1)
-    return best, timings
+    return dict(best), timings

@@ -26,6 +26,7 @@
 #include <cfloat>
 #include <map>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/taichi_sim_gb300.h"
@@ -43,17 +44,24 @@ struct BSrc {
     float scale;  // dt / rho at the vy node
 };
 
+// Flat block range of one phantom in one kernel's launch: blocks of 32 lanes
+// x CY nodes along y, TX nodes along x per thread.
+struct Decomp {
+    int block0, xchunks, yblocks;
+};
+
 struct BPh {
     int nx, ny, S, W, n_shots;   // S shots padded to a multiple of W (shots per block row: 32 or 64)
     int G;      // nx * ny * S (checked < 2^31 with the memory variables)
-    int block0, xchunks, yblocks, sblocks;
+    int sblocks;
+    Decomp dc[2];  // block decomposition of the stress (0) and velocity (1) launches
     float cd[2][kMaxOrd];
     float *v[2], *s[3], *r[3], *psi[8];
     const Cpml *tab_f[2], *tab_h[2];
     Strip strip[2];
     const float *lam, *mu, *mus, *dtr0, *dtr1, *gp, *gs;
     const BSrc *src;
-    const int *src_start;  // [nx * yblocks + 1]
+    const int *src_start;  // [xchunks * yblocks + 1] of the velocity launch
     const float *shot_tab;  // [n_shots][rows][ncol]
     int ncol;
     int n_rec;
@@ -67,7 +75,7 @@ struct BPh {
 struct BParams {
     int n_ph;
     BPh ph[kMaxPhantoms];
-    int block_end[kMaxPhantoms];  // exclusive flat block end per phantom
+    int block_end[2][kMaxPhantoms];  // exclusive flat block end per kernel and phantom
     Zener zen;
     int rows;
     float v2_threshold;
@@ -89,23 +97,25 @@ struct Loc {
     bool live;
 };
 
-// Block b of a launch: phantom, then (x-chunk, y-block, shot-block) within it.
+// Block b of a launch of kernel KIND (0 stress, 1 velocity): phantom, then
+// (x-chunk, y-block, shot-block) within it.
 // W = 32 * SPT shots per shot block: lane l owns shots SPT l .. SPT l + SPT-1.
-template <int CY, int TX, int SPT>
+template <int KIND, int CY, int TX, int SPT>
 __device__ __forceinline__ Loc locate(const BParams &p) {
     constexpr int W = 32 * SPT;
     const int b = blockIdx.x;
     int q = 0;
 #pragma unroll 1
-    while (q + 1 < p.n_ph && b >= p.block_end[q]) ++q;
+    while (q + 1 < p.n_ph && b >= p.block_end[KIND][q]) ++q;
     Loc L;
     L.ph = p.ph + q;
     const BPh &h = *L.ph;
-    const int local = b - h.block0;
+    const Decomp &dc = h.dc[KIND];
+    const int local = b - dc.block0;
     L.sb = local % h.sblocks;
     const int t = local / h.sblocks;
-    const int yb = t % h.yblocks;
-    L.x0 = (t / h.yblocks) * TX;
+    const int yb = t % dc.yblocks;
+    L.x0 = (t / dc.yblocks) * TX;
     L.y = yb * CY + threadIdx.y;
     L.lane = threadIdx.x;
     L.s0 = L.sb * W + L.lane * SPT;
@@ -146,25 +156,25 @@ __device__ __forceinline__ void sto(float *q, const float (&v)[SPT]) {
 }
 
 // Rows r0 .. r0+2*ORD-1 of one field at (y, shots), zero outside the grid.
-template <int ORD, int SPT>
+template <int ORD, int SPT, bool CHECK = true>
 __device__ __forceinline__ void bwindow(float (&w)[2 * ORD][SPT], const float *f, int r0, int nx, int X, int col) {
 #pragma unroll
     for (int j = 0; j < 2 * ORD; ++j) {
         const int r = r0 + j;
-        if (r >= 0 && r < nx) ldf<SPT>(w[j], f + r * X + col);
+        if (!CHECK || (r >= 0 && r < nx)) ldf<SPT>(w[j], f + r * X + col);
         else
 #pragma unroll
             for (int q = 0; q < SPT; ++q) w[j][q] = 0.f;
     }
 }
 
-template <int ORD, int SPT>
+template <int ORD, int SPT, bool CHECK = true>
 __device__ __forceinline__ void bshift(float (&w)[2 * ORD][SPT], const float *f, int r_new, int nx, int X, int col) {
 #pragma unroll
     for (int j = 0; j < 2 * ORD - 1; ++j)
 #pragma unroll
         for (int q = 0; q < SPT; ++q) w[j][q] = w[j + 1][q];
-    if (r_new >= 0 && r_new < nx) ldf<SPT>(w[2 * ORD - 1], f + r_new * X + col);
+    if (!CHECK || (r_new >= 0 && r_new < nx)) ldf<SPT>(w[2 * ORD - 1], f + r_new * X + col);
     else
 #pragma unroll
         for (int q = 0; q < SPT; ++q) w[2 * ORD - 1][q] = 0.f;
@@ -179,16 +189,24 @@ struct MinBlocks {
 template <int ORD, int ZM, int NS, int CY, int TX, int SPT>
 __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bstress(const __grid_constant__ BParams p) {
     constexpr int W = 32 * SPT, Y = W;
-    const Loc at = locate<CY, TX, SPT>(p);
+    const Loc at = locate<0, CY, TX, SPT>(p);
     if (!at.live) return;
     const BPh &h = *at.ph;
-    const int y = at.y, nx = h.nx;
-    const int X = h.ny * W, col = (at.sb * h.nx * h.ny + y) * W + at.lane * SPT;
-    const bool yn = y >= ORD && y < h.ny - ORD + 1;
-    const bool ys = y >= ORD - 1 && y < h.ny - ORD;
+    // per-phantom values used at every node, copied to registers once
+    const int y = at.y, nx = h.nx, ny = h.ny, G = h.G;
+    const int X = ny * W, col = (at.sb * nx * ny + y) * W + at.lane * SPT;
+    const bool yn = y >= ORD && y < ny - ORD + 1;
+    const bool ys = y >= ORD - 1 && y < ny - ORD;
     const int sy = strip_index(h.strip[1], y);
+    const Strip stx = h.strip[0];
     const int n_mech = NS == 3 ? 3 : p.zen.n;
     constexpr int R = NS > 0 ? NS : 1;
+    float cdx[ORD], cdy[ORD];
+#pragma unroll
+    for (int c = 0; c < ORD; ++c) {
+        cdx[c] = h.cd[0][c];
+        cdy[c] = h.cd[1][c];
+    }
     const float *__restrict__ vx = h.v[0];   // read with ldf only
     const float *__restrict__ vy = h.v[1];
     float *__restrict__ s0 = h.s[0];
@@ -198,156 +216,167 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bstress(co
     float *__restrict__ r1 = h.r[1];
     float *__restrict__ r2 = h.r[2];
     pdl_wait();
-    // vx rows [x-ORD+1, x+ORD] (normal x-derivative), vy rows [x-ORD, x+ORD-1] (shear)
-    float wvx[2 * ORD][SPT], wvy[2 * ORD][SPT];
-    bwindow<ORD, SPT>(wvx, vx, at.x0 - ORD + 1, nx, X, col);
-    bwindow<ORD, SPT>(wvy, vy, at.x0 - ORD, nx, X, col);
+    // Interior chunks (every node of the thread inside both update regions and
+    // outside the CPML strips, window rows inside the grid) take a sweep with
+    // no per-node region, strip or bounds tests.
+    const bool fast = sy < 0 && y >= ORD && y < ny - ORD && at.x0 >= ORD && at.x0 >= stx.lo &&
+                      at.x0 + TX + ORD <= nx && at.x0 + TX <= stx.hi;
+    auto sweep = [&](auto fast_tag) {
+        constexpr bool FAST = decltype(fast_tag)::value;
+        const int syl = FAST ? -1 : sy;
+        // vx rows [x-ORD+1, x+ORD] (normal x-derivative), vy rows [x-ORD, x+ORD-1] (shear)
+        float wvx[2 * ORD][SPT], wvy[2 * ORD][SPT];
+        bwindow<ORD, SPT, !FAST>(wvx, vx, at.x0 - ORD + 1, nx, X, col);
+        bwindow<ORD, SPT, !FAST>(wvy, vy, at.x0 - ORD, nx, X, col);
 #pragma unroll
-    for (int t = 0; t < TX; ++t) {
-        const int x = at.x0 + t;
-        if (x >= nx) break;
-        const int cell = at.cell0 + t * h.ny;
-        const int i = at.i0 + t * X;
-        const bool in_n = yn && x >= ORD - 1 && x < nx - ORD;
-        const bool in_s = ys && x >= ORD && x < nx - ORD + 1;
-        if (in_n || in_s) {
-            const int sx = strip_index(h.strip[0], x);
-            const int ix = ((at.sb * h.strip[0].width + sx) * h.ny + y) * W + at.lane * SPT;
-            const int iy = ((at.sb * h.nx + x) * h.strip[1].width + sy) * W + at.lane * SPT;
-            // ---- loads ----
-            float L = 0.f, M = 0.f, Ms = 0.f, gp = 1.f, gs = 1.f;
-            float sxx[SPT], syy[SPT], sxy[SPT], pn0[SPT], pn1[SPT], ps0[SPT], ps1[SPT];
-            float ny_lo[ORD][SPT], ny_hi[ORD][SPT], sx_lo[ORD][SPT], sx_hi[ORD][SPT];
-            float rxx[R][SPT], ryy[R][SPT], rxy[R][SPT];
-            if (in_n) {
-                L = __ldg(h.lam + cell);
-                M = __ldg(h.mu + cell);
-                if (ZM == 2) gp = __ldg(h.gp + cell);
-#pragma unroll
-                for (int c = 0; c < ORD; ++c) {
-                    ldf<SPT>(ny_hi[c], vy + i + c * Y);         // vy[y+c]
-                    ldf<SPT>(ny_lo[c], vy + i - (c + 1) * Y);   // vy[y-c-1]
-                }
-                ldo<SPT>(sxx, s0 + i);
-                ldo<SPT>(syy, s1 + i);
-                if (sx >= 0) ldo<SPT>(pn0, h.psi[0] + ix);
-                if (sy >= 0) ldo<SPT>(pn1, h.psi[2] + iy);
-                if (ZM != 0) {
-#pragma unroll
-                    for (int l = 0; l < R; ++l)
-                        if (l < n_mech) {
-                            ldo<SPT>(rxx[l], r0 + l * h.G + i);
-                            ldo<SPT>(ryy[l], r1 + l * h.G + i);
-                        }
-                }
-            }
-            if (in_s) {
-                Ms = __ldg(h.mus + cell);
-#pragma unroll
-                for (int c = 0; c < ORD; ++c) {
-                    ldf<SPT>(sx_hi[c], vx + i + (c + 1) * Y);   // vx[y+c+1]
-                    ldf<SPT>(sx_lo[c], vx + i - c * Y);         // vx[y-c]
-                }
-                ldo<SPT>(sxy, s2 + i);
-                if (sx >= 0) ldo<SPT>(ps0, h.psi[1] + ix);
-                if (sy >= 0) ldo<SPT>(ps1, h.psi[3] + iy);
-                if (ZM != 0) {
-#pragma unroll
-                    for (int l = 0; l < R; ++l)
-                        if (l < n_mech) ldo<SPT>(rxy[l], r2 + l * h.G + i);
-                }
-            }
-            if (ZM == 2) gs = __ldg(h.gs + cell);
-            // ---- normal stresses ----
-            if (in_n) {
-                float ux[SPT], uy[SPT], pn0n[SPT], pn1n[SPT];
-                float ra[R][SPT], rb[R][SPT];
-#pragma unroll
-                for (int q = 0; q < SPT; ++q) {
-                    float ddx = 0.f, ddy = 0.f;
+        for (int t = 0; t < TX; ++t) {
+            const int x = at.x0 + t;
+            if (!FAST && x >= nx) break;
+            const int cell = at.cell0 + t * h.ny;
+            const int i = at.i0 + t * X;
+            const bool in_n = FAST || (yn && x >= ORD - 1 && x < nx - ORD);
+            const bool in_s = FAST || (ys && x >= ORD && x < nx - ORD + 1);
+            if (in_n || in_s) {
+                const int sx = FAST ? -1 : strip_index(stx, x);
+                const int ix = ((at.sb * stx.width + sx) * ny + y) * W + at.lane * SPT;
+                const int iy = ((at.sb * nx + x) * h.strip[1].width + syl) * W + at.lane * SPT;
+                // ---- loads ----
+                float L = 0.f, M = 0.f, Ms = 0.f, gp = 1.f, gs = 1.f;
+                float sxx[SPT], syy[SPT], sxy[SPT], pn0[SPT], pn1[SPT], ps0[SPT], ps1[SPT];
+                float ny_lo[ORD][SPT], ny_hi[ORD][SPT], sx_lo[ORD][SPT], sx_hi[ORD][SPT];
+                float rxx[R][SPT], ryy[R][SPT], rxy[R][SPT];
+                if (in_n) {
+                    L = __ldg(h.lam + cell);
+                    M = __ldg(h.mu + cell);
+                    if (ZM == 2) gp = __ldg(h.gp + cell);
 #pragma unroll
                     for (int c = 0; c < ORD; ++c) {
-                        ddx = fmaf(h.cd[0][c], wvx[c + ORD][q] - wvx[ORD - 1 - c][q], ddx);
-                        ddy = fmaf(h.cd[1][c], ny_hi[c][q] - ny_lo[c][q], ddy);
+                        ldf<SPT>(ny_hi[c], vy + i + c * Y);         // vy[y+c]
+                        ldf<SPT>(ny_lo[c], vy + i - (c + 1) * Y);   // vy[y-c-1]
                     }
-                    if (sx >= 0) ddx = cpml(ddx, pn0[q], pn0n[q], h.tab_h[0][x]);
-                    if (sy >= 0) ddy = cpml(ddy, pn1[q], pn1n[q], h.tab_f[1][y]);
-                    const float L2M = fmaf(2.f, M, L);
-                    ux[q] = fmaf(L2M, ddx, L * ddy);
-                    uy[q] = fmaf(L, ddx, L2M * ddy);
+                    ldo<SPT>(sxx, s0 + i);
+                    ldo<SPT>(syy, s1 + i);
+                    if (sx >= 0) ldo<SPT>(pn0, h.psi[0] + ix);
+                    if (syl >= 0) ldo<SPT>(pn1, h.psi[2] + iy);
                     if (ZM != 0) {
-                        float srxx = 0.f, sryy = 0.f;
-                        const float dsum = ddx + ddy, ddif = 0.5f * (ddx - ddy);
 #pragma unroll
                         for (int l = 0; l < R; ++l)
                             if (l < n_mech) {
-                                ra[l][q] = fmaf(p.zen.Ap[l], rxx[l][q], (p.zen.Bp[l] * gp) * dsum);
-                                rb[l][q] = fmaf(p.zen.As[l], ryy[l][q], (p.zen.Bs[l] * gs) * ddif);
-                                srxx += rxx[l][q] + ra[l][q];
-                                sryy += ryy[l][q] + rb[l][q];
+                                ldo<SPT>(rxx[l], r0 + l * G + i);
+                                ldo<SPT>(ryy[l], r1 + l * G + i);
                             }
-                        const float hl = 0.5f * (L + M);
-                        ux[q] = fmaf(hl, srxx, fmaf(M, sryy, ux[q]));
-                        uy[q] = fmaf(hl, srxx, fmaf(-M, sryy, uy[q]));
                     }
-                    ux[q] += sxx[q];
-                    uy[q] += syy[q];
                 }
-                if (sx >= 0) sto<SPT>(h.psi[0] + ix, pn0n);
-                if (sy >= 0) sto<SPT>(h.psi[2] + iy, pn1n);
-                if (ZM != 0) {
-#pragma unroll
-                    for (int l = 0; l < R; ++l)
-                        if (l < n_mech) {
-                            sto<SPT>(r0 + l * h.G + i, ra[l]);
-                            sto<SPT>(r1 + l * h.G + i, rb[l]);
-                        }
-                }
-                sto<SPT>(s0 + i, ux);
-                sto<SPT>(s1 + i, uy);
-            }
-            // ---- shear stress ----
-            if (in_s) {
-                float u[SPT], ps0n[SPT], ps1n[SPT], rn[R][SPT];
-#pragma unroll
-                for (int q = 0; q < SPT; ++q) {
-                    float a = 0.f, b = 0.f;
+                if (in_s) {
+                    Ms = __ldg(h.mus + cell);
 #pragma unroll
                     for (int c = 0; c < ORD; ++c) {
-                        a = fmaf(h.cd[0][c], wvy[c + ORD][q] - wvy[ORD - 1 - c][q], a);
-                        b = fmaf(h.cd[1][c], sx_hi[c][q] - sx_lo[c][q], b);
+                        ldf<SPT>(sx_hi[c], vx + i + (c + 1) * Y);   // vx[y+c+1]
+                        ldf<SPT>(sx_lo[c], vx + i - c * Y);         // vx[y-c]
                     }
-                    if (sx >= 0) a = cpml(a, ps0[q], ps0n[q], h.tab_f[0][x]);
-                    if (sy >= 0) b = cpml(b, ps1[q], ps1n[q], h.tab_h[1][y]);
-                    const float e = a + b;
-                    u[q] = Ms * e;
+                    ldo<SPT>(sxy, s2 + i);
+                    if (sx >= 0) ldo<SPT>(ps0, h.psi[1] + ix);
+                    if (syl >= 0) ldo<SPT>(ps1, h.psi[3] + iy);
                     if (ZM != 0) {
-                        float sr = 0.f;
+#pragma unroll
+                        for (int l = 0; l < R; ++l)
+                            if (l < n_mech) ldo<SPT>(rxy[l], r2 + l * G + i);
+                    }
+                }
+                if (ZM == 2) gs = __ldg(h.gs + cell);
+                // ---- normal stresses ----
+                if (in_n) {
+                    float ux[SPT], uy[SPT], pn0n[SPT], pn1n[SPT];
+                    float ra[R][SPT], rb[R][SPT];
+#pragma unroll
+                    for (int q = 0; q < SPT; ++q) {
+                        float ddx = 0.f, ddy = 0.f;
+#pragma unroll
+                        for (int c = 0; c < ORD; ++c) {
+                            ddx = fmaf(cdx[c], wvx[c + ORD][q] - wvx[ORD - 1 - c][q], ddx);
+                            ddy = fmaf(cdy[c], ny_hi[c][q] - ny_lo[c][q], ddy);
+                        }
+                        if (sx >= 0) ddx = cpml(ddx, pn0[q], pn0n[q], h.tab_h[0][x]);
+                        if (syl >= 0) ddy = cpml(ddy, pn1[q], pn1n[q], h.tab_f[1][y]);
+                        const float L2M = fmaf(2.f, M, L);
+                        ux[q] = fmaf(L2M, ddx, L * ddy);
+                        uy[q] = fmaf(L, ddx, L2M * ddy);
+                        if (ZM != 0) {
+                            float srxx = 0.f, sryy = 0.f;
+                            const float dsum = ddx + ddy, ddif = 0.5f * (ddx - ddy);
+#pragma unroll
+                            for (int l = 0; l < R; ++l)
+                                if (l < n_mech) {
+                                    ra[l][q] = fmaf(p.zen.Ap[l], rxx[l][q], (p.zen.Bp[l] * gp) * dsum);
+                                    rb[l][q] = fmaf(p.zen.As[l], ryy[l][q], (p.zen.Bs[l] * gs) * ddif);
+                                    srxx += rxx[l][q] + ra[l][q];
+                                    sryy += ryy[l][q] + rb[l][q];
+                                }
+                            const float hl = 0.5f * (L + M);
+                            ux[q] = fmaf(hl, srxx, fmaf(M, sryy, ux[q]));
+                            uy[q] = fmaf(hl, srxx, fmaf(-M, sryy, uy[q]));
+                        }
+                        ux[q] += sxx[q];
+                        uy[q] += syy[q];
+                    }
+                    if (sx >= 0) sto<SPT>(h.psi[0] + ix, pn0n);
+                    if (syl >= 0) sto<SPT>(h.psi[2] + iy, pn1n);
+                    if (ZM != 0) {
 #pragma unroll
                         for (int l = 0; l < R; ++l)
                             if (l < n_mech) {
-                                rn[l][q] = fmaf(p.zen.As[l], rxy[l][q], (p.zen.Bs[l] * gs) * e);
-                                sr += rxy[l][q] + rn[l][q];
+                                sto<SPT>(r0 + l * G + i, ra[l]);
+                                sto<SPT>(r1 + l * G + i, rb[l]);
                             }
-                        u[q] = fmaf(0.5f * Ms, sr, u[q]);
                     }
-                    u[q] += sxy[q];
+                    sto<SPT>(s0 + i, ux);
+                    sto<SPT>(s1 + i, uy);
                 }
-                if (sx >= 0) sto<SPT>(h.psi[1] + ix, ps0n);
-                if (sy >= 0) sto<SPT>(h.psi[3] + iy, ps1n);
-                if (ZM != 0) {
+                // ---- shear stress ----
+                if (in_s) {
+                    float u[SPT], ps0n[SPT], ps1n[SPT], rn[R][SPT];
 #pragma unroll
-                    for (int l = 0; l < R; ++l)
-                        if (l < n_mech) sto<SPT>(r2 + l * h.G + i, rn[l]);
+                    for (int q = 0; q < SPT; ++q) {
+                        float a = 0.f, b = 0.f;
+#pragma unroll
+                        for (int c = 0; c < ORD; ++c) {
+                            a = fmaf(cdx[c], wvy[c + ORD][q] - wvy[ORD - 1 - c][q], a);
+                            b = fmaf(cdy[c], sx_hi[c][q] - sx_lo[c][q], b);
+                        }
+                        if (sx >= 0) a = cpml(a, ps0[q], ps0n[q], h.tab_f[0][x]);
+                        if (syl >= 0) b = cpml(b, ps1[q], ps1n[q], h.tab_h[1][y]);
+                        const float e = a + b;
+                        u[q] = Ms * e;
+                        if (ZM != 0) {
+                            float sr = 0.f;
+#pragma unroll
+                            for (int l = 0; l < R; ++l)
+                                if (l < n_mech) {
+                                    rn[l][q] = fmaf(p.zen.As[l], rxy[l][q], (p.zen.Bs[l] * gs) * e);
+                                    sr += rxy[l][q] + rn[l][q];
+                                }
+                            u[q] = fmaf(0.5f * Ms, sr, u[q]);
+                        }
+                        u[q] += sxy[q];
+                    }
+                    if (sx >= 0) sto<SPT>(h.psi[1] + ix, ps0n);
+                    if (syl >= 0) sto<SPT>(h.psi[3] + iy, ps1n);
+                    if (ZM != 0) {
+#pragma unroll
+                        for (int l = 0; l < R; ++l)
+                            if (l < n_mech) sto<SPT>(r2 + l * G + i, rn[l]);
+                    }
+                    sto<SPT>(s2 + i, u);
                 }
-                sto<SPT>(s2 + i, u);
+            }
+            if (t + 1 < TX) {
+                bshift<ORD, SPT, !FAST>(wvx, vx, x + ORD + 1, nx, X, col);
+                bshift<ORD, SPT, !FAST>(wvy, vy, x + ORD, nx, X, col);
             }
         }
-        if (t + 1 < TX) {
-            bshift<ORD, SPT>(wvx, vx, x + ORD + 1, nx, X, col);
-            bshift<ORD, SPT>(wvy, vy, x + ORD, nx, X, col);
-        }
-    }
+    };
+    if (fast) sweep(std::true_type{});
+    else sweep(std::false_type{});
     pdl_trigger();
 }
 
@@ -355,39 +384,62 @@ template <int ORD, int CY, int TX, int SPT>
 __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bvelocity(const __grid_constant__ BParams p,
                                                                               const int j) {
     constexpr int W = 32 * SPT, Y = W;
-    const Loc at = locate<CY, TX, SPT>(p);
+    const Loc at = locate<1, CY, TX, SPT>(p);
     const BPh &h = *at.ph;
-    const int y = at.y, nx = h.nx;
-    const int X = h.ny * W, col = (at.sb * h.nx * h.ny + y) * W + at.lane * SPT;
-    const bool yvy = y >= ORD - 1 && y < h.ny - ORD;
+    // per-phantom values used at every node, copied to registers once
+    const int y = at.y, nx = h.nx, ny = h.ny;
+    const int X = ny * W, col = (at.sb * nx * ny + y) * W + at.lane * SPT;
+    const bool yvy = y >= ORD - 1 && y < ny - ORD;
     const bool yvx = yvy && y >= ORD;
     const int sy = at.live ? strip_index(h.strip[1], y) : -1;
-    const int yb = y / CY;
+    const Strip stx = h.strip[0];
+    float cdx[ORD], cdy[ORD];
+#pragma unroll
+    for (int c = 0; c < ORD; ++c) {
+        cdx[c] = h.cd[0][c];
+        cdy[c] = h.cd[1][c];
+    }
     const float *__restrict__ sxx = h.s[0];  // read with ldf only
     const float *__restrict__ syy = h.s[1];
     const float *__restrict__ sxy = h.s[2];
+    const float *__restrict__ dtr0 = h.dtr0;
+    const float *__restrict__ dtr1 = h.dtr1;
     float *__restrict__ v0 = h.v[0];
     float *__restrict__ v1 = h.v[1];
     pdl_wait();
     const int k = *p.step_base + j;
-    float vmax = 0.f;
+    // source nodes among this thread's TX nodes: one bin per (x-chunk, y-block)
+    int q0 = 0, q1 = 0;
+    if (at.live && k < p.rows) {
+        const int bin = (at.x0 / TX) * h.dc[1].yblocks + y / CY;
+        q0 = __ldg(h.src_start + bin);
+        q1 = __ldg(h.src_start + bin + 1);
+    }
+    unsigned vmax = 0u;  // max |v|^2 as float bits (v2 >= 0 or NaN: NaN ranks highest)
     bool bad = false;
-    if (at.live) {
+    // Interior chunks (every node inside both update regions, outside the
+    // CPML strips, window rows inside the grid, no source node) take a sweep
+    // with no per-node region, strip, bounds or source tests.
+    const bool fast = at.live && sy < 0 && q0 == q1 && y >= ORD && y < ny - ORD && at.x0 >= ORD &&
+                      at.x0 >= stx.lo && at.x0 + TX + ORD <= nx && at.x0 + TX <= stx.hi;
+    auto sweep = [&](auto fast_tag) {
+        constexpr bool FAST = decltype(fast_tag)::value;
+        const int syl = FAST ? -1 : sy;
         // sxx rows [x-ORD, x+ORD-1] (vx), sxy rows [x-ORD+1, x+ORD] (vy)
         float wxx[2 * ORD][SPT], wxy[2 * ORD][SPT];
-        bwindow<ORD, SPT>(wxx, sxx, at.x0 - ORD, nx, X, col);
-        bwindow<ORD, SPT>(wxy, sxy, at.x0 - ORD + 1, nx, X, col);
+        bwindow<ORD, SPT, !FAST>(wxx, sxx, at.x0 - ORD, nx, X, col);
+        bwindow<ORD, SPT, !FAST>(wxy, sxy, at.x0 - ORD + 1, nx, X, col);
 #pragma unroll
         for (int t = 0; t < TX; ++t) {
             const int x = at.x0 + t;
-            if (x >= nx) break;
+            if (!FAST && x >= nx) break;
             const int cell = at.cell0 + t * h.ny;
             const int i = at.i0 + t * X;
-            const bool in_vy = yvy && x >= ORD - 1 && x < nx - ORD;
-            const bool in_vx = yvx && in_vy && x >= ORD;
-            const int sx = strip_index(h.strip[0], x);
-            const int ix = ((at.sb * h.strip[0].width + sx) * h.ny + y) * W + at.lane * SPT;
-            const int iy = ((at.sb * h.nx + x) * h.strip[1].width + sy) * W + at.lane * SPT;
+            const bool in_vy = FAST || (yvy && x >= ORD - 1 && x < nx - ORD);
+            const bool in_vx = FAST || (yvx && in_vy && x >= ORD);
+            const int sx = FAST ? -1 : strip_index(stx, x);
+            const int ix = ((at.sb * stx.width + sx) * ny + y) * W + at.lane * SPT;
+            const int iy = ((at.sb * nx + x) * h.strip[1].width + syl) * W + at.lane * SPT;
             // ---- loads ----
             float bx_hi[ORD][SPT], bx_lo[ORD][SPT], by_hi[ORD][SPT], by_lo[ORD][SPT];
             float vx0[SPT], vy0[SPT], pxa[SPT], pxb[SPT], pya[SPT], pyb[SPT];
@@ -399,9 +451,9 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bvelocity(
                     ldf<SPT>(bx_lo[c], sxy + i - (c + 1) * Y);   // sxy[y-c-1]
                 }
                 ldo<SPT>(vx0, v0 + i);
-                dx0 = __ldg(h.dtr0 + cell);
+                dx0 = __ldg(dtr0 + cell);
                 if (sx >= 0) ldo<SPT>(pxa, h.psi[4] + ix);
-                if (sy >= 0) ldo<SPT>(pxb, h.psi[6] + iy);
+                if (syl >= 0) ldo<SPT>(pxb, h.psi[6] + iy);
             }
             if (in_vy) {
 #pragma unroll
@@ -410,11 +462,10 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bvelocity(
                     ldf<SPT>(by_lo[c], syy + i - c * Y);         // syy[y-c]
                 }
                 ldo<SPT>(vy0, v1 + i);
-                dy0 = __ldg(h.dtr1 + cell);
+                dy0 = __ldg(dtr1 + cell);
                 if (sx >= 0) ldo<SPT>(pya, h.psi[5] + ix);
-                if (sy >= 0) ldo<SPT>(pyb, h.psi[7] + iy);
+                if (syl >= 0) ldo<SPT>(pyb, h.psi[7] + iy);
             }
-            const int q0 = __ldg(h.src_start + x * h.yblocks + yb), q1 = __ldg(h.src_start + x * h.yblocks + yb + 1);
             // ---- update ----
             float vxn[SPT], vyn[SPT], pxan[SPT], pxbn[SPT], pyan[SPT], pybn[SPT];
 #pragma unroll
@@ -425,26 +476,26 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bvelocity(
                     float a = 0.f, b = 0.f;
 #pragma unroll
                     for (int c = 0; c < ORD; ++c) {
-                        a = fmaf(h.cd[0][c], wxx[c + ORD][q] - wxx[ORD - 1 - c][q], a);
-                        b = fmaf(h.cd[1][c], bx_hi[c][q] - bx_lo[c][q], b);
+                        a = fmaf(cdx[c], wxx[c + ORD][q] - wxx[ORD - 1 - c][q], a);
+                        b = fmaf(cdy[c], bx_hi[c][q] - bx_lo[c][q], b);
                     }
                     if (sx >= 0) a = cpml(a, pxa[q], pxan[q], h.tab_f[0][x]);
-                    if (sy >= 0) b = cpml(b, pxb[q], pxbn[q], h.tab_f[1][y]);
+                    if (syl >= 0) b = cpml(b, pxb[q], pxbn[q], h.tab_f[1][y]);
                     vxn[q] = fmaf(a + b, dx0, vx0[q]);
                 }
                 if (in_vy) {
                     float a = 0.f, b = 0.f;
 #pragma unroll
                     for (int c = 0; c < ORD; ++c) {
-                        a = fmaf(h.cd[0][c], wxy[c + ORD][q] - wxy[ORD - 1 - c][q], a);
-                        b = fmaf(h.cd[1][c], by_hi[c][q] - by_lo[c][q], b);
+                        a = fmaf(cdx[c], wxy[c + ORD][q] - wxy[ORD - 1 - c][q], a);
+                        b = fmaf(cdy[c], by_hi[c][q] - by_lo[c][q], b);
                     }
                     if (sx >= 0) a = cpml(a, pya[q], pyan[q], h.tab_h[0][x]);
-                    if (sy >= 0) b = cpml(b, pyb[q], pybn[q], h.tab_h[1][y]);
+                    if (syl >= 0) b = cpml(b, pyb[q], pybn[q], h.tab_h[1][y]);
                     vyn[q] = fmaf(a + b, dy0, vy0[q]);
                 }
                 const int shot = at.s0 + q;
-                if (shot < h.n_shots && k < p.rows)
+                if (!FAST && q0 < q1 && shot < h.n_shots)
                     for (int qq = q0; qq < q1; ++qq) {
                         const BSrc s = h.src[qq];
                         if (s.cell == cell)
@@ -453,25 +504,26 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bvelocity(
                     }
                 const float v2 = fmaf(vxn[q], vxn[q], vyn[q] * vyn[q]);
                 bad |= !(v2 <= p.v2_threshold);
-                vmax = fmaxf(vmax, v2);
-                if (v2 != v2) vmax = v2;  // keep a NaN visible
+                vmax = max(vmax, __float_as_uint(v2));
             }
             if (in_vx) {
                 if (sx >= 0) sto<SPT>(h.psi[4] + ix, pxan);
-                if (sy >= 0) sto<SPT>(h.psi[6] + iy, pxbn);
+                if (syl >= 0) sto<SPT>(h.psi[6] + iy, pxbn);
             }
             if (in_vy) {
                 if (sx >= 0) sto<SPT>(h.psi[5] + ix, pyan);
-                if (sy >= 0) sto<SPT>(h.psi[7] + iy, pybn);
+                if (syl >= 0) sto<SPT>(h.psi[7] + iy, pybn);
             }
             sto<SPT>(v0 + i, vxn);
             sto<SPT>(v1 + i, vyn);
             if (t + 1 < TX) {
-                bshift<ORD, SPT>(wxx, sxx, x + ORD, nx, X, col);
-                bshift<ORD, SPT>(wxy, sxy, x + ORD + 1, nx, X, col);
+                bshift<ORD, SPT, !FAST>(wxx, sxx, x + ORD, nx, X, col);
+                bshift<ORD, SPT, !FAST>(wxy, sxy, x + ORD + 1, nx, X, col);
             }
         }
-    }
+    };
+    if (fast) sweep(std::true_type{});
+    else if (at.live) sweep(std::false_type{});
     // receivers: flat work item g = (phantom, shot, receiver)
     const int g = blockIdx.x * (32 * CY) + threadIdx.y * 32 + threadIdx.x;
     if (g < p.rec_work) {
@@ -486,7 +538,7 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bvelocity(
             r.traces[((int64_t)shot * p.rows + k) * r.n_rec + rec] = acc;
         }
     }
-    warp_stability(vmax, bad, reinterpret_cast<unsigned *>(p.block_max) + blockIdx.x, p.first_bad, k);
+    warp_stability(__uint_as_float(vmax), bad, reinterpret_cast<unsigned *>(p.block_max) + blockIdx.x, p.first_bad, k);
     pdl_trigger();
 }
 
@@ -513,9 +565,11 @@ void launch_ord(const BParams &p, int n_blocks, int cy, int tx, int spt, int zen
     if constexpr (ORD == 2) {
         if (spt == 2) {
             if (cy == 4 && tx == 1) return launch_shape<ORD, 4, 1, 2>(p, n_blocks, zen_mode, j, st, parts);
-            if (cy == 4) return launch_shape<ORD, 4, 2, 2>(p, n_blocks, zen_mode, j, st, parts);
+            if (cy == 4 && tx == 2) return launch_shape<ORD, 4, 2, 2>(p, n_blocks, zen_mode, j, st, parts);
+            if (cy == 4) return launch_shape<ORD, 4, 4, 2>(p, n_blocks, zen_mode, j, st, parts);
             if (tx == 1) return launch_shape<ORD, 8, 1, 2>(p, n_blocks, zen_mode, j, st, parts);
-            return launch_shape<ORD, 8, 2, 2>(p, n_blocks, zen_mode, j, st, parts);
+            if (tx == 2) return launch_shape<ORD, 8, 2, 2>(p, n_blocks, zen_mode, j, st, parts);
+            return launch_shape<ORD, 8, 4, 2>(p, n_blocks, zen_mode, j, st, parts);
         }
         if (cy == 4 && tx == 1) return launch_shape<ORD, 4, 1, 1>(p, n_blocks, zen_mode, j, st, parts);
         if (cy == 4 && tx == 2) return launch_shape<ORD, 4, 2, 1>(p, n_blocks, zen_mode, j, st, parts);
@@ -526,12 +580,17 @@ void launch_ord(const BParams &p, int n_blocks, int cy, int tx, int spt, int zen
     launch_shape<ORD, 8, 2, 1>(p, n_blocks, zen_mode, j, st, parts);
 }
 
-void launch_batch(const BParams &p, int n_blocks, int ord, int cy, int tx, int spt, int zen_mode, int j,
-                  cudaStream_t st, int parts = 3) {
-    switch (ord) {
-    case 2: launch_ord<2>(p, n_blocks, cy, tx, spt, zen_mode, j, st, parts); break;
-    case 4: launch_ord<4>(p, n_blocks, cy, tx, spt, zen_mode, j, st, parts); break;
-    default: break;
+// One time step: the stress launch (shape 0) then the velocity launch (shape
+// 1); `parts` selects them (bit 0 stress, bit 1 velocity).
+void launch_batch(const BParams &p, const int (&n_blocks)[2], int ord, const int (&cy)[2], const int (&tx)[2], int spt,
+                  int zen_mode, int j, cudaStream_t st, int parts = 3) {
+    for (int k = 0; k < 2; ++k) {
+        if (!(parts & (1 << k))) continue;
+        switch (ord) {
+        case 2: launch_ord<2>(p, n_blocks[k], cy[k], tx[k], spt, zen_mode, j, st, 1 << k); break;
+        case 4: launch_ord<4>(p, n_blocks[k], cy[k], tx[k], spt, zen_mode, j, st, 1 << k); break;
+        default: break;
+        }
     }
 }
 
@@ -548,8 +607,9 @@ int bfail(int code, const std::string &m) {
 using namespace ts;
 
 struct ts_batch {
-    int device = 0, ord = 2, cy = 8, tx = 2, spt = 1, zen_mode = 0, rows = 0;
-    int n_blocks = 0, steps_done = 0, n_ph = 0;
+    int device = 0, ord = 2, spt = 1, zen_mode = 0, rows = 0;
+    int cy[2] = {8, 8}, tx[2] = {2, 2}, n_blocks[2] = {0, 0};  // stress, velocity launch shapes
+    int steps_done = 0, n_ph = 0;
     int64_t launches = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
@@ -616,18 +676,19 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
     if (bd->abi_version != TS_ABI_VERSION) return bfail(TS_E_ARG, "abi_version mismatch");
     if (bd->n_phantoms < 1 || bd->n_phantoms > kMaxPhantoms) return bfail(TS_E_ARG, "n_phantoms must be in [1, 8]");
     if (!bd->phantoms || !bd->n_shots || !bd->shot_sources) return bfail(TS_E_ARG, "missing phantom tables");
-    if (!(bd->block_cells == 0 || bd->block_cells == 4 || bd->block_cells == 8))
-        return bfail(TS_E_ARG, "block_cells must be 0 (default), 4 or 8");
-    if (!(bd->nodes_per_thread == 0 || bd->nodes_per_thread == 1 || bd->nodes_per_thread == 2 ||
-          bd->nodes_per_thread == 4))
-        return bfail(TS_E_ARG, "nodes_per_thread must be 0 (default), 1, 2 or 4");
+    const int cells[2] = {bd->block_cells, bd->velocity_block_cells};
+    const int nodes[2] = {bd->nodes_per_thread, bd->velocity_nodes_per_thread};
+    for (int k = 0; k < 2; ++k) {
+        if (!(cells[k] == 0 || cells[k] == 4 || cells[k] == 8))
+            return bfail(TS_E_ARG, "block_cells must be 0 (default), 4 or 8");
+        if (!(nodes[k] == 0 || nodes[k] == 1 || nodes[k] == 2 || nodes[k] == 4))
+            return bfail(TS_E_ARG, "nodes_per_thread must be 0 (default), 1, 2 or 4");
+        if (bd->phantoms && bd->phantoms->ord == 4 && !((cells[k] == 0 || cells[k] == 8) && (nodes[k] == 0 || nodes[k] == 2)))
+            return bfail(TS_E_ARG, "order-4 batches take the default launch shape (8 cells, 2 nodes, 1 shot per thread)");
+    }
     if (!(bd->shots_per_thread == 0 || bd->shots_per_thread == 1 || bd->shots_per_thread == 2))
         return bfail(TS_E_ARG, "shots_per_thread must be 0 (default), 1 or 2");
-    if (bd->shots_per_thread == 2 && bd->nodes_per_thread == 4)
-        return bfail(TS_E_ARG, "two shots per thread take 1 or 2 nodes per thread");
-    if (bd->phantoms && bd->phantoms->ord == 4 &&
-        !((bd->block_cells == 0 || bd->block_cells == 8) && (bd->nodes_per_thread == 0 || bd->nodes_per_thread == 2) &&
-          bd->shots_per_thread <= 1))
+    if (bd->phantoms && bd->phantoms->ord == 4 && bd->shots_per_thread > 1)
         return bfail(TS_E_ARG, "order-4 batches take the default launch shape (8 cells, 2 nodes, 1 shot per thread)");
     const ts_desc *d0 = bd->phantoms;
     for (int q = 0; q < bd->n_phantoms; ++q) {
@@ -662,12 +723,14 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
     b->ord = d0->ord;
     b->rows = d0->n_steps;
     b->n_ph = bd->n_phantoms;
-    b->cy = bd->block_cells ? bd->block_cells : 8;
-    b->tx = bd->nodes_per_thread ? bd->nodes_per_thread : 2;
+    b->cy[0] = bd->block_cells ? bd->block_cells : 8;
+    b->tx[0] = bd->nodes_per_thread ? bd->nodes_per_thread : 2;
+    b->cy[1] = bd->velocity_block_cells ? bd->velocity_block_cells : b->cy[0];
+    b->tx[1] = bd->velocity_nodes_per_thread ? bd->velocity_nodes_per_thread : b->tx[0];
     b->spt = bd->shots_per_thread ? bd->shots_per_thread : 1;
     b->zen_mode = !d0->visco ? 0 : (d0->g_p ? 2 : 1);
     b->ph.resize(b->n_ph);
-    int block0 = 0, rec0 = 0, rc;
+    int block0[2] = {0, 0}, rec0 = 0, rc;
     for (int q = 0; q < b->n_ph; ++q) {
         const ts_desc *d = bd->phantoms + q;
         BPh &h = b->ph[q];
@@ -680,11 +743,15 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
         if ((int64_t)h.nx * h.ny * h.S * std::max(1, d->visco ? d->n_sls : 1) >= (int64_t)1 << 31)
             return bail(bfail(TS_E_ARG, "phantom too large for one batch (nodes x shots x mechanisms >= 2^31)"));
         h.G = h.nx * h.ny * h.S;
-        h.yblocks = (h.ny + b->cy - 1) / b->cy;
+
         h.sblocks = h.S / h.W;
-        h.xchunks = (h.nx + b->tx - 1) / b->tx;
-        h.block0 = block0;
-        block0 += h.xchunks * h.yblocks * h.sblocks;
+        for (int k = 0; k < 2; ++k) {
+            Decomp &dc = h.dc[k];
+            dc.yblocks = (h.ny + b->cy[k] - 1) / b->cy[k];
+            dc.xchunks = (h.nx + b->tx[k] - 1) / b->tx[k];
+            dc.block0 = block0[k];
+            block0[k] += dc.xchunks * dc.yblocks * h.sblocks;
+        }
         const float steps[2] = {d->dx, d->dy};
         for (int a = 0; a < 2; ++a)
             for (int c = 0; c < kMaxOrd; ++c) h.cd[a][c] = c < d->ord ? d->coefs[c] / steps[a] : 0.f;
@@ -740,15 +807,15 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
             if ((rc = b->upload(&dev, gs))) return bail(rc);
             h.gs = dev;
         }
-        // sources: nodes of the source map, binned by (x, y-block)
-        std::vector<std::vector<BSrc>> bins((size_t)h.nx * h.yblocks);
+        // sources: nodes of the source map, binned by (x-chunk, y-block)
+        std::vector<std::vector<BSrc>> bins((size_t)h.dc[1].xchunks * h.dc[1].yblocks);
         int maxcol = 0;
         for (int x = 0; x < h.nx; ++x)
             for (int y = 0; y < h.ny; ++y) {
                 const int idx = d->pos_sources[(int64_t)x * h.ny + y];
                 const float r4 = rho_vy[(int64_t)x * h.ny + y];
                 if (idx < 0 || idx >= d->src_cols || !(r4 > 0.f)) continue;
-                bins[(size_t)x * h.yblocks + y / b->cy].push_back(BSrc{x * h.ny + y, idx, d->dt / r4});
+                bins[(size_t)(x / b->tx[1]) * h.dc[1].yblocks + y / b->cy[1]].push_back(BSrc{x * h.ny + y, idx, d->dt / r4});
                 maxcol = std::max(maxcol, idx + 1);
             }
         std::vector<BSrc> list;
@@ -791,19 +858,23 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
         b->ncol.push_back(d->src_cols);
         b->cells.push_back(h.nx * h.ny);
     }
-    b->n_blocks = block0;
     BParams &p = b->p;
     p.n_ph = b->n_ph;
     for (int q = 0; q < b->n_ph; ++q) p.ph[q] = b->ph[q];
-    for (int q = 0; q < kMaxPhantoms; ++q)
-        p.block_end[q] = q < b->n_ph ? b->ph[q].block0 + b->ph[q].xchunks * b->ph[q].yblocks * b->ph[q].sblocks : block0;
-    if ((int64_t)rec0 > (int64_t)block0 * 32 * b->cy)
+    for (int k = 0; k < 2; ++k) {
+        b->n_blocks[k] = block0[k];
+        for (int q = 0; q < kMaxPhantoms; ++q) {
+            const Decomp &dc = b->ph[std::min(q, b->n_ph - 1)].dc[k];
+            p.block_end[k][q] = q < b->n_ph ? dc.block0 + dc.xchunks * dc.yblocks * b->ph[q].sblocks : block0[k];
+        }
+    }
+    if ((int64_t)rec0 > (int64_t)block0[1] * 32 * b->cy[1])
         return bail(bfail(TS_E_ARG, "more (shot, receiver) pairs than threads of a step launch"));
     p.zen = zener_constants(d0);
     p.rows = b->rows;
     p.v2_threshold = FLT_MAX;
     p.rec_work = rec0;
-    if ((rc = b->alloc(&p.block_max, b->n_blocks, true))) return bail(rc);
+    if ((rc = b->alloc(&p.block_max, b->n_blocks[1], true))) return bail(rc);
     int *fb = nullptr, *sb = nullptr;
     if ((rc = b->alloc(&fb, 1, false)) || (rc = b->alloc(&sb, 1, false))) return bail(rc);
     p.first_bad = fb;
@@ -861,7 +932,7 @@ int ts_batch_status(ts_batch *b, int32_t *steps_done, float *max_v2, int32_t *fi
     cudaEventSynchronize(b->done);
     if (steps_done) *steps_done = b->steps_done;
     if (max_v2) {
-        std::vector<unsigned> bm(b->n_blocks);
+        std::vector<unsigned> bm(b->n_blocks[1]);
         if (cudaMemcpy(bm.data(), b->p.block_max, bm.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
             return bfail(TS_E_CUDA, "cudaMemcpy");
         unsigned m = 0;

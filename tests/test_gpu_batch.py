@@ -38,7 +38,7 @@ def _single_shot(sim, table):
     return st
 
 
-@pytest.mark.parametrize("shape", [(4, 1, 1), (4, 2, 1), (8, 2, 1), (8, 4, 1), (4, 1, 2), (8, 2, 2)],
+@pytest.mark.parametrize("shape", [(4, 1, 1), (4, 2, 1), (8, 2, 1), (8, 4, 1), (4, 1, 2), (8, 2, 2), (4, 4, 2)],
                          ids=lambda s: f"{s[0]}x{s[1]}x{s[2]}")
 def test_batch_matches_single_shots(shape):
     sims = _phantoms()
@@ -81,9 +81,31 @@ def test_autotuner_picks_and_caches(tmp_path, monkeypatch):
     sims = _phantoms(steps=40)
     shots = [fmc_shot_sources(s) for s in sims]
     best, timings = autotune(sims, shots, steps=4)
-    assert best in batch.SHAPES and set(timings) == {f"{cy}x{tx}x{spt}" for cy, tx, spt in batch.SHAPES}
+    assert set(timings) == {f"{cy}x{tx}x{spt}" for cy, tx, spt in batch.SHAPES}
+    assert (best["block_cells"], best["nodes_per_thread"], best["shots_per_thread"]) in batch.SHAPES
+    assert (best["velocity_block_cells"], best["velocity_nodes_per_thread"], best["shots_per_thread"]) in batch.SHAPES
     again, _ = autotune(sims, shots, steps=4)
     assert again == best and (tmp_path / "autotune.json").exists()
+
+
+@pytest.mark.parametrize("shapes", [((4, 4), (8, 2), 1), ((8, 1), (4, 4), 2), ((4, 2), (8, 4), 2)],
+                         ids=["4x4-8x2-s1", "8x1-4x4-s2", "4x2-8x4-s2"])
+def test_split_launch_shapes_match_single_shots(shapes):
+    """Stress and velocity launches with different block decompositions."""
+    (cs, ts_), (cv, tv), spt = shapes
+    sims = _phantoms()
+    shots = [fmc_shot_sources(s) for s in sims]
+    with BatchStepper(sims, shots, block_cells=cs, nodes_per_thread=ts_, shots_per_thread=spt,
+                      velocity_block_cells=cv, velocity_nodes_per_thread=tv) as b:
+        b.run(sims[0]._n_steps)
+        assert b.status()[2] == -1
+        for q, sim in enumerate(sims):
+            tr = b.traces(q)
+            for s in (1, shots[q].shape[0] - 1):
+                with _single_shot(sim, shots[q][s]) as one:
+                    one.run(sim._n_steps)
+                    want = one.read("traces")
+                assert rel_l2(tr[s], want) <= TOL, (q, s, rel_l2(tr[s], want))
 
 
 def test_focal_law_shots_match_single_shots():
