@@ -32,6 +32,8 @@
 // reference's float arithmetic to rounding (checked against the CPU oracle).
 #pragma once
 #include <cuda_runtime.h>
+
+#include <type_traits>
 #include "ts_internal.cuh"
 
 namespace ts {
@@ -56,26 +58,40 @@ __device__ __forceinline__ float cpml(float d, float psi_old, float &psi_new, co
 
 // Window of 2*ORD rows of one field at column y, first row `r0`; rows
 // outside the grid read 0 (they are only used by nodes outside the regions).
-template <int ORD>
+// CHECK = false: every row is known to lie inside the grid.
+template <int ORD, bool CHECK = true>
 __device__ __forceinline__ void load_window(float (&w)[2 * ORD], const float *f, int r0, int nx, int P, int y) {
 #pragma unroll
     for (int j = 0; j < 2 * ORD; ++j) {
         const int r = r0 + j;
-        w[j] = (r >= 0 && r < nx) ? ldf(f + (int64_t)r * P + y) : 0.f;
+        w[j] = (!CHECK || (r >= 0 && r < nx)) ? ldf(f + (int64_t)r * P + y) : 0.f;
     }
 }
 
-template <int ORD>
+template <int ORD, bool CHECK = true>
 __device__ __forceinline__ void shift_window(float (&w)[2 * ORD], const float *f, int r_new, int nx, int P, int y) {
 #pragma unroll
     for (int j = 0; j < 2 * ORD - 1; ++j) w[j] = w[j + 1];
-    w[2 * ORD - 1] = (r_new >= 0 && r_new < nx) ? ldf(f + (int64_t)r_new * P + y) : 0.f;
+    w[2 * ORD - 1] = (!CHECK || (r_new >= 0 && r_new < nx)) ? ldf(f + (int64_t)r_new * P + y) : 0.f;
+}
+
+// A warp whose TX-node chunk lies wholly in the interior (every node inside
+// the update regions of both kernels, outside the CPML strips, window rows
+// inside the grid) sweeps without per-node region, strip or bounds tests.
+// Evaluated by all 32 lanes before any of them returns.
+template <int ORD, int TX>
+__device__ __forceinline__ bool interior_warp(const StepParams &p, int y, int x0, int sy) {
+    const bool lane = y < p.ny && sy < 0 && y >= ORD && y < p.ny - ORD && x0 >= ORD && x0 >= p.strip[0].lo &&
+                      x0 + TX + ORD <= p.nx && x0 + TX <= p.strip[0].hi;
+    return __all_sync(0xffffffffu, lane);
 }
 
 template <int ORD, int FAM, int ZM, int NS, int TX, bool FEAT = false, int MINB = 0>
 __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams p) {
     const int y = blockIdx.x * kBX2 + threadIdx.x;
     const int x0 = (blockIdx.y * kBY2 + threadIdx.y) * TX;
+    const int sy = y < p.ny ? strip_index(p.strip[1], y) : -1;
+    const bool fast = interior_warp<ORD, TX>(p, y, x0, sy);
     if (y >= p.ny || x0 >= p.nx) return;
     const int P = p.pitch, nx = p.nx;
     const float *__restrict__ vx = p.v[0];   // read with ldf only
@@ -84,156 +100,161 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
     constexpr int R = NS > 0 ? NS : 1;
     const bool yn = y >= ORD && y < p.ny - ORD + 1;   // normal-stress rows in y
     const bool ys = y >= ORD - 1 && y < p.ny - ORD;   // shear-stress rows in y
-    const int sy = strip_index(p.strip[1], y);
     pdl_wait();
-    // vx rows [x-ORD+1, x+ORD] (normal x-derivative), vy rows [x-ORD, x+ORD-1] (shear)
-    float wvx[2 * ORD], wvy[2 * ORD];
-    load_window<ORD>(wvx, vx, x0 - ORD + 1, nx, P, y);
-    load_window<ORD>(wvy, vy, x0 - ORD, nx, P, y);
+    auto sweep = [&](auto fast_tag) {
+        constexpr bool FAST = decltype(fast_tag)::value;
+        const int syl = FAST ? -1 : sy;
+        // vx rows [x-ORD+1, x+ORD] (normal x-derivative), vy rows [x-ORD, x+ORD-1] (shear)
+        float wvx[2 * ORD], wvy[2 * ORD];
+        load_window<ORD, !FAST>(wvx, vx, x0 - ORD + 1, nx, P, y);
+        load_window<ORD, !FAST>(wvy, vy, x0 - ORD, nx, P, y);
 
 #pragma unroll
-    for (int t = 0; t < TX; ++t) {
-        const int x = x0 + t;
-        if (x >= nx) break;
-        const int64_t i = (int64_t)x * P + y;
-        const bool in_n = yn && x >= ORD - 1 && x < nx - ORD;
-        const bool in_s = ys && x >= ORD && x < nx - ORD + 1;
-        if (in_n || in_s) {
-            const int sx = strip_index(p.strip[0], x);
-            const int64_t ix = (int64_t)sx * P + y, iy = (int64_t)x * p.strip[1].width + sy;
-            // ---- loads ----
-            float L = 0.f, M = 0.f, Ms = 0.f, gp = 1.f, gs = 1.f, sxx = 0.f, syy = 0.f, sxy = 0.f;
-            float ny_lo[ORD], ny_hi[ORD - 1 > 0 ? ORD - 1 : 1], sx_lo[ORD - 1 > 0 ? ORD - 1 : 1], sx_hi[ORD];
-            float rxx[R], ryy[R], rxy[R];
-            float pn0 = 0.f, pn1 = 0.f, ps0 = 0.f, ps1 = 0.f;
-            if (in_n) {
-                L = ldg(p.lam_dt + i);
-                M = ldg(p.mu_dt + i);
-                if (ZM == 2) gp = ldg(p.g_p + i);
+        for (int t = 0; t < TX; ++t) {
+            const int x = x0 + t;
+            if (!FAST && x >= nx) break;
+            const int64_t i = (int64_t)x * P + y;
+            const bool in_n = FAST || (yn && x >= ORD - 1 && x < nx - ORD);
+            const bool in_s = FAST || (ys && x >= ORD && x < nx - ORD + 1);
+            if (in_n || in_s) {
+                const int sx = FAST ? -1 : strip_index(p.strip[0], x);
+                const int64_t ix = (int64_t)sx * P + y, iy = (int64_t)x * p.strip[1].width + syl;
+                // ---- loads ----
+                float L = 0.f, M = 0.f, Ms = 0.f, gp = 1.f, gs = 1.f, sxx = 0.f, syy = 0.f, sxy = 0.f;
+                float ny_lo[ORD], ny_hi[ORD - 1 > 0 ? ORD - 1 : 1], sx_lo[ORD - 1 > 0 ? ORD - 1 : 1], sx_hi[ORD];
+                float rxx[R], ryy[R], rxy[R];
+                float pn0 = 0.f, pn1 = 0.f, ps0 = 0.f, ps1 = 0.f;
+                if (in_n) {
+                    L = ldg(p.lam_dt + i);
+                    M = ldg(p.mu_dt + i);
+                    if (ZM == 2) gp = ldg(p.g_p + i);
 #pragma unroll
-                for (int c = 0; c < ORD; ++c) ny_lo[c] = ldf(vy + i - c - 1);   // vy[y-c-1]
+                    for (int c = 0; c < ORD; ++c) ny_lo[c] = ldf(vy + i - c - 1);   // vy[y-c-1]
 #pragma unroll
-                for (int c = 1; c < ORD; ++c) ny_hi[c - 1] = ldf(vy + i + c);   // vy[y+c], c >= 1
-                sxx = p.s[0][i];
-                syy = p.s[1][i];
-                if (sx >= 0) pn0 = p.psi[0][ix];
-                if (sy >= 0) pn1 = p.psi[2][iy];
-                if (ZM != 0) {
-#pragma unroll
-                    for (int l = 0; l < R; ++l)
-                        if (l < n_mech) {
-                            rxx[l] = p.r[0][l * p.grid_elems + i];
-                            ryy[l] = p.r[1][l * p.grid_elems + i];
-                        }
-                }
-            }
-            if (in_s) {
-                Ms = ldg(p.mus_dt[0] + i);
-#pragma unroll
-                for (int c = 0; c < ORD; ++c) sx_hi[c] = ldf(vx + i + c + 1);   // vx[y+c+1]
-#pragma unroll
-                for (int c = 1; c < ORD; ++c) sx_lo[c - 1] = ldf(vx + i - c);   // vx[y-c], c >= 1
-                sxy = p.s[3][i];
-                if (sx >= 0) ps0 = p.psi[1][ix];
-                if (sy >= 0) ps1 = p.psi[3][iy];
-                if (ZM != 0) {
-#pragma unroll
-                    for (int l = 0; l < R; ++l)
-                        if (l < n_mech) rxy[l] = p.r[2][l * p.grid_elems + i];
-                }
-            }
-            if (ZM == 2) gs = ldg(p.g_s + i);
-            // ---- normal stresses ----
-            if (in_n) {
-                float ddx = 0.f, ddy = 0.f, np_;
-#pragma unroll
-                for (int c = 0; c < ORD; ++c) {
-                    ddx = fmaf(p.cd[0][c], wvx[c + ORD] - wvx[ORD - 1 - c], ddx);
-                    const float hi = c == 0 ? wvy[ORD] : ny_hi[c > 0 ? c - 1 : 0];
-                    ddy = fmaf(p.cd[1][c], hi - ny_lo[c], ddy);
-                }
-                if (sx >= 0) {
-                    ddx = cpml(ddx, pn0, np_, p.tab_h[0][x]);
-                    p.psi[0][ix] = np_;
-                }
-                if (sy >= 0) {
-                    ddy = cpml(ddy, pn1, np_, p.tab_f[1][y]);
-                    p.psi[2][iy] = np_;
-                }
-                if (FAM == kTaichi) {
-                    const float dl = L * (ddx + ddy);
-                    sxx += fmaf(2.f * M, ddx, dl);
-                    syy += fmaf(2.f * M, ddy, dl);
-                } else {
-                    const float L2M = fmaf(2.f, M, L);
-                    float ux = fmaf(L2M, ddx, L * ddy), uy = fmaf(L, ddx, L2M * ddy);
-                    float srxx = 0.f, sryy = 0.f;
+                    for (int c = 1; c < ORD; ++c) ny_hi[c - 1] = ldf(vy + i + c);   // vy[y+c], c >= 1
+                    sxx = p.s[0][i];
+                    syy = p.s[1][i];
+                    if (sx >= 0) pn0 = p.psi[0][ix];
+                    if (syl >= 0) pn1 = p.psi[2][iy];
                     if (ZM != 0) {
-                        const float dsum = ddx + ddy, ddif = 0.5f * (ddx - ddy);
 #pragma unroll
                         for (int l = 0; l < R; ++l)
                             if (l < n_mech) {
-                                const float a = fmaf(p.zen.Ap[l], rxx[l], (p.zen.Bp[l] * gp) * dsum);
-                                const float b = fmaf(p.zen.As[l], ryy[l], (p.zen.Bs[l] * gs) * ddif);
-                                srxx += rxx[l] + a;
-                                sryy += ryy[l] + b;
-                                p.r[0][l * p.grid_elems + i] = a;
-                                p.r[1][l * p.grid_elems + i] = b;
+                                rxx[l] = p.r[0][l * p.grid_elems + i];
+                                ryy[l] = p.r[1][l * p.grid_elems + i];
                             }
-                        const float hl = 0.5f * (L + M);
-                        ux = fmaf(hl, srxx, fmaf(M, sryy, ux));
-                        uy = fmaf(hl, srxx, fmaf(-M, sryy, uy));
-                    }
-                    sxx += ux;
-                    syy += uy;
-                    if (FEAT) {
-                        const float h = 0.5f * srxx;
-                        p.feat[kFeatLam * p.grid_elems + i] = ddx + ddy + h;
-                        p.feat[kFeatMuX * p.grid_elems + i] = fmaf(2.f, ddx, h + sryy);
-                        p.feat[kFeatMuY * p.grid_elems + i] = fmaf(2.f, ddy, h - sryy);
                     }
                 }
-                p.s[0][i] = sxx;
-                p.s[1][i] = syy;
-            }
-            // ---- shear stress ----
-            if (in_s) {
-                float a = 0.f, b = 0.f, np_;
+                if (in_s) {
+                    Ms = ldg(p.mus_dt[0] + i);
 #pragma unroll
-                for (int c = 0; c < ORD; ++c) {
-                    a = fmaf(p.cd[0][c], wvy[c + ORD] - wvy[ORD - 1 - c], a);
-                    const float lo = c == 0 ? wvx[ORD - 1] : sx_lo[c > 0 ? c - 1 : 0];
-                    b = fmaf(p.cd[1][c], sx_hi[c] - lo, b);
-                }
-                if (sx >= 0) {
-                    a = cpml(a, ps0, np_, p.tab_f[0][x]);
-                    p.psi[1][ix] = np_;
-                }
-                if (sy >= 0) {
-                    b = cpml(b, ps1, np_, p.tab_h[1][y]);
-                    p.psi[3][iy] = np_;
-                }
-                const float e = a + b;
-                float u = Ms * e, sr = 0.f;
-                if (FAM != kTaichi && ZM != 0) {
+                    for (int c = 0; c < ORD; ++c) sx_hi[c] = ldf(vx + i + c + 1);   // vx[y+c+1]
 #pragma unroll
-                    for (int l = 0; l < R; ++l)
-                        if (l < n_mech) {
-                            const float n_ = fmaf(p.zen.As[l], rxy[l], (p.zen.Bs[l] * gs) * e);
-                            sr += rxy[l] + n_;
-                            p.r[2][l * p.grid_elems + i] = n_;
+                    for (int c = 1; c < ORD; ++c) sx_lo[c - 1] = ldf(vx + i - c);   // vx[y-c], c >= 1
+                    sxy = p.s[3][i];
+                    if (sx >= 0) ps0 = p.psi[1][ix];
+                    if (syl >= 0) ps1 = p.psi[3][iy];
+                    if (ZM != 0) {
+#pragma unroll
+                        for (int l = 0; l < R; ++l)
+                            if (l < n_mech) rxy[l] = p.r[2][l * p.grid_elems + i];
+                    }
+                }
+                if (ZM == 2) gs = ldg(p.g_s + i);
+                // ---- normal stresses ----
+                if (in_n) {
+                    float ddx = 0.f, ddy = 0.f, np_;
+#pragma unroll
+                    for (int c = 0; c < ORD; ++c) {
+                        ddx = fmaf(p.cd[0][c], wvx[c + ORD] - wvx[ORD - 1 - c], ddx);
+                        const float hi = c == 0 ? wvy[ORD] : ny_hi[c > 0 ? c - 1 : 0];
+                        ddy = fmaf(p.cd[1][c], hi - ny_lo[c], ddy);
+                    }
+                    if (sx >= 0) {
+                        ddx = cpml(ddx, pn0, np_, p.tab_h[0][x]);
+                        p.psi[0][ix] = np_;
+                    }
+                    if (syl >= 0) {
+                        ddy = cpml(ddy, pn1, np_, p.tab_f[1][y]);
+                        p.psi[2][iy] = np_;
+                    }
+                    if (FAM == kTaichi) {
+                        const float dl = L * (ddx + ddy);
+                        sxx += fmaf(2.f * M, ddx, dl);
+                        syy += fmaf(2.f * M, ddy, dl);
+                    } else {
+                        const float L2M = fmaf(2.f, M, L);
+                        float ux = fmaf(L2M, ddx, L * ddy), uy = fmaf(L, ddx, L2M * ddy);
+                        float srxx = 0.f, sryy = 0.f;
+                        if (ZM != 0) {
+                            const float dsum = ddx + ddy, ddif = 0.5f * (ddx - ddy);
+#pragma unroll
+                            for (int l = 0; l < R; ++l)
+                                if (l < n_mech) {
+                                    const float a = fmaf(p.zen.Ap[l], rxx[l], (p.zen.Bp[l] * gp) * dsum);
+                                    const float b = fmaf(p.zen.As[l], ryy[l], (p.zen.Bs[l] * gs) * ddif);
+                                    srxx += rxx[l] + a;
+                                    sryy += ryy[l] + b;
+                                    p.r[0][l * p.grid_elems + i] = a;
+                                    p.r[1][l * p.grid_elems + i] = b;
+                                }
+                            const float hl = 0.5f * (L + M);
+                            ux = fmaf(hl, srxx, fmaf(M, sryy, ux));
+                            uy = fmaf(hl, srxx, fmaf(-M, sryy, uy));
                         }
-                    u = fmaf(0.5f * Ms, sr, u);
+                        sxx += ux;
+                        syy += uy;
+                        if (FEAT) {
+                            const float h = 0.5f * srxx;
+                            p.feat[kFeatLam * p.grid_elems + i] = ddx + ddy + h;
+                            p.feat[kFeatMuX * p.grid_elems + i] = fmaf(2.f, ddx, h + sryy);
+                            p.feat[kFeatMuY * p.grid_elems + i] = fmaf(2.f, ddy, h - sryy);
+                        }
+                    }
+                    p.s[0][i] = sxx;
+                    p.s[1][i] = syy;
                 }
-                if (FEAT) p.feat[kFeatShear * p.grid_elems + i] = fmaf(0.5f, sr, e);
-                p.s[3][i] = sxy + u;
+                // ---- shear stress ----
+                if (in_s) {
+                    float a = 0.f, b = 0.f, np_;
+#pragma unroll
+                    for (int c = 0; c < ORD; ++c) {
+                        a = fmaf(p.cd[0][c], wvy[c + ORD] - wvy[ORD - 1 - c], a);
+                        const float lo = c == 0 ? wvx[ORD - 1] : sx_lo[c > 0 ? c - 1 : 0];
+                        b = fmaf(p.cd[1][c], sx_hi[c] - lo, b);
+                    }
+                    if (sx >= 0) {
+                        a = cpml(a, ps0, np_, p.tab_f[0][x]);
+                        p.psi[1][ix] = np_;
+                    }
+                    if (syl >= 0) {
+                        b = cpml(b, ps1, np_, p.tab_h[1][y]);
+                        p.psi[3][iy] = np_;
+                    }
+                    const float e = a + b;
+                    float u = Ms * e, sr = 0.f;
+                    if (FAM != kTaichi && ZM != 0) {
+#pragma unroll
+                        for (int l = 0; l < R; ++l)
+                            if (l < n_mech) {
+                                const float n_ = fmaf(p.zen.As[l], rxy[l], (p.zen.Bs[l] * gs) * e);
+                                sr += rxy[l] + n_;
+                                p.r[2][l * p.grid_elems + i] = n_;
+                            }
+                        u = fmaf(0.5f * Ms, sr, u);
+                    }
+                    if (FEAT) p.feat[kFeatShear * p.grid_elems + i] = fmaf(0.5f, sr, e);
+                    p.s[3][i] = sxy + u;
+                }
+            }
+            if (t + 1 < TX) {
+                shift_window<ORD, !FAST>(wvx, vx, x + ORD + 1, nx, P, y);
+                shift_window<ORD, !FAST>(wvy, vy, x + ORD, nx, P, y);
             }
         }
-        if (t + 1 < TX) {
-            shift_window<ORD>(wvx, vx, x + ORD + 1, nx, P, y);
-            shift_window<ORD>(wvy, vy, x + ORD, nx, P, y);
-        }
-    }
+    };
+    if (fast) sweep(std::true_type{});
+    else sweep(std::false_type{});
     pdl_trigger();
 }
 
@@ -253,25 +274,28 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
     const bool yvy = y >= ORD - 1 && y < p.ny - ORD;
     const bool yvx = FAM == kTaichi ? (y >= ORD && y < p.ny - ORD + 1) : (yvy && y >= ORD);
     const int q0 = __ldg(p.src_block_start + blk), q1 = __ldg(p.src_block_start + blk + 1);
+    const bool fast = interior_warp<ORD, TX>(p, y, x0, sy) && q0 == q1;   // no source node in the block
     pdl_wait();
     const int k = *p.step_base + j;
-    float vmax = 0.f;
+    unsigned vmax = 0u;  // max |v|^2 as float bits (v2 >= 0 or NaN: NaN ranks highest)
     bool bad = false;
 
-    if (live_col && x0 < nx) {
+    auto sweep = [&](auto fast_tag) {
+        constexpr bool FAST = decltype(fast_tag)::value;
+        const int syl = FAST ? -1 : sy;
         // sxx rows [x-ORD, x+ORD-1] (vx), sxy rows [x-ORD+1, x+ORD] (vy; row x also feeds vx's y-derivative)
         float wxx[2 * ORD], wxy[2 * ORD];
-        load_window<ORD>(wxx, sxx, x0 - ORD, nx, P, y);
-        load_window<ORD>(wxy, sxy, x0 - ORD + 1, nx, P, y);
+        load_window<ORD, !FAST>(wxx, sxx, x0 - ORD, nx, P, y);
+        load_window<ORD, !FAST>(wxy, sxy, x0 - ORD + 1, nx, P, y);
 #pragma unroll
         for (int t = 0; t < TX; ++t) {
             const int x = x0 + t;
-            if (x >= nx) break;
+            if (!FAST && x >= nx) break;
             const int64_t i = (int64_t)x * P + y;
-            const bool in_vy = yvy && x >= ORD - 1 && x < nx - ORD;
-            const bool in_vx = FAM == kTaichi ? (yvx && x >= ORD && x < nx - ORD + 1) : (yvx && in_vy && x >= ORD);
-            const int sx = strip_index(p.strip[0], x);
-            const int64_t ix = (int64_t)sx * P + y, iy = (int64_t)x * p.strip[1].width + sy;
+            const bool in_vy = FAST || (yvy && x >= ORD - 1 && x < nx - ORD);
+            const bool in_vx = FAST || (FAM == kTaichi ? (yvx && x >= ORD && x < nx - ORD + 1) : (yvx && in_vy && x >= ORD));
+            const int sx = FAST ? -1 : strip_index(p.strip[0], x);
+            const int64_t ix = (int64_t)sx * P + y, iy = (int64_t)x * p.strip[1].width + syl;
             // ---- loads ----
             float bx_lo[ORD], bx_hi[ORD - 1 > 0 ? ORD - 1 : 1], by[2 * ORD];
             float vx0 = 0.f, vy0 = 0.f, dx0 = 0.f, dy0 = 0.f, pxa = 0.f, pxb = 0.f, pya = 0.f, pyb = 0.f;
@@ -283,7 +307,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                 vx0 = p.v[0][i];
                 dx0 = ldg(p.dtr[0] + i);
                 if (sx >= 0) pxa = p.psi[4][ix];
-                if (sy >= 0) pxb = p.psi[6][iy];
+                if (syl >= 0) pxb = p.psi[6][iy];
             }
             if (in_vy) {
 #pragma unroll
@@ -291,7 +315,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                 vy0 = p.v[1][i];
                 dy0 = ldg(p.dtr[1] + i);
                 if (sx >= 0) pya = p.psi[5][ix];
-                if (sy >= 0) pyb = p.psi[7][iy];
+                if (syl >= 0) pyb = p.psi[7][iy];
             }
             // ---- update ----
             float vxn = 0.f, vyn = 0.f, np_, fax = 0.f, fay = 0.f;
@@ -307,7 +331,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                     a = cpml(a, pxa, np_, p.tab_f[0][x]);
                     p.psi[4][ix] = np_;
                 }
-                if (sy >= 0) {
+                if (syl >= 0) {
                     b = cpml(b, pxb, np_, p.tab_f[1][y]);
                     p.psi[6][iy] = np_;
                 }
@@ -325,17 +349,19 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                     a = cpml(a, pya, np_, p.tab_h[0][x]);
                     p.psi[5][ix] = np_;
                 }
-                if (sy >= 0) {
+                if (syl >= 0) {
                     b = cpml(b, pyb, np_, p.tab_h[1][y]);
                     p.psi[7][iy] = np_;
                 }
                 fay = a + b;
                 vyn = fmaf(fay, dy0, vy0);
             }
-            for (int q = q0; q < q1; ++q) {
-                const Source s = p.src[q];
-                if (s.cell == i && k < p.src_rows)
-                    vyn = fmaf(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), s.scale, vyn);
+            if constexpr (!FAST) {
+                for (int q = q0; q < q1; ++q) {
+                    const Source s = p.src[q];
+                    if (s.cell == i && k < p.src_rows)
+                        vyn = fmaf(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), s.scale, vyn);
+                }
             }
             p.v[0][i] = vxn;
             p.v[1][i] = vyn;
@@ -345,14 +371,15 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             }
             const float v2 = fmaf(vxn, vxn, vyn * vyn);
             bad |= !(v2 <= p.v2_threshold);
-            vmax = fmaxf(vmax, v2);
-            if (v2 != v2) vmax = v2;  // keep a NaN visible
+            vmax = max(vmax, __float_as_uint(v2));
             if (t + 1 < TX) {
-                shift_window<ORD>(wxx, sxx, x + ORD, nx, P, y);
-                shift_window<ORD>(wxy, sxy, x + ORD + 1, nx, P, y);
+                shift_window<ORD, !FAST>(wxx, sxx, x + ORD, nx, P, y);
+                shift_window<ORD, !FAST>(wxy, sxy, x + ORD + 1, nx, P, y);
             }
         }
-    }
+    };
+    if (fast) sweep(std::true_type{});
+    else if (live_col && x0 < nx) sweep(std::false_type{});
 
     // receivers: global thread g samples receiver g (syy is final for step k)
     const int g = blk * (kBX2 * kBY2) + tid;
@@ -361,7 +388,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
         for (int q = __ldg(p.rec_start + g); q < __ldg(p.rec_start + g + 1); ++q) acc += ldf(syy + __ldg(p.rec_cell + q));
         p.traces[(int64_t)k * p.n_rec + g] = acc;
     }
-    warp_stability(vmax, bad, reinterpret_cast<unsigned *>(p.block_max) + blk, p.first_bad, k);
+    warp_stability(__uint_as_float(vmax), bad, reinterpret_cast<unsigned *>(p.block_max) + blk, p.first_bad, k);
     pdl_trigger();
 }
 
