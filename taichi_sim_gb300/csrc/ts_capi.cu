@@ -268,13 +268,13 @@ int ts_create(const ts_desc *d, ts_sim **out) {
 
     StepParams &p = s->p;
     p.family = s->family;
-    // nodes per thread along x (2D): enough blocks to fill the GPU, as few
+    // nodes per thread along x (2D; 3D velocity kernel): enough blocks to fill the GPU, as few
     // index/region/bookkeeping instructions per node as that allows
     {
         const int64_t cells = (int64_t)d->nx * d->ny;
         // measured on GB300: 2 nodes per thread is fastest from ~200k nodes
         // (1024^2 viscoelastic, 512^2 elastic); 4 loses occupancy to registers
-        p.tx = s->dims == 3 ? 1 : (cells >= 200000 ? 2 : 1);
+        p.tx = s->dims == 3 ? ts::velocity_tx_3d(d->ord) : (cells >= 200000 ? 2 : 1);
         if (const char *env = getenv("TS_2D_NODES_PER_THREAD")) {
             const int v = atoi(env);
             if (v == 1 || v == 2 || v == 4) p.tx = v;

@@ -164,14 +164,16 @@ inline int block_of_2d(const StepParams &p, int x, int y) {
     return (x / (kBY2 * p.tx)) * gx + y / kBX2;
 }
 // 3D kernels: blocks of 32 (z) x 8 (y) threads, each updating kTX3S (stress
-// kernels) or kTX3 (velocity kernel) consecutive nodes along x (measured on
-// the 256^3 three-mechanism case against 1, 2 and 4).
-constexpr int kBX3 = 32, kBY3 = 8, kTX3 = 2, kTX3S = 4;
+// kernels) or p.tx (velocity kernel: 4 for order 2, 2 above, where 4 spills)
+// consecutive nodes along x (measured on the 256^3 three-mechanism case
+// against 1, 2 and 4).
+constexpr int kBX3 = 32, kBY3 = 8, kTX3S = 4;
+constexpr int velocity_tx_3d(int ord) { return ord == 2 ? 4 : 2; }
 
 // Flat index of the 3D velocity block that updates node (x, y, z).
 inline int block_of_3d(const StepParams &p, int x, int y, int z) {
     const int gx = (p.nz + kBX3 - 1) / kBX3, gy = (p.ny + kBY3 - 1) / kBY3;
-    return ((x / kTX3) * gy + y / kBY3) * gx + z / kBX3;
+    return ((x / p.tx) * gy + y / kBY3) * gx + z / kBX3;
 }
 
 }  // namespace ts

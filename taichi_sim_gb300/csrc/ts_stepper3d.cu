@@ -18,6 +18,8 @@
 // cs == 0 test, vz uses the vy-node density, all three velocities are zeroed
 // outside the vz region, the source drives vz).
 #include <cuda_runtime.h>
+
+#include <type_traits>
 #include "ts_internal.cuh"
 
 namespace ts {
@@ -67,20 +69,33 @@ __device__ __forceinline__ float deriv(const Pairs<ORD> &q, const float *cd) {
 constexpr int kStressMinBlocks = 4, kVelocityMinBlocks = 3;
 // x window of 2*ORD planes of one field at (y, z), first plane r0; planes
 // outside the grid read 0
-template <int ORD, typename I>
+// (CHECK = false: every plane is known to lie inside the grid)
+template <int ORD, bool CHECK = true, typename I>
 __device__ __forceinline__ void xwindow(float (&w)[2 * ORD], const float *f, int r0, int nx, I X, I yz) {
 #pragma unroll
     for (int j = 0; j < 2 * ORD; ++j) {
         const int r = r0 + j;
-        w[j] = (r >= 0 && r < nx) ? fld(f + r * X + yz) : 0.f;
+        w[j] = (!CHECK || (r >= 0 && r < nx)) ? fld(f + r * X + yz) : 0.f;
     }
 }
 
-template <int ORD, typename I>
+template <int ORD, bool CHECK = true, typename I>
 __device__ __forceinline__ void xshift(float (&w)[2 * ORD], const float *f, int r_new, int nx, I X, I yz) {
 #pragma unroll
     for (int j = 0; j < 2 * ORD - 1; ++j) w[j] = w[j + 1];
-    w[2 * ORD - 1] = (r_new >= 0 && r_new < nx) ? fld(f + r_new * X + yz) : 0.f;
+    w[2 * ORD - 1] = (!CHECK || (r_new >= 0 && r_new < nx)) ? fld(f + r_new * X + yz) : 0.f;
+}
+
+// A warp whose TX-node chunks lie wholly in the interior (every node inside
+// the update regions of all three kernels, outside the CPML strips, window
+// planes inside the grid) sweeps without per-node region, strip or bounds
+// tests.  Evaluated by all 32 lanes before any of them returns.
+template <int ORD, int TX>
+__device__ __forceinline__ bool interior_warp(const StepParams &p, int y, int z, int x0, int sy, int sz) {
+    const bool lane = y < p.ny && z < p.nz && sy < 0 && sz < 0 && y >= ORD && y < p.ny - ORD && z >= ORD &&
+                      z < p.nz - ORD && x0 >= ORD && x0 >= p.strip[0].lo && x0 + TX + ORD <= p.nx &&
+                      x0 + TX <= p.strip[0].hi;
+    return __all_sync(0xffffffffu, lane);
 }
 
 // sum_c cd[c] (w[ORD + c] - w[ORD - 1 - c])
@@ -342,14 +357,14 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_shear3d(const 
     pdl_trigger();
 }
 
-// Velocity update, x-marching: thread (z, y) updates kTX3 consecutive nodes
+// Velocity update, x-marching: thread (z, y) updates TX consecutive nodes
 // along x; the x-derivatives of sxx, sxy, sxz come from register windows that
 // take one new plane per node, the y- and z-derivatives from loads.
-template <int ORD, typename I>
+template <int ORD, typename I, int TX>
 __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(const StepParams p, const int j) {
     const int z = blockIdx.x * kBX3 + threadIdx.x;
     const int y = blockIdx.y * kBY3 + threadIdx.y;
-    const int x0 = blockIdx.z * kTX3;
+    const int x0 = blockIdx.z * TX;
     const int tid = threadIdx.y * kBX3 + threadIdx.x;
     const int blk = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
     const bool col = y < p.ny && z < p.nz;
@@ -360,32 +375,35 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
     const float *__restrict__ sxy = p.s[3];
     const float *__restrict__ sxz = p.s[4];
     const float *__restrict__ syz = p.s[5];
-    const int sy = strip_index(p.strip[1], y), sz = strip_index(p.strip[2], z);
+    const int sy = col ? strip_index(p.strip[1], y) : -1, sz = col ? strip_index(p.strip[2], z) : -1;
     // vz region in (y, z); outside the vz region all three components are zero (wgsl:1754-1758)
     const bool yz_vz = col && y >= ORD && y < p.ny - ORD + 1 && z >= ORD - 1 && z < p.nz - ORD;
     const int q0 = __ldg(p.src_block_start + blk), q1 = __ldg(p.src_block_start + blk + 1);
+    const bool fast = interior_warp<ORD, TX>(p, y, z, x0, sy, sz) && q0 == q1;   // no source node in the block
     pdl_wait();
     const int k = *p.step_base + j;
-    float vmax = 0.f;
+    unsigned vmax = 0u;  // max |v|^2 as float bits (v2 >= 0 or NaN: NaN ranks highest)
     bool bad = false;
-    if (col && x0 < p.nx) {
+    auto sweep = [&](auto fast_tag) {
+        constexpr bool FAST = decltype(fast_tag)::value;
+        const int syl = FAST ? -1 : sy, szl = FAST ? -1 : sz;
         // sxx planes [x-ORD, x+ORD-1] (vx), sxy and sxz planes [x-ORD+1, x+ORD] (vy, vz)
         float wa[2 * ORD], wb[2 * ORD], wc[2 * ORD];
-        xwindow<ORD>(wa, sxx, x0 - ORD, p.nx, X, yz);
-        xwindow<ORD>(wb, sxy, x0 - ORD + 1, p.nx, X, yz);
-        xwindow<ORD>(wc, sxz, x0 - ORD + 1, p.nx, X, yz);
+        xwindow<ORD, !FAST>(wa, sxx, x0 - ORD, p.nx, X, yz);
+        xwindow<ORD, !FAST>(wb, sxy, x0 - ORD + 1, p.nx, X, yz);
+        xwindow<ORD, !FAST>(wc, sxz, x0 - ORD + 1, p.nx, X, yz);
 #pragma unroll
-        for (int t = 0; t < kTX3; ++t) {
+        for (int t = 0; t < TX; ++t) {
             const int x = x0 + t;
-            if (x >= p.nx) break;
+            if (!FAST && x >= p.nx) break;
             const I i = (I)x * X + yz;
-            const bool in_vz = yz_vz && x >= ORD - 1 && x < p.nx - ORD;
-            const bool in_vx = in_vz && x >= ORD && z >= ORD;        // vx region within the vz region
-            const bool in_vy = in_vz && y < p.ny - ORD && z >= ORD;  // vy region within the vz region
-            const int sx = strip_index(p.strip[0], x);
+            const bool in_vz = FAST || (yz_vz && x >= ORD - 1 && x < p.nx - ORD);
+            const bool in_vx = FAST || (in_vz && x >= ORD && z >= ORD);        // vx region within the vz region
+            const bool in_vy = FAST || (in_vz && y < p.ny - ORD && z >= ORD);  // vy region within the vz region
+            const int sx = FAST ? -1 : strip_index(p.strip[0], x);
             const I ix = ((I)sx * p.ny + y) * Y + z;
-            const I iy = ((I)x * p.strip[1].width + sy) * Y + z;
-            const I iz = ((I)x * p.ny + y) * p.strip[2].width + sz;
+            const I iy = ((I)x * p.strip[1].width + syl) * Y + z;
+            const I iz = ((I)x * p.ny + y) * p.strip[2].width + szl;
             // ---- loads ----
             Pairs<ORD> xb, xe, yb, ye, zb, ze;
             float v0[3] = {0.f, 0.f, 0.f}, dtx = 0.f, dty = 0.f;
@@ -396,16 +414,16 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
                 v0[0] = p.v[0][i];
                 dtx = __ldg(p.dtr[0] + i);
                 if (sx >= 0) psi[0] = p.psi[9][ix];
-                if (sy >= 0) psi[1] = p.psi[10][iy];
-                if (sz >= 0) psi[2] = p.psi[11][iz];
+                if (syl >= 0) psi[1] = p.psi[10][iy];
+                if (szl >= 0) psi[2] = p.psi[11][iz];
             }
             if (in_vy) {
                 yb = load_pairs<ORD, true>(syy, i, Y);
                 ye = load_pairs<ORD, false>(syz, i, (I)1);
                 v0[1] = p.v[1][i];
                 if (sx >= 0) psi[3] = p.psi[12][ix];
-                if (sy >= 0) psi[4] = p.psi[13][iy];
-                if (sz >= 0) psi[5] = p.psi[14][iz];
+                if (syl >= 0) psi[4] = p.psi[13][iy];
+                if (szl >= 0) psi[5] = p.psi[14][iz];
             }
             if (in_vz) {
                 zb = load_pairs<ORD, false>(syz, i, Y);
@@ -413,8 +431,8 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
                 v0[2] = p.v[2][i];
                 dty = __ldg(p.dtr[1] + i);
                 if (sx >= 0) psi[6] = p.psi[15][ix];
-                if (sy >= 0) psi[7] = p.psi[16][iy];
-                if (sz >= 0) psi[8] = p.psi[17][iz];
+                if (syl >= 0) psi[7] = p.psi[16][iy];
+                if (szl >= 0) psi[8] = p.psi[17][iz];
             }
             // ---- update ----
             float vxn = 0.f, vyn = 0.f, vzn = 0.f, np_;
@@ -425,11 +443,11 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
                     a = cpml(a, psi[0], np_, p.tab_f[0][x]);
                     p.psi[9][ix] = np_;
                 }
-                if (sy >= 0) {
+                if (syl >= 0) {
                     b = cpml(b, psi[1], np_, p.tab_f[1][y]);
                     p.psi[10][iy] = np_;
                 }
-                if (sz >= 0) {
+                if (szl >= 0) {
                     e = cpml(e, psi[2], np_, p.tab_f[2][z]);
                     p.psi[11][iz] = np_;
                 }
@@ -442,11 +460,11 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
                     a = cpml(a, psi[3], np_, p.tab_h[0][x]);
                     p.psi[12][ix] = np_;
                 }
-                if (sy >= 0) {
+                if (syl >= 0) {
                     b = cpml(b, psi[4], np_, p.tab_h[1][y]);
                     p.psi[13][iy] = np_;
                 }
-                if (sz >= 0) {
+                if (szl >= 0) {
                     e = cpml(e, psi[5], np_, p.tab_f[2][z]);
                     p.psi[14][iz] = np_;
                 }
@@ -459,35 +477,38 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
                     a = cpml(a, psi[6], np_, p.tab_h[0][x]);
                     p.psi[15][ix] = np_;
                 }
-                if (sy >= 0) {
+                if (syl >= 0) {
                     b = cpml(b, psi[7], np_, p.tab_f[1][y]);
                     p.psi[16][iy] = np_;
                 }
-                if (sz >= 0) {
+                if (szl >= 0) {
                     e = cpml(e, psi[8], np_, p.tab_h[2][z]);
                     p.psi[17][iz] = np_;
                 }
                 vzn = fmaf(a + b + e, dty, v0[2]);  // the vy-node density (wgsl3d:1748)
             }
-            for (int q = q0; q < q1; ++q) {
-                const Source s = p.src[q];
-                if (s.cell == i && k < p.src_rows)
-                    vzn = fmaf(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), s.scale, vzn);
+            if constexpr (!FAST) {
+                for (int q = q0; q < q1; ++q) {
+                    const Source s = p.src[q];
+                    if (s.cell == i && k < p.src_rows)
+                        vzn = fmaf(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), s.scale, vzn);
+                }
             }
             p.v[0][i] = vxn;
             p.v[1][i] = vyn;
             p.v[2][i] = vzn;
             const float v2 = fmaf(vxn, vxn, fmaf(vyn, vyn, vzn * vzn));
             bad |= !(v2 <= p.v2_threshold);
-            vmax = fmaxf(vmax, v2);
-            if (v2 != v2) vmax = v2;  // keep a NaN visible
-            if (t + 1 < kTX3) {
-                xshift<ORD>(wa, sxx, x + ORD, p.nx, X, yz);
-                xshift<ORD>(wb, sxy, x + ORD + 1, p.nx, X, yz);
-                xshift<ORD>(wc, sxz, x + ORD + 1, p.nx, X, yz);
+            vmax = max(vmax, __float_as_uint(v2));
+            if (t + 1 < TX) {
+                xshift<ORD, !FAST>(wa, sxx, x + ORD, p.nx, X, yz);
+                xshift<ORD, !FAST>(wb, sxy, x + ORD + 1, p.nx, X, yz);
+                xshift<ORD, !FAST>(wc, sxz, x + ORD + 1, p.nx, X, yz);
             }
         }
-    }
+    };
+    if (fast) sweep(std::true_type{});
+    else if (col && x0 < p.nx) sweep(std::false_type{});
 
     // receivers: global thread g samples receiver g (szz is final for step k)
     const int g = blk * (kBX3 * kBY3) + tid;
@@ -496,7 +517,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
         for (int q = __ldg(p.rec_start + g); q < __ldg(p.rec_start + g + 1); ++q) acc += fld(szz + __ldg(p.rec_cell + q));
         p.traces[(int64_t)k * p.n_rec + g] = acc;
     }
-    warp_stability(vmax, bad, reinterpret_cast<unsigned *>(p.block_max) + blk, p.first_bad, k);
+    warp_stability(__uint_as_float(vmax), bad, reinterpret_cast<unsigned *>(p.block_max) + blk, p.first_bad, k);
     pdl_trigger();
 }
 
@@ -524,8 +545,8 @@ void launch_idx(const StepParams &p, int zen_mode, int j, cudaStream_t st, int p
         }
     }
     if (parts & 2) {
-        const dim3 grid((p.nz + kBX3 - 1) / kBX3, (p.ny + kBY3 - 1) / kBY3, (p.nx + kTX3 - 1) / kTX3);
-        launch_pdl(k_velocity3d<ORD, I>, grid, block, st, p, j);
+        const dim3 grid((p.nz + kBX3 - 1) / kBX3, (p.ny + kBY3 - 1) / kBY3, (p.nx + p.tx - 1) / p.tx);
+        launch_pdl(k_velocity3d<ORD, I, velocity_tx_3d(ORD)>, grid, block, st, p, j);  // p.tx == velocity_tx_3d(ORD)
     }
 }
 
@@ -542,7 +563,7 @@ void launch_ord(const StepParams &p, int zen_mode, int j, cudaStream_t st, int p
 }  // namespace
 
 int blocks_3d(const StepParams &p) {
-    return ((p.nz + kBX3 - 1) / kBX3) * ((p.ny + kBY3 - 1) / kBY3) * ((p.nx + kTX3 - 1) / kTX3);
+    return ((p.nz + kBX3 - 1) / kBX3) * ((p.ny + kBY3 - 1) / kBY3) * ((p.nx + p.tx - 1) / p.tx);
 }
 
 void launch_step_3d(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st, int parts) {

@@ -138,3 +138,48 @@ def rel_l2(a, b):
     b = np.asarray(b, np.float64)
     nb = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a - b))
+
+
+def _strip_bounds(n, ord_, tabs):
+    """CPML strip [0, lo) + [hi, n) of one grid axis as the library derives
+    it: nodes whose CPML tables (re-indexed by node, offset ord - 1) differ
+    from the identity a = 0, b = 1, 1/k = 1."""
+    off = ord_ - 1
+    a, b, k, ah, bh, kh = (np.asarray(t, np.float32).ravel() for t in tabs)
+    nonid = np.zeros(n, bool)
+    for x in range(n):
+        t = x - off
+        if 0 <= t < n - 2 * off:
+            full = a[t] != 0 or b[t] != 1 or np.float32(1) / k[t] != 1
+            half = ah[t] != 0 or bh[t] != 1 or np.float32(1) / kh[t] != 1
+            nonid[x] = full or half
+    lo = max([x + 1 for x in range(n // 2) if nonid[x]], default=0)
+    hi = min([x for x in range(n // 2, n) if nonid[x]], default=n)
+    return lo, hi
+
+
+def _axis_tabs(sim, ax):
+    return [getattr(sim, f"_{c}_{ax}{s}") for s in ("", "_half") for c in "abk"]
+
+
+def interior_warps(sim, tx):
+    """Number of warps of the single-shot step kernels that take the interior
+    sweep (32 lanes along the contiguous axis, tx nodes along x per thread):
+    every node of the warp inside the update regions, outside the CPML strips
+    and with its window rows inside the grid (source blocks aside)."""
+    shape = sim.grid_shape()
+    ord_ = int(sim._coefs.shape[0])
+    axes = ("x", "y") if len(shape) == 2 else ("x", "y", "z")
+    bounds = [_strip_bounds(n, ord_, _axis_tabs(sim, a)) for n, a in zip(shape, axes)]
+    nx, lanes_n = shape[0], shape[-1]
+    lo_l, hi_l = bounds[-1]
+    lane_ok = [(0 <= c < lanes_n and c >= max(ord_, lo_l) and c < min(lanes_n - ord_, hi_l))
+               for c in range(((lanes_n + 31) // 32) * 32)]
+    warps_lane = sum(all(lane_ok[w * 32:(w + 1) * 32]) for w in range(len(lane_ok) // 32))
+    lo_x, hi_x = bounds[0]
+    chunks = sum(x0 >= max(ord_, lo_x) and x0 + tx + ord_ <= nx and x0 + tx <= hi_x for x0 in range(0, nx, tx))
+    rows = 1
+    if len(shape) == 3:
+        lo_y, hi_y = bounds[1]
+        rows = sum(max(ord_, lo_y) <= y < min(shape[1] - ord_, hi_y) for y in range(shape[1]))
+    return warps_lane * chunks * rows

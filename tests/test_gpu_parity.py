@@ -37,6 +37,9 @@ CASES_3D = {
     "wgsl3d_visco": lambda: case_3d(visco=1),
     "wgsl3d_visco_matrix_q": lambda: case_3d(visco=1, matrix=True, q=(30.0, 300.0), seed=4),
     "wgsl3d_acc4": lambda: case_3d(visco=1, acc=4, seed=5, w=34, d=30, h=36),
+    # deep enough along z for warps that take the interior sweep
+    "wgsl3d_visco_deep": lambda: case_3d(visco=1, h=64, seed=6),
+    "wgsl3d_acc4_deep": lambda: case_3d(visco=1, acc=4, h=70, seed=7, q=(30.0, 300.0)),
 }
 
 
