@@ -180,10 +180,16 @@ __device__ __forceinline__ void bshift(float (&w)[2 * ORD][SPT], const float *f,
         for (int q = 0; q < SPT; ++q) w[2 * ORD - 1][q] = 0.f;
 }
 
-// Register budget: 64 per thread for one shot per thread, 128 for two.
+// Register budget of the stress kernel: 64 per thread for one shot per
+// thread, 128 for two.  The velocity kernel takes 128 in both cases: its
+// interior sweep holds every load of the thread's nodes at once.
 template <int CY, int SPT>
 struct MinBlocks {
     static constexpr int v = (SPT == 1 ? 32 : 16) / CY;
+};
+template <int CY>
+struct MinBlocksV {
+    static constexpr int v = 16 / CY;
 };
 
 template <int ORD, int ZM, int NS, int CY, int TX, int SPT>
@@ -381,7 +387,7 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bstress(co
 }
 
 template <int ORD, int CY, int TX, int SPT>
-__global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bvelocity(const __grid_constant__ BParams p,
+__global__ void __launch_bounds__(32 * CY, (MinBlocksV<CY>::v)) k_bvelocity(const __grid_constant__ BParams p,
                                                                               const int j) {
     constexpr int W = 32 * SPT, Y = W;
     const Loc at = locate<1, CY, TX, SPT>(p);
@@ -422,6 +428,60 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bvelocity(
     // with no per-node region, strip, bounds or source tests.
     const bool fast = at.live && sy < 0 && q0 == q1 && y >= ORD && y < ny - ORD && at.x0 >= ORD &&
                       at.x0 >= stx.lo && at.x0 + TX + ORD <= nx && at.x0 + TX <= stx.hi;
+    // The interior sweep issues every load of the thread's TX nodes before
+    // the first update, so the thread waits for memory once, not once per
+    // node: x rows x0-ORD .. x0+TX+ORD-2 of sxx and x0-ORD+1 .. x0+TX+ORD-1
+    // of sxy, and per node the y-neighbours of sxy and syy, vx, vy, dt/rho.
+    auto interior = [&]() {
+        constexpr int NR = TX + 2 * ORD - 1;
+        float rxx[NR][SPT], rxy[NR][SPT];
+        float bxh[TX][ORD][SPT], bxl[TX][ORD][SPT], byh[TX][ORD][SPT], byl[TX][ORD][SPT];
+        float vx0[TX][SPT], vy0[TX][SPT], dx0[TX], dy0[TX];
+#pragma unroll
+        for (int r = 0; r < NR; ++r) {
+            ldf<SPT>(rxx[r], sxx + (at.x0 - ORD + r) * X + col);
+            ldf<SPT>(rxy[r], sxy + (at.x0 - ORD + 1 + r) * X + col);
+        }
+#pragma unroll
+        for (int t = 0; t < TX; ++t) {
+            const int i = at.i0 + t * X, cell = at.cell0 + t * ny;
+#pragma unroll
+            for (int c = 0; c < ORD; ++c) {
+                ldf<SPT>(bxh[t][c], sxy + i + c * Y);         // sxy[y+c]
+                ldf<SPT>(bxl[t][c], sxy + i - (c + 1) * Y);   // sxy[y-c-1]
+                ldf<SPT>(byh[t][c], syy + i + (c + 1) * Y);   // syy[y+c+1]
+                ldf<SPT>(byl[t][c], syy + i - c * Y);         // syy[y-c]
+            }
+            ldo<SPT>(vx0[t], v0 + i);
+            ldo<SPT>(vy0[t], v1 + i);
+            dx0[t] = __ldg(dtr0 + cell);
+            dy0[t] = __ldg(dtr1 + cell);
+        }
+#pragma unroll
+        for (int t = 0; t < TX; ++t) {
+            const int i = at.i0 + t * X;
+            float vxn[SPT], vyn[SPT];
+#pragma unroll
+            for (int q = 0; q < SPT; ++q) {
+                float ax = 0.f, bx = 0.f, ay = 0.f, by = 0.f;
+#pragma unroll
+                for (int c = 0; c < ORD; ++c) {
+                    // rows x+c / x-c-1 of sxx and x+c+1 / x-c of sxy sit at t+ORD+c / t+ORD-1-c
+                    ax = fmaf(cdx[c], rxx[t + ORD + c][q] - rxx[t + ORD - 1 - c][q], ax);
+                    bx = fmaf(cdy[c], bxh[t][c][q] - bxl[t][c][q], bx);
+                    ay = fmaf(cdx[c], rxy[t + ORD + c][q] - rxy[t + ORD - 1 - c][q], ay);
+                    by = fmaf(cdy[c], byh[t][c][q] - byl[t][c][q], by);
+                }
+                vxn[q] = fmaf(ax + bx, dx0[t], vx0[t][q]);
+                vyn[q] = fmaf(ay + by, dy0[t], vy0[t][q]);
+                const float v2 = fmaf(vxn[q], vxn[q], vyn[q] * vyn[q]);
+                bad |= !(v2 <= p.v2_threshold);
+                vmax = max(vmax, __float_as_uint(v2));
+            }
+            sto<SPT>(v0 + i, vxn);
+            sto<SPT>(v1 + i, vyn);
+        }
+    };
     auto sweep = [&](auto fast_tag) {
         constexpr bool FAST = decltype(fast_tag)::value;
         const int syl = FAST ? -1 : sy;
@@ -522,7 +582,7 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bvelocity(
             }
         }
     };
-    if (fast) sweep(std::true_type{});
+    if (fast) interior();
     else if (at.live) sweep(std::false_type{});
     // receivers: flat work item g = (phantom, shot, receiver)
     const int g = blockIdx.x * (32 * CY) + threadIdx.y * 32 + threadIdx.x;
