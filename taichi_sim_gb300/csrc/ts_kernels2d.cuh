@@ -280,6 +280,66 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
     unsigned vmax = 0u;  // max |v|^2 as float bits (v2 >= 0 or NaN: NaN ranks highest)
     bool bad = false;
 
+    // The interior sweep issues every load of the thread's TX nodes before
+    // the first update (one memory latency per thread, not per node): sxx
+    // rows x0-ORD .. x0+TX+ORD-2, sxy rows x0-ORD+1 .. x0+TX+ORD-1, and per
+    // node the y-neighbours of sxy and syy, vx, vy and dt/rho.
+    auto interior = [&]() {
+        constexpr int NR = TX + 2 * ORD - 1;
+        float rxx[NR], rxy[NR];
+        float bl[TX][ORD], bh[TX][ORD - 1 > 0 ? ORD - 1 : 1], by[TX][2 * ORD];
+        float vx0[TX], vy0[TX], dx0[TX], dy0[TX];
+#pragma unroll
+        for (int r = 0; r < NR; ++r) {
+            rxx[r] = ldf(sxx + (int64_t)(x0 - ORD + r) * P + y);
+            rxy[r] = ldf(sxy + (int64_t)(x0 - ORD + 1 + r) * P + y);
+        }
+#pragma unroll
+        for (int t = 0; t < TX; ++t) {
+            const int64_t i = (int64_t)(x0 + t) * P + y;
+#pragma unroll
+            for (int c = 0; c < ORD; ++c) bl[t][c] = ldf(sxy + i - c - 1);   // sxy[y-c-1]
+#pragma unroll
+            for (int c = 1; c < ORD; ++c) bh[t][c - 1] = ldf(sxy + i + c);   // sxy[y+c], c >= 1
+#pragma unroll
+            for (int c = 0; c < 2 * ORD; ++c) by[t][c] = ldf(syy + i - ORD + 1 + c);   // syy[y-ORD+1 .. y+ORD]
+            vx0[t] = p.v[0][i];
+            vy0[t] = p.v[1][i];
+            dx0[t] = ldg(p.dtr[0] + i);
+            dy0[t] = ldg(p.dtr[1] + i);
+        }
+#pragma unroll
+        for (int t = 0; t < TX; ++t) {
+            const int64_t i = (int64_t)(x0 + t) * P + y;
+            // rows x+c / x-c-1 of sxx and x+c+1 / x-c of sxy sit at t+ORD+c / t+ORD-1-c; sxy row x at t+ORD-1
+            float a = 0.f, b = 0.f;
+#pragma unroll
+            for (int c = 0; c < ORD; ++c) {
+                a = fmaf(p.cd[0][c], rxx[t + ORD + c] - rxx[t + ORD - 1 - c], a);
+                const float hi = c == 0 ? rxy[t + ORD - 1] : bh[t][c > 0 ? c - 1 : 0];
+                b = fmaf(p.cd[1][c], hi - bl[t][c], b);
+            }
+            const float fax = a + b, vxn = fmaf(fax, dx0[t], vx0[t]);
+            a = 0.f;
+            b = 0.f;
+#pragma unroll
+            for (int c = 0; c < ORD; ++c) {
+                a = fmaf(p.cd[0][c], rxy[t + ORD + c] - rxy[t + ORD - 1 - c], a);
+                b = fmaf(p.cd[1][c], by[t][ORD + c] - by[t][ORD - 1 - c], b);
+            }
+            const float fay = a + b, vyn = fmaf(fay, dy0[t], vy0[t]);
+            p.v[0][i] = vxn;
+            p.v[1][i] = vyn;
+            if (FEAT) {
+                p.feat[kFeatVx * p.grid_elems + i] = fax;
+                p.feat[kFeatVy * p.grid_elems + i] = fay;
+            }
+            const float v2 = fmaf(vxn, vxn, vyn * vyn);
+            bad |= !(v2 <= p.v2_threshold);
+            vmax = max(vmax, __float_as_uint(v2));
+        }
+    };
+
     auto sweep = [&](auto fast_tag) {
         constexpr bool FAST = decltype(fast_tag)::value;
         const int syl = FAST ? -1 : sy;
@@ -378,7 +438,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             }
         }
     };
-    if (fast) sweep(std::true_type{});
+    if (fast) interior();
     else if (live_col && x0 < nx) sweep(std::false_type{});
 
     // receivers: global thread g samples receiver g (syy is final for step k)
