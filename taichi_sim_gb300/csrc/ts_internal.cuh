@@ -168,12 +168,17 @@ inline int block_of_2d(const StepParams &p, int x, int y) {
 // consecutive nodes along x (measured on the 256^3 three-mechanism case
 // against 1, 2 and 4).
 constexpr int kBX3 = 32, kBY3 = 8, kTX3S = 4;
+// The 8 warps of a block cover kZW3 consecutive 32-node runs along z (the
+// contiguous axis) times 8 / kZW3 rows along y (2 measured best of 1, 2, 4,
+// 8 on the 256^3 case: longer contiguous runs per block, y-neighbours still
+// shared in L1).
+constexpr int kZW3 = 2, kZB3 = kBX3 * kZW3, kYB3 = kBY3 / kZW3;
 constexpr int velocity_tx_3d(int ord) { return ord == 2 ? 4 : 2; }
 
 // Flat index of the 3D velocity block that updates node (x, y, z).
 inline int block_of_3d(const StepParams &p, int x, int y, int z) {
-    const int gx = (p.nz + kBX3 - 1) / kBX3, gy = (p.ny + kBY3 - 1) / kBY3;
-    return ((x / p.tx) * gy + y / kBY3) * gx + z / kBX3;
+    const int gx = (p.nz + kZB3 - 1) / kZB3, gy = (p.ny + kYB3 - 1) / kYB3;
+    return ((x / p.tx) * gy + y / kYB3) * gx + z / kZB3;
 }
 
 }  // namespace ts

@@ -113,8 +113,8 @@ __device__ __forceinline__ float wderiv(const float (&w)[2 * ORD], const float *
 // from loads.
 template <int ORD, int ZM, int NS, typename I>
 __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_normal3d(const StepParams p) {
-    const int z = blockIdx.x * kBX3 + threadIdx.x;
-    const int y = blockIdx.y * kBY3 + threadIdx.y;
+    const int z = blockIdx.x * kZB3 + (threadIdx.y % kZW3) * kBX3 + threadIdx.x;
+    const int y = blockIdx.y * kYB3 + threadIdx.y / kZW3;
     const int x0 = blockIdx.z * kTX3S;
     if (y >= p.ny || z >= p.nz || x0 >= p.nx) return;
     const I X = (I)p.plane, Y = (I)p.pitch, yz = (I)y * Y + z, G = (I)p.grid_elems;
@@ -214,8 +214,8 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_normal3d(const
 // register windows.
 template <int ORD, int ZM, int NS, typename I>
 __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_shear3d(const StepParams p) {
-    const int z = blockIdx.x * kBX3 + threadIdx.x;
-    const int y = blockIdx.y * kBY3 + threadIdx.y;
+    const int z = blockIdx.x * kZB3 + (threadIdx.y % kZW3) * kBX3 + threadIdx.x;
+    const int y = blockIdx.y * kYB3 + threadIdx.y / kZW3;
     const int x0 = blockIdx.z * kTX3S;
     if (y >= p.ny || z >= p.nz || x0 >= p.nx) return;
     const I X = (I)p.plane, Y = (I)p.pitch, yz = (I)y * Y + z, G = (I)p.grid_elems;
@@ -362,8 +362,8 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_shear3d(const 
 // take one new plane per node, the y- and z-derivatives from loads.
 template <int ORD, typename I, int TX>
 __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(const StepParams p, const int j) {
-    const int z = blockIdx.x * kBX3 + threadIdx.x;
-    const int y = blockIdx.y * kBY3 + threadIdx.y;
+    const int z = blockIdx.x * kZB3 + (threadIdx.y % kZW3) * kBX3 + threadIdx.x;
+    const int y = blockIdx.y * kYB3 + threadIdx.y / kZW3;
     const int x0 = blockIdx.z * TX;
     const int tid = threadIdx.y * kBX3 + threadIdx.x;
     const int blk = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
@@ -526,7 +526,7 @@ void launch_idx(const StepParams &p, int zen_mode, int j, cudaStream_t st, int p
     const dim3 block(kBX3, kBY3);
     const bool three = p.zen.n == 3;
     if (parts & 1) {
-        const dim3 grid((p.nz + kBX3 - 1) / kBX3, (p.ny + kBY3 - 1) / kBY3, (p.nx + kTX3S - 1) / kTX3S);
+        const dim3 grid((p.nz + kZB3 - 1) / kZB3, (p.ny + kYB3 - 1) / kYB3, (p.nx + kTX3S - 1) / kTX3S);
         if (zen_mode == 0) {
             launch_pdl(k_normal3d<ORD, 0, 0, I>, grid, block, st, p);
             launch_pdl(k_shear3d<ORD, 0, 0, I>, grid, block, st, p);
@@ -545,7 +545,7 @@ void launch_idx(const StepParams &p, int zen_mode, int j, cudaStream_t st, int p
         }
     }
     if (parts & 2) {
-        const dim3 grid((p.nz + kBX3 - 1) / kBX3, (p.ny + kBY3 - 1) / kBY3, (p.nx + p.tx - 1) / p.tx);
+        const dim3 grid((p.nz + kZB3 - 1) / kZB3, (p.ny + kYB3 - 1) / kYB3, (p.nx + p.tx - 1) / p.tx);
         launch_pdl(k_velocity3d<ORD, I, velocity_tx_3d(ORD)>, grid, block, st, p, j);  // p.tx == velocity_tx_3d(ORD)
     }
 }
@@ -563,7 +563,7 @@ void launch_ord(const StepParams &p, int zen_mode, int j, cudaStream_t st, int p
 }  // namespace
 
 int blocks_3d(const StepParams &p) {
-    return ((p.nz + kBX3 - 1) / kBX3) * ((p.ny + kBY3 - 1) / kBY3) * ((p.nx + p.tx - 1) / p.tx);
+    return ((p.nz + kZB3 - 1) / kZB3) * ((p.ny + kYB3 - 1) / kYB3) * ((p.nx + p.tx - 1) / p.tx);
 }
 
 void launch_step_3d(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st, int parts) {
