@@ -42,6 +42,7 @@
 #include <cfloat>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/taichi_sim_gb300.h"
@@ -112,27 +113,34 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_velocity(const AdjStat
     const bool yvx = yvy && y >= ORD;
     const int sy = live_col ? strip_index(a.strip[1], y) : -1;
     const int q0 = __ldg(a.src_block_start + blk), q1 = __ldg(a.src_block_start + blk + 1);
+    // warps wholly in the interior (no source node in the block) sweep
+    // without per-node region, strip, bounds or source tests
+    const bool fast = interior_warp<ORD, TX>(a, y, x0, sy) && q0 == q1;
     pdl_wait();
-    if (live_col && x0 < nx) {
+    auto sweep = [&](auto fast_tag) {
+        constexpr bool FAST = decltype(fast_tag)::value;
+        const int syl = FAST ? -1 : sy;
         // dx~ adjoints rows [x-ORD, x+ORD-1] (vx), dvy/dx~ adjoints rows [x-ORD+1, x+ORD] (vy)
         float wdx[2 * ORD], wex[2 * ORD];
-        load_window<ORD>(wdx, a.dv[0], x0 - ORD, nx, P, y);
-        load_window<ORD>(wex, a.dv[2], x0 - ORD + 1, nx, P, y);
+        load_window<ORD, !FAST>(wdx, a.dv[0], x0 - ORD, nx, P, y);
+        load_window<ORD, !FAST>(wex, a.dv[2], x0 - ORD + 1, nx, P, y);
 #pragma unroll
         for (int t = 0; t < TX; ++t) {
             const int x = x0 + t;
-            if (x >= nx) break;
+            if (!FAST && x >= nx) break;
             const int64_t row = (int64_t)x * P, i = row + y;
-            const bool in_vy = yvy && x >= ORD - 1 && x < nx - ORD;
-            const bool in_vx = yvx && in_vy && x >= ORD;
-            const int sx = strip_index(a.strip[0], x);
-            const int64_t ix = (int64_t)sx * P + y, iy = (int64_t)x * a.strip[1].width + sy;
+            const bool in_vy = FAST || (yvy && x >= ORD - 1 && x < nx - ORD);
+            const bool in_vx = FAST || (yvx && in_vy && x >= ORD);
+            const int sx = FAST ? -1 : strip_index(a.strip[0], x);
+            const int64_t ix = (int64_t)sx * P + y, iy = (int64_t)x * a.strip[1].width + syl;
             // ---- loads ----
             float dey[2 * ORD], dvy[2 * ORD];
 #pragma unroll
-            for (int c = 0; c < 2 * ORD; ++c) dey[c] = ld_y(a.dv[3], row, y - ORD + c, ny);      // y-ORD .. y+ORD-1
+            for (int c = 0; c < 2 * ORD; ++c)   // y-ORD .. y+ORD-1
+                dey[c] = FAST ? __ldca(a.dv[3] + row + y - ORD + c) : ld_y(a.dv[3], row, y - ORD + c, ny);
 #pragma unroll
-            for (int c = 0; c < 2 * ORD; ++c) dvy[c] = ld_y(a.dv[1], row, y - ORD + 1 + c, ny);  // y-ORD+1 .. y+ORD
+            for (int c = 0; c < 2 * ORD; ++c)   // y-ORD+1 .. y+ORD
+                dvy[c] = FAST ? __ldca(a.dv[1] + row + y - ORD + 1 + c) : ld_y(a.dv[1], row, y - ORD + 1 + c, ny);
             float avx = a.avx[i], avy = a.avy[i];
             float bx = 0.f, by = 0.f, fax = 0.f, fay = 0.f, gbx = 0.f, gby = 0.f;
             float pxa = 0.f, pxb = 0.f, pya = 0.f, pyb = 0.f;
@@ -141,13 +149,13 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_velocity(const AdjStat
                 fax = __ldca(rec + kFeatVx * G + i);
                 gbx = a.gBx[i];
                 if (sx >= 0) pxa = a.apsi[4][ix];
-                if (sy >= 0) pxb = a.apsi[6][iy];
+                if (syl >= 0) pxb = a.apsi[6][iy];
             }
             if (in_vy) {
                 by = __ldg(a.By + i);
                 fay = __ldca(rec + kFeatVy * G + i);
                 if (sx >= 0) pya = a.apsi[5][ix];
-                if (sy >= 0) pyb = a.apsi[7][iy];
+                if (syl >= 0) pyb = a.apsi[7][iy];
             }
             // ---- transposed stress stencils of the next step ----
             float gx = 0.f, gy = 0.f;
@@ -171,16 +179,18 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_velocity(const AdjStat
                     d0 = cpml_adj(ab, pxa, a.tab_f[0][x]);
                     a.apsi[4][ix] = pxa;
                 }
-                if (sy >= 0) {
+                if (syl >= 0) {
                     d1 = cpml_adj(ab, pxb, a.tab_f[1][y]);
                     a.apsi[6][iy] = pxb;
                 }
             }
             float gsrc = 0.f;
-            for (int q = q0; q < q1; ++q) {
-                const Source s = a.src[q];
-                if (s.cell == i && k < a.src_rows)
-                    gsrc = fmaf(avy, __ldg(a.src_tab + (int64_t)k * a.src_ncol + s.col), gsrc);
+            if constexpr (!FAST) {
+                for (int q = q0; q < q1; ++q) {
+                    const Source s = a.src[q];
+                    if (s.cell == i && k < a.src_rows)
+                        gsrc = fmaf(avy, __ldg(a.src_tab + (int64_t)k * a.src_ncol + s.col), gsrc);
+                }
             }
             if (in_vy) {
                 const float ab = by * avy;
@@ -191,7 +201,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_velocity(const AdjStat
                     d2 = cpml_adj(ab, pya, a.tab_h[0][x]);
                     a.apsi[5][ix] = pya;
                 }
-                if (sy >= 0) {
+                if (syl >= 0) {
                     d3 = cpml_adj(ab, pyb, a.tab_h[1][y]);
                     a.apsi[7][iy] = pyb;
                 }
@@ -207,11 +217,13 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_velocity(const AdjStat
             a.avx[i] = in_vx ? avx : 0.f;
             a.avy[i] = in_vy ? avy : 0.f;
             if (t + 1 < TX) {
-                shift_window<ORD>(wdx, a.dv[0], x + ORD, nx, P, y);
-                shift_window<ORD>(wex, a.dv[2], x + ORD + 1, nx, P, y);
+                shift_window<ORD, !FAST>(wdx, a.dv[0], x + ORD, nx, P, y);
+                shift_window<ORD, !FAST>(wex, a.dv[2], x + ORD + 1, nx, P, y);
             }
         }
-    }
+    };
+    if (fast) sweep(std::true_type{});
+    else if (live_col && x0 < nx) sweep(std::false_type{});
     // residuals of step k into syy^bar: global thread g injects receiver g
     const int g = blk * (kBX2 * kBY2) + tid;
     if (g < a.n_rec && k >= __ldg(a.rec_first + g)) {
@@ -226,6 +238,8 @@ template <int ORD, int ZM, int NS, int TX, int MINB>
 __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_stress(const AdjState a, const float *rec) {
     const int y = blockIdx.x * kBX2 + threadIdx.x;
     const int x0 = (blockIdx.y * kBY2 + threadIdx.y) * TX;
+    const int sy = y < a.ny ? strip_index(a.strip[1], y) : -1;
+    const bool fast = interior_warp<ORD, TX>(a, y, x0, sy);
     if (y >= a.ny || x0 >= a.nx) return;
     const int P = a.P, nx = a.nx, ny = a.ny;
     const int64_t G = a.G;
@@ -233,141 +247,148 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_stress(const AdjState 
     constexpr int R = NS > 0 ? NS : 1;
     const bool yn = y >= ORD && y < ny - ORD + 1;
     const bool ys = y >= ORD - 1 && y < ny - ORD;
-    const int sy = strip_index(a.strip[1], y);
     pdl_wait();
-    // dsxx/dx~ adjoints rows [x-ORD+1, x+ORD], dsxy/dx~ adjoints rows [x-ORD, x+ORD-1]
-    float wax[2 * ORD], way[2 * ORD];
-    load_window<ORD>(wax, a.ds[0], x0 - ORD + 1, nx, P, y);
-    load_window<ORD>(way, a.ds[2], x0 - ORD, nx, P, y);
+    auto sweep = [&](auto fast_tag) {
+        constexpr bool FAST = decltype(fast_tag)::value;
+        const int syl = FAST ? -1 : sy;
+        // dsxx/dx~ adjoints rows [x-ORD+1, x+ORD], dsxy/dx~ adjoints rows [x-ORD, x+ORD-1]
+        float wax[2 * ORD], way[2 * ORD];
+        load_window<ORD, !FAST>(wax, a.ds[0], x0 - ORD + 1, nx, P, y);
+        load_window<ORD, !FAST>(way, a.ds[2], x0 - ORD, nx, P, y);
 #pragma unroll
-    for (int t = 0; t < TX; ++t) {
-        const int x = x0 + t;
-        if (x >= nx) break;
-        const int64_t row = (int64_t)x * P, i = row + y;
-        const bool in_n = yn && x >= ORD - 1 && x < nx - ORD;
-        const bool in_s = ys && x >= ORD && x < nx - ORD + 1;
-        const int sx = strip_index(a.strip[0], x);
-        const int64_t ix = (int64_t)sx * P + y, iy = (int64_t)x * a.strip[1].width + sy;
-        // ---- loads ----
-        float axy[2 * ORD], ayy[2 * ORD];
+        for (int t = 0; t < TX; ++t) {
+            const int x = x0 + t;
+            if (!FAST && x >= nx) break;
+            const int64_t row = (int64_t)x * P, i = row + y;
+            const bool in_n = FAST || (yn && x >= ORD - 1 && x < nx - ORD);
+            const bool in_s = FAST || (ys && x >= ORD && x < nx - ORD + 1);
+            const int sx = FAST ? -1 : strip_index(a.strip[0], x);
+            const int64_t ix = (int64_t)sx * P + y, iy = (int64_t)x * a.strip[1].width + syl;
+            // ---- loads ----
+            float axy[2 * ORD], ayy[2 * ORD];
 #pragma unroll
-        for (int c = 0; c < 2 * ORD; ++c) axy[c] = ld_y(a.ds[1], row, y - ORD + 1 + c, ny);  // y-ORD+1 .. y+ORD
+            for (int c = 0; c < 2 * ORD; ++c)   // y-ORD+1 .. y+ORD
+                axy[c] = FAST ? __ldca(a.ds[1] + row + y - ORD + 1 + c) : ld_y(a.ds[1], row, y - ORD + 1 + c, ny);
 #pragma unroll
-        for (int c = 0; c < 2 * ORD; ++c) ayy[c] = ld_y(a.ds[3], row, y - ORD + c, ny);      // y-ORD .. y+ORD-1
-        float sxx = a.asxx[i], syy = a.asyy[i], sxy = a.asxy[i];
-        float L = 0.f, M = 0.f, Ms = 0.f, gp = 1.f, gs = 1.f, fl = 0.f, fmx = 0.f, fmy = 0.f, fsh = 0.f;
-        float gl = 0.f, gm = 0.f, gms = 0.f, pn0 = 0.f, pn1 = 0.f, ps0 = 0.f, ps1 = 0.f;
-        float rxx[R], ryy[R], rxy[R];
-        if (in_n) {
-            L = __ldg(a.L + i);
-            M = __ldg(a.M + i);
-            if (ZM == 2) gp = __ldg(a.gp + i);
-            fl = __ldca(rec + kFeatLam * G + i);
-            fmx = __ldca(rec + kFeatMuX * G + i);
-            fmy = __ldca(rec + kFeatMuY * G + i);
-            gl = a.gL[i];
-            gm = a.gM[i];
-            if (sx >= 0) pn0 = a.apsi[0][ix];
-            if (sy >= 0) pn1 = a.apsi[2][iy];
-            if (ZM != 0) {
+            for (int c = 0; c < 2 * ORD; ++c)   // y-ORD .. y+ORD-1
+                ayy[c] = FAST ? __ldca(a.ds[3] + row + y - ORD + c) : ld_y(a.ds[3], row, y - ORD + c, ny);
+            float sxx = a.asxx[i], syy = a.asyy[i], sxy = a.asxy[i];
+            float L = 0.f, M = 0.f, Ms = 0.f, gp = 1.f, gs = 1.f, fl = 0.f, fmx = 0.f, fmy = 0.f, fsh = 0.f;
+            float gl = 0.f, gm = 0.f, gms = 0.f, pn0 = 0.f, pn1 = 0.f, ps0 = 0.f, ps1 = 0.f;
+            float rxx[R], ryy[R], rxy[R];
+            if (in_n) {
+                L = __ldg(a.L + i);
+                M = __ldg(a.M + i);
+                if (ZM == 2) gp = __ldg(a.gp + i);
+                fl = __ldca(rec + kFeatLam * G + i);
+                fmx = __ldca(rec + kFeatMuX * G + i);
+                fmy = __ldca(rec + kFeatMuY * G + i);
+                gl = a.gL[i];
+                gm = a.gM[i];
+                if (sx >= 0) pn0 = a.apsi[0][ix];
+                if (syl >= 0) pn1 = a.apsi[2][iy];
+                if (ZM != 0) {
 #pragma unroll
-                for (int l = 0; l < R; ++l)
-                    if (l < n_mech) {
-                        rxx[l] = a.ar[0][l * G + i];
-                        ryy[l] = a.ar[1][l * G + i];
-                    }
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) {
+                            rxx[l] = a.ar[0][l * G + i];
+                            ryy[l] = a.ar[1][l * G + i];
+                        }
+                }
+            }
+            if (in_s) {
+                Ms = __ldg(a.Ms + i);
+                fsh = __ldca(rec + kFeatShear * G + i);
+                gms = a.gMs[i];
+                if (sx >= 0) ps0 = a.apsi[1][ix];
+                if (syl >= 0) ps1 = a.apsi[3][iy];
+                if (ZM != 0) {
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) rxy[l] = a.ar[2][l * G + i];
+                }
+            }
+            if (ZM == 2 && (in_n || in_s)) gs = __ldg(a.gs + i);
+            // ---- transposed velocity stencils of this step ----
+#pragma unroll
+            for (int c = 0; c < ORD; ++c) {
+                sxx = fmaf(a.cd[0][c], wax[ORD - 1 - c] - wax[ORD + c], sxx);
+                sxy = fmaf(a.cd[1][c], axy[ORD - 1 - c] - axy[ORD + c], sxy);
+                sxy = fmaf(a.cd[0][c], way[ORD - 1 - c] - way[ORD + c], sxy);
+                syy = fmaf(a.cd[1][c], ayy[ORD - 1 - c] - ayy[ORD + c], syy);
+            }
+            a.asxx[i] = sxx;
+            a.asyy[i] = syy;
+            a.asxy[i] = sxy;
+            // ---- stress update of this step, transposed ----
+            float o0 = 0.f, o1 = 0.f, o2 = 0.f, o3 = 0.f;
+            if (in_n) {
+                a.gL[i] = fmaf(sxx + syy, fl, gl);
+                a.gM[i] = fmaf(sxx, fmx, fmaf(syy, fmy, gm));
+                const float L2M = fmaf(2.f, M, L);
+                float bx = fmaf(L2M, sxx, L * syy), by = fmaf(L, sxx, L2M * syy);
+                if (ZM != 0) {
+                    const float Sx = 0.5f * (L + M) * (sxx + syy), Sy = M * (sxx - syy);
+                    float drx = 0.f, dry = 0.f;
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) {
+                            const float qx = rxx[l] + Sx, qy = ryy[l] + Sy;
+                            a.ar[0][l * G + i] = fmaf(a.zen.Ap[l], qx, Sx);
+                            a.ar[1][l * G + i] = fmaf(a.zen.As[l], qy, Sy);
+                            drx = fmaf(a.zen.Bp[l] * gp, qx, drx);
+                            dry = fmaf(a.zen.Bs[l] * gs, qy, dry);
+                        }
+                    bx += fmaf(0.5f, dry, drx);
+                    by += fmaf(-0.5f, dry, drx);
+                }
+                o0 = bx;
+                o1 = by;
+                if (sx >= 0) {
+                    o0 = cpml_adj(bx, pn0, a.tab_h[0][x]);
+                    a.apsi[0][ix] = pn0;
+                }
+                if (syl >= 0) {
+                    o1 = cpml_adj(by, pn1, a.tab_f[1][y]);
+                    a.apsi[2][iy] = pn1;
+                }
+            }
+            if (in_s) {
+                a.gMs[i] = fmaf(sxy, fsh, gms);
+                float eb = Ms * sxy;
+                if (ZM != 0) {
+                    const float S = 0.5f * Ms * sxy;
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) {
+                            const float q = rxy[l] + S;
+                            a.ar[2][l * G + i] = fmaf(a.zen.As[l], q, S);
+                            eb = fmaf(a.zen.Bs[l] * gs, q, eb);
+                        }
+                }
+                o2 = eb;
+                o3 = eb;
+                if (sx >= 0) {
+                    o2 = cpml_adj(eb, ps0, a.tab_f[0][x]);
+                    a.apsi[1][ix] = ps0;
+                }
+                if (syl >= 0) {
+                    o3 = cpml_adj(eb, ps1, a.tab_h[1][y]);
+                    a.apsi[3][iy] = ps1;
+                }
+            }
+            a.dv[0][i] = o0;
+            a.dv[1][i] = o1;
+            a.dv[2][i] = o2;
+            a.dv[3][i] = o3;
+            if (t + 1 < TX) {
+                shift_window<ORD, !FAST>(wax, a.ds[0], x + ORD + 1, nx, P, y);
+                shift_window<ORD, !FAST>(way, a.ds[2], x + ORD, nx, P, y);
             }
         }
-        if (in_s) {
-            Ms = __ldg(a.Ms + i);
-            fsh = __ldca(rec + kFeatShear * G + i);
-            gms = a.gMs[i];
-            if (sx >= 0) ps0 = a.apsi[1][ix];
-            if (sy >= 0) ps1 = a.apsi[3][iy];
-            if (ZM != 0) {
-#pragma unroll
-                for (int l = 0; l < R; ++l)
-                    if (l < n_mech) rxy[l] = a.ar[2][l * G + i];
-            }
-        }
-        if (ZM == 2 && (in_n || in_s)) gs = __ldg(a.gs + i);
-        // ---- transposed velocity stencils of this step ----
-#pragma unroll
-        for (int c = 0; c < ORD; ++c) {
-            sxx = fmaf(a.cd[0][c], wax[ORD - 1 - c] - wax[ORD + c], sxx);
-            sxy = fmaf(a.cd[1][c], axy[ORD - 1 - c] - axy[ORD + c], sxy);
-            sxy = fmaf(a.cd[0][c], way[ORD - 1 - c] - way[ORD + c], sxy);
-            syy = fmaf(a.cd[1][c], ayy[ORD - 1 - c] - ayy[ORD + c], syy);
-        }
-        a.asxx[i] = sxx;
-        a.asyy[i] = syy;
-        a.asxy[i] = sxy;
-        // ---- stress update of this step, transposed ----
-        float o0 = 0.f, o1 = 0.f, o2 = 0.f, o3 = 0.f;
-        if (in_n) {
-            a.gL[i] = fmaf(sxx + syy, fl, gl);
-            a.gM[i] = fmaf(sxx, fmx, fmaf(syy, fmy, gm));
-            const float L2M = fmaf(2.f, M, L);
-            float bx = fmaf(L2M, sxx, L * syy), by = fmaf(L, sxx, L2M * syy);
-            if (ZM != 0) {
-                const float Sx = 0.5f * (L + M) * (sxx + syy), Sy = M * (sxx - syy);
-                float drx = 0.f, dry = 0.f;
-#pragma unroll
-                for (int l = 0; l < R; ++l)
-                    if (l < n_mech) {
-                        const float qx = rxx[l] + Sx, qy = ryy[l] + Sy;
-                        a.ar[0][l * G + i] = fmaf(a.zen.Ap[l], qx, Sx);
-                        a.ar[1][l * G + i] = fmaf(a.zen.As[l], qy, Sy);
-                        drx = fmaf(a.zen.Bp[l] * gp, qx, drx);
-                        dry = fmaf(a.zen.Bs[l] * gs, qy, dry);
-                    }
-                bx += fmaf(0.5f, dry, drx);
-                by += fmaf(-0.5f, dry, drx);
-            }
-            o0 = bx;
-            o1 = by;
-            if (sx >= 0) {
-                o0 = cpml_adj(bx, pn0, a.tab_h[0][x]);
-                a.apsi[0][ix] = pn0;
-            }
-            if (sy >= 0) {
-                o1 = cpml_adj(by, pn1, a.tab_f[1][y]);
-                a.apsi[2][iy] = pn1;
-            }
-        }
-        if (in_s) {
-            a.gMs[i] = fmaf(sxy, fsh, gms);
-            float eb = Ms * sxy;
-            if (ZM != 0) {
-                const float S = 0.5f * Ms * sxy;
-#pragma unroll
-                for (int l = 0; l < R; ++l)
-                    if (l < n_mech) {
-                        const float q = rxy[l] + S;
-                        a.ar[2][l * G + i] = fmaf(a.zen.As[l], q, S);
-                        eb = fmaf(a.zen.Bs[l] * gs, q, eb);
-                    }
-            }
-            o2 = eb;
-            o3 = eb;
-            if (sx >= 0) {
-                o2 = cpml_adj(eb, ps0, a.tab_f[0][x]);
-                a.apsi[1][ix] = ps0;
-            }
-            if (sy >= 0) {
-                o3 = cpml_adj(eb, ps1, a.tab_h[1][y]);
-                a.apsi[3][iy] = ps1;
-            }
-        }
-        a.dv[0][i] = o0;
-        a.dv[1][i] = o1;
-        a.dv[2][i] = o2;
-        a.dv[3][i] = o3;
-        if (t + 1 < TX) {
-            shift_window<ORD>(wax, a.ds[0], x + ORD + 1, nx, P, y);
-            shift_window<ORD>(way, a.ds[2], x + ORD, nx, P, y);
-        }
-    }
+    };
+    if (fast) sweep(std::true_type{});
+    else sweep(std::false_type{});
     pdl_trigger();
 }
 

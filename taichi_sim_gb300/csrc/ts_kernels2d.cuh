@@ -79,8 +79,8 @@ __device__ __forceinline__ void shift_window(float (&w)[2 * ORD], const float *f
 // the update regions of both kernels, outside the CPML strips, window rows
 // inside the grid) sweeps without per-node region, strip or bounds tests.
 // Evaluated by all 32 lanes before any of them returns.
-template <int ORD, int TX>
-__device__ __forceinline__ bool interior_warp(const StepParams &p, int y, int x0, int sy) {
+template <int ORD, int TX, typename Params>
+__device__ __forceinline__ bool interior_warp(const Params &p, int y, int x0, int sy) {
     const bool lane = y < p.ny && sy < 0 && y >= ORD && y < p.ny - ORD && x0 >= ORD && x0 >= p.strip[0].lo &&
                       x0 + TX + ORD <= p.nx && x0 + TX <= p.strip[0].hi;
     return __all_sync(0xffffffffu, lane);
