@@ -229,10 +229,14 @@ const char *ts_batch_last_error(void);
  * the returned gradients back.  With per-cell Q (desc g_p/g_s) the scales
  * g_p, g_s [nx][pitch] are passed too.
  *
- *   ts_adj_create      checkpoint_every = 0 keeps the 8 per-node features of
- *                      every step (8 * nx * pitch * n_steps floats);
+ *   ts_adj_create      checkpoint_every = 0 keeps the 6 per-node features of
+ *                      every step (6 * nx * pitch * n_steps floats);
  *                      K > 0 keeps the forward state every K steps and
- *                      recomputes each K-step segment in the backward pass
+ *                      recomputes each K-step segment in the backward pass,
+ *                      except the trailing segments whose features the
+ *                      forward pass records (1 by default)
+ *   ts_adj_set_record_segments  number of those trailing segments (memory:
+ *                      6 * nx * pitch * K floats each; checkpointed handles)
  *   ts_adj_set_sources replaces the source table (a new shot)
  *   ts_adj_forward     traces[n_steps][n_rec] (device), as ts_run records them
  *   ts_adj_backward    given residual[n_steps][n_rec] = dJ/dtraces (device),
@@ -258,6 +262,7 @@ typedef struct ts_adj_grads {
 
 int ts_adj_create(const ts_desc *desc, int32_t checkpoint_every, ts_adj **out);
 int ts_adj_pitch(const ts_adj *a, int32_t *pitch);
+int ts_adj_set_record_segments(ts_adj *a, int32_t segments);
 int ts_adj_set_sources(ts_adj *a, const float *source_term);   /* host, [src_rows][src_cols] */
 int ts_adj_forward(ts_adj *a, const ts_adj_coefs *coefs, float *traces, void *stream);
 int ts_adj_backward(ts_adj *a, const float *residual, const ts_adj_grads *grads, void *stream);

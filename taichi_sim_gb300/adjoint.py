@@ -15,9 +15,11 @@ differentiable without changing it:
   and, in ``backward``, the time-reversed adjoint (``ts_adj_backward``) with
   the incoming trace gradient as the adjoint source.  The forward keeps the
   state every ``checkpoint_every`` steps (default ceil(sqrt(n_steps)),
-  revolve-style) and recomputes each segment before its adjoint sweep;
-  ``checkpoint_every=0`` keeps every step's features instead (no
-  recomputation, 8 floats per node and step).
+  revolve-style) and recomputes each segment before its adjoint sweep,
+  except the ``record_segments`` trailing segments (default 1) whose
+  features the forward pass records as it goes; ``checkpoint_every=0``
+  keeps every step's features instead (no recomputation, 6 floats per node
+  and step).
 
 Shots share one problem: :meth:`AdjointProblem.set_source_term` swaps the
 source table, and gradients of several shots add up in ``.grad`` as usual.
@@ -48,6 +50,7 @@ def _bind(lib):
     sigs = {
         "ts_adj_create": ([ctypes.POINTER(engine.TsDesc), ctypes.c_int32, ctypes.POINTER(_P)], ctypes.c_int),
         "ts_adj_pitch": ([_P, ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
+        "ts_adj_set_record_segments": ([_P, ctypes.c_int32], ctypes.c_int),
         "ts_adj_set_sources": ([_P, _f], ctypes.c_int),
         "ts_adj_forward": ([_P, ctypes.POINTER(AdjCoefs), _P, _P], ctypes.c_int),
         "ts_adj_backward": ([_P, _P, ctypes.POINTER(AdjGrads), _P], ctypes.c_int),
@@ -91,10 +94,13 @@ class AdjointProblem:
     whose material is a differentiable input.
 
     ``checkpoint_every``: None = ceil(sqrt(n_steps)); 0 = keep every step's
-    features (8 floats per node and step of device memory).
+    features (6 floats per node and step of device memory).
+    ``record_segments``: trailing segments of a checkpointed run that the
+    forward pass records, so that the backward pass does not recompute
+    them (6 floats per node and step of each; at least 1).
     """
 
-    def __init__(self, sim, checkpoint_every=None, visco=None, device=None):
+    def __init__(self, sim, checkpoint_every=None, visco=None, device=None, record_segments=1):
         if sim._dims != 2:
             raise ValueError("the adjoint covers 2D models")
         self._lib = _bind(engine.load_library())
@@ -125,6 +131,11 @@ class AdjointProblem:
             _check(self._lib, self._lib.ts_adj_create(ctypes.byref(desc), self.checkpoint_every, ctypes.byref(h)),
                    "ts_adj_create")
         self._h = h
+        self.record_segments = int(record_segments)
+        if self.checkpoint_every > 0 and self.record_segments != 1:
+            n_seg = -(-self.n_rows // self.checkpoint_every)
+            _check(self._lib, self._lib.ts_adj_set_record_segments(self._h, min(self.record_segments, n_seg)),
+                   "ts_adj_set_record_segments")
         p = ctypes.c_int32()
         _check(self._lib, self._lib.ts_adj_pitch(self._h, ctypes.byref(p)), "ts_adj_pitch")
         self.pitch = p.value

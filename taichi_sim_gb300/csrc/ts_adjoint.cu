@@ -22,7 +22,8 @@
 // (GB300's HBM holds a 512 x 1024 x 3000-step record in 38 GB); otherwise
 // the forward state is checkpointed every K steps and each K-step segment
 // is recomputed, recording, before its adjoint sweep (revolve-style,
-// K ~ sqrt(steps)).
+// K ~ sqrt(steps)); the last segment records during the forward pass, since
+// its sweep comes first.
 //
 // Adjoint step n, from the adjoints of the state after step n, as two
 // launches (same block shape and x-marching as the forward):
@@ -405,12 +406,11 @@ void launch_adj_shape(const AdjState &a, int zm, const float *rec, int k, cudaSt
 }
 
 // Block shape of the adjoint kernels: one node per thread, and a register
-// budget that keeps 4 (ord 2) or 3 blocks resident per SM without spills
-// (measured on the 512 x 1024 three-mechanism case: about 1.3x the speed of
-// two nodes per thread with an unconstrained budget).
+// budget that keeps 3 blocks resident per SM (measured on the 512 x 1024
+// three-mechanism case against 4 blocks and two nodes per thread).
 template <int ORD>
 void launch_adj_ord(const AdjState &a, int zm, const float *rec, int k, cudaStream_t st) {
-    launch_adj_shape<ORD, kAdjTx, ORD == 2 ? 4 : 3>(a, zm, rec, k, st);
+    launch_adj_shape<ORD, kAdjTx, 3>(a, zm, rec, k, st);
 }
 
 void launch_adjoint_step(const AdjState &a, int ord, int zm, const float *rec, int k, cudaStream_t st) {
@@ -459,6 +459,8 @@ struct ts_adj {
     float *src_tab = nullptr;
     int *scalars = nullptr;     // first_bad, step_base
     int forward_done = 0;
+    int rec_segs = 1;           // trailing segments the forward pass records (checkpointed runs)
+    int tail_recorded = 0;      // the record holds those segments, written by the forward pass
 
     template <typename T>
     int alloc(T **ptr, size_t n) {
@@ -485,9 +487,12 @@ struct ts_adj {
         for (int k = k0; k < k1; ++k) forward_step(k, record_of(k - k0), st);
         return TS_OK;
     }
-    void sweep(int s, cudaStream_t st) {
+    // first step of the trailing segments the forward pass records
+    int tail0() const { return std::max(0, n_ckpt - rec_segs) * ckpt; }
+    // sweep of segment s; its record starts at step `base` of the record buffer
+    void sweep(int s, int base, cudaStream_t st) {
         const int k0 = s * ckpt, k1 = std::min(rows, k0 + ckpt);
-        for (int k = k1 - 1; k >= k0; --k) adjoint_step(k, record_of(k - k0), st);
+        for (int k = k1 - 1; k >= k0; --k) adjoint_step(k, record_of(k - base), st);
     }
     void forward_step(int k, float *rec, cudaStream_t st) {
         sp.feat = rec;
@@ -766,6 +771,32 @@ int ts_adj_read_field(ts_adj *a, int32_t what, void *host_dst, size_t bytes) {
     return TS_OK;
 }
 
+int ts_adj_set_record_segments(ts_adj *a, int32_t segments) {
+    if (!a) return afail(TS_E_ARG, "null handle");
+    if (a->ckpt <= 0) return afail(TS_E_STATE, "every step is recorded already (checkpoint_every = 0)");
+    if (segments < 1 || segments > a->n_ckpt) return afail(TS_E_ARG, "segments must be in [1, number of segments]");
+    if (segments == a->rec_segs) return TS_OK;
+    cudaSetDevice(a->device);
+    cudaDeviceSynchronize();  // the record may be in use by enqueued work
+    float *fresh = nullptr;
+    const size_t n = (size_t)a->ckpt * segments * kFeat * a->G;
+    if (cudaMalloc(&fresh, n * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError();
+        return afail(TS_E_NOMEM, "record of the trailing segments");
+    }
+    for (auto &d : a->allocs)
+        if (d == a->record) {
+            cudaFree(d);
+            d = fresh;
+        }
+    a->record = fresh;
+    a->n_record_steps = a->ckpt * segments;
+    a->rec_segs = segments;
+    a->tail_recorded = 0;
+    a->forward_done = 0;   // the next backward needs a forward that fills the new record
+    return TS_OK;
+}
+
 int ts_adj_launch_count(const ts_adj *a, int64_t *launches) {
     if (!a || !launches) return afail(TS_E_ARG, "null argument");
     *launches = a->launches;
@@ -795,8 +826,13 @@ int ts_adj_forward(ts_adj *a, const ts_adj_coefs *c, float *traces, void *stream
         if (a->ckpt > 0 && k % a->ckpt == 0 &&
             (rc = a->copy_state(a->checkpoints + (int64_t)(k / a->ckpt) * a->state_floats, true, st)))
             return rc;
-        a->forward_step(k, a->ckpt > 0 ? nullptr : a->record_of(k), st);
+        // The trailing segments record as they go: their adjoint sweeps come
+        // first and need no recomputation.
+        const int t0 = a->tail0();
+        float *rec = a->ckpt <= 0 ? a->record_of(k) : (k >= t0 ? a->record_of(k - t0) : nullptr);
+        a->forward_step(k, rec, st);
     }
+    a->tail_recorded = a->ckpt > 0;
     a->sp.n_rec = 0;
     a->sp.traces = nullptr;
     const cudaError_t e = cudaGetLastError();
@@ -827,9 +863,15 @@ int ts_adj_backward(ts_adj *a, const float *residual, const ts_adj_grads *g, voi
     } else {
         // (recomputing segment s-1 on a second stream while segment s is swept
         // was measured no faster: both passes share the same memory system)
+        const int first_tail = a->n_ckpt - std::min(a->rec_segs, a->n_ckpt);
         for (int s = a->n_ckpt - 1; s >= 0; --s) {
-            if ((rc = a->recompute(s, st))) return rc;
-            a->sweep(s, st);
+            if (s >= first_tail && a->tail_recorded) {
+                a->sweep(s, a->tail0(), st);
+            } else {
+                if ((rc = a->recompute(s, st))) return rc;
+                a->tail_recorded = 0;   // the recomputed segment overwrote the start of the record
+                a->sweep(s, s * a->ckpt, st);
+            }
         }
     }
     const cudaError_t e = cudaGetLastError();

@@ -20,12 +20,11 @@ void launch_feat_mb(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
     launch_pdl(k_velocity2d<ORD, 1, TX, true, MINB>, grid, block, st, p, j);
 }
 
-// Register budget: 4 (ord 2) or 3 (ord 3, 4) resident blocks per SM where
-// that spills nothing (ord 2: about 10 % faster than an unconstrained
-// budget); ord 5, 6 keep the compiler's choice (0: no constraint).
+// Register budget: 3 resident blocks per SM (ord 2 to 4), which spills
+// nothing; ord 5, 6 keep the compiler's choice (0: no constraint).
 template <int ORD>
 void launch_feat(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
-    launch_feat_mb<ORD, ORD == 2 ? 4 : (ORD <= 4 ? 3 : 0)>(p, zen_mode, j, st);
+    launch_feat_mb<ORD, ORD <= 4 ? 3 : 0>(p, zen_mode, j, st);
 }
 
 }  // namespace

@@ -101,20 +101,40 @@ def test_gradient_matches_central_differences():
 
 
 def test_checkpointing_matches_store_all():
-    """Recomputing K-step segments from checkpoints gives the gradient of
+    """Recomputing K-step segments from checkpoints (with 1, 3 or all
+    trailing segments recorded by the forward pass) gives the gradient of
     keeping every step's features."""
     true, start = _problem_pair(64, 64, 150)
     grads = []
     with AdjointProblem(true, checkpoint_every=0) as pt, torch.no_grad():
         obs = pt.traces(*pt.material()).clone()
-    for ckpt in (0, 7, 13, None):
-        with AdjointProblem(start, checkpoint_every=ckpt) as prob:
+    # (checkpoint interval, trailing segments recorded by the forward pass)
+    for ckpt, segs in ((0, 1), (7, 1), (13, 1), (None, 1), (13, 3), (7, 50)):
+        with AdjointProblem(start, checkpoint_every=ckpt, record_segments=segs) as prob:
             m = [t.clone().requires_grad_(True) for t in prob.material()]
             l2_misfit(prob.traces(*m), obs).backward()
             grads.append([t.grad.cpu().numpy() for t in m])
     for g in grads[1:]:
         for a, b in zip(g, grads[0]):
             assert rel_l2(a, b) <= 1e-6
+
+
+def test_repeated_backward_recomputes_the_last_segment():
+    """The forward pass records the last segment for the first backward; a
+    second backward of the same forward recomputes it from its checkpoint
+    and gives the same coefficient gradients bit for bit."""
+    true, start = _problem_pair(64, 64, 150)
+    with AdjointProblem(true, checkpoint_every=0) as pt, torch.no_grad():
+        obs = pt.traces(*pt.material()).clone()
+    with AdjointProblem(start, checkpoint_every=13) as prob:
+        coefs = prob.node_coefficients(*prob.material())
+        traces, token = prob.forward_raw(*coefs)
+        residual = (traces - obs.to(traces.device)).contiguous()
+        first = [g.clone() for g in prob.backward_raw(residual, token)]
+        second = prob.backward_raw(residual, token)
+        for a, b in zip(first, second):
+            assert torch.equal(a, b)
+        assert max(float(a.abs().max()) for a in first) > 0
 
 
 def test_shot_gradients_add_up():
