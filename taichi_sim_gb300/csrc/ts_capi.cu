@@ -32,6 +32,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/taichi_sim_gb300.h"
@@ -148,6 +149,54 @@ struct ts_sim {
 };
 
 using ts::Axis;
+
+// Coefficient palette of a 3D model: the distinct tuples of the stress
+// kernels' per-node coefficients (compared bit for bit) and each node's
+// 16-bit index into them.  Models built from a few materials (layers, inclusions) have a few
+// dozen tuples; false when there are more than 65536 (the arrays are used).
+bool build_palette_3d(const std::vector<float> *const (&c)[7], std::vector<uint16_t> &idx,
+                      std::vector<ts::Pal3> &table) {
+    struct Key {
+        uint32_t w[7];
+        bool operator==(const Key &o) const { return std::memcmp(w, o.w, sizeof w) == 0; }
+    };
+    struct Hash {
+        size_t operator()(const Key &k) const {
+            uint64_t h = 1469598103934665603ull;   // FNV-1a over the words
+            for (uint32_t v : k.w) h = (h ^ v) * 1099511628211ull;
+            return (size_t)h;
+        }
+    };
+    const size_t n = c[0]->size();
+    idx.assign(n, 0);
+    table.clear();
+    std::unordered_map<Key, uint16_t, Hash> ids;
+    Key last{};
+    int last_id = -1;
+    for (size_t i = 0; i < n; ++i) {
+        Key k;
+        for (int f = 0; f < 7; ++f) std::memcpy(&k.w[f], &(*c[f])[i], 4);
+        if (last_id >= 0 && k == last) {   // runs along z share a tuple
+            idx[i] = (uint16_t)last_id;
+            continue;
+        }
+        auto it = ids.find(k);
+        int id;
+        if (it != ids.end()) {
+            id = it->second;
+        } else {
+            if (table.size() == 65536) return false;
+            id = (int)table.size();
+            ids.emplace(k, (uint16_t)id);
+            const auto v = [&](int f) { return (*c[f])[i]; };
+            table.push_back(ts::Pal3{make_float4(v(0), v(1), v(2), v(3)), make_float4(v(4), v(5), v(6), v(3))});
+        }
+        idx[i] = (uint16_t)id;
+        last = k;
+        last_id = id;
+    }
+    return true;
+}
 using ts::make_axis;
 using ts::round_up;
 
@@ -375,23 +424,9 @@ int ts_create(const ts_desc *d, ts_sim **out) {
                     dtr1[i] = inv_or0(0.5f * (rho(x, y + 1, z) + r));
                 }
     }
-    float *dev = nullptr;
-    if ((rc = s->upload(&dev, lam))) return bail(rc);
-    p.lam_dt = dev;
-    if ((rc = s->upload(&dev, mu))) return bail(rc);
-    p.mu_dt = dev;
-    for (int k = 0; k < n_shear; ++k) {
-        if ((rc = s->upload(&dev, mus[k]))) return bail(rc);
-        p.mus_dt[k] = dev;
-    }
-    if ((rc = s->upload(&dev, dtr0))) return bail(rc);
-    p.dtr[0] = dev;
-    if ((rc = s->upload(&dev, dtr1))) return bail(rc);
-    p.dtr[1] = dev;
-    p.dtr[2] = dev;  // vz uses the vy-node density (wgsl3d:1748)
-
     // ---- attenuation ----
     s->zen_mode = !d->visco ? 0 : (d->g_p ? 2 : 1);
+    std::vector<float> gp, gs;
     if (d->visco) {
         const int L = d->n_sls;
         p.zen = ts::zener_constants(d);
@@ -399,13 +434,52 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         for (int m = 0; m < nmem; ++m)
             if ((rc = s->alloc(&p.r[m], s->grid_elems * L, true))) return bail(rc);
         if (s->zen_mode == 2) {
-            std::vector<float> gp(s->grid_elems, 0.f), gs(s->grid_elems, 0.f);
+            gp.assign(s->grid_elems, 0.f);
+            gs.assign(s->grid_elems, 0.f);
             for (int x = 0; x < nx; ++x)
                 for (int y = 0; y < ny; ++y)
                     for (int z = 0; z < nz; ++z) {
                         gp[s->at(x, y, z)] = d->g_p[href(x, y, z)];
                         gs[s->at(x, y, z)] = d->g_s[href(x, y, z)];
                     }
+        }
+    }
+
+    // ---- coefficients to the device: a palette (3D, 32-bit offsets) or arrays ----
+    float *dev = nullptr;
+    bool palette = false;
+    const char *pal_env = getenv("TS_3D_COEF_PALETTE");   // "0": arrays (tests cover both paths)
+    if (s->dims == 3 && s->grid_elems * (int64_t)std::max(1, p.zen.n) < ((int64_t)1 << 31) &&
+        !(pal_env && pal_env[0] == '0')) {
+        const std::vector<float> ones(gp.empty() ? s->grid_elems : 0, 1.f);
+        const std::vector<float> *cols[7] = {&lam, &mu, gp.empty() ? &ones : &gp, gs.empty() ? &ones : &gs,
+                                             &mus[0], &mus[1], &mus[2]};
+        std::vector<uint16_t> idx;
+        std::vector<ts::Pal3> table;
+        if (build_palette_3d(cols, idx, table)) {
+            uint16_t *didx = nullptr;
+            ts::Pal3 *dtab = nullptr;
+            if ((rc = s->upload(&didx, idx)) || (rc = s->upload(&dtab, table))) return bail(rc);
+            p.pal_idx = didx;
+            p.pal = dtab;
+            palette = true;
+        }
+    }
+    if ((rc = s->upload(&dev, dtr0))) return bail(rc);
+    p.dtr[0] = dev;
+    if ((rc = s->upload(&dev, dtr1))) return bail(rc);
+    p.dtr[1] = dev;
+    p.dtr[2] = dev;  // vz uses the vy-node density (wgsl3d:1748)
+    if (!palette) {
+        if ((rc = s->upload(&dev, lam))) return bail(rc);
+        p.lam_dt = dev;
+        if ((rc = s->upload(&dev, mu))) return bail(rc);
+        p.mu_dt = dev;
+        for (int k = 0; k < n_shear; ++k) {
+            if ((rc = s->upload(&dev, mus[k]))) return bail(rc);
+            p.mus_dt[k] = dev;
+        }
+        if (s->zen_mode == 2) {
             if ((rc = s->upload(&dev, gp))) return bail(rc);
             p.g_p = dev;
             if ((rc = s->upload(&dev, gs))) return bail(rc);

@@ -15,6 +15,8 @@
 //  * sources are a sparse point list binned by thread block; receivers a
 //    CSR list of grid offsets per receiver.
 #pragma once
+#include <cuda_runtime.h>
+
 #include <cstdint>
 
 namespace ts {
@@ -51,6 +53,15 @@ struct Source {
 };
 
 // Everything a 2D or 3D kernel reads, passed by value.
+// One entry of the 3D coefficient palette: the coefficients each stress
+// kernel reads at a node, grouped so that a kernel fetches its own with one
+// load.  (The velocity kernel reads dt / rho from its arrays: its palette
+// variant measured slower.)
+struct alignas(16) Pal3 {
+    float4 normal;    // lambda dt, mu dt, Q scale p, Q scale s
+    float4 shear;     // mu dt at the xy, xz, yz nodes, Q scale s
+};
+
 struct StepParams {
     int family;
     int tx;                // 2D: nodes each thread updates along x (1, 2 or 4)
@@ -75,6 +86,10 @@ struct StepParams {
     const float *mus_dt[3];               // shear nodes xy, xz, yz (2D: xy)
     const float *dtr[3];                  // dt / rho at vx, vy, vz nodes (0: no update)
     const float *g_p, *g_s;               // per-cell attenuation scale (or null)
+    // 3D coefficient palette (or null): the stress kernels take node i's
+    // coefficients from pal[pal_idx[i]] instead of the arrays above
+    const uint16_t *pal_idx;
+    const Pal3 *pal;
     float *r[6];                          // memory variables, [n_sls] grids each
     int64_t grid_elems;                   // elements of one padded grid
     Zener zen;
@@ -152,6 +167,8 @@ void launch_step_2d(const StepParams &p, int ord, int zen_mode, int j, cudaStrea
 // (p.tx must be 2).
 void launch_step_2d_feat(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st);
 void launch_step_3d(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st, int parts = 3);
+// the palette instantiations of the stress kernels (p.pal set; 32-bit offsets)
+void launch_step_3d_pal(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st, int parts);
 void launch_reset_scalars(int *first_bad, int *step_base, cudaStream_t st);
 void launch_advance(int *step_base, int n, cudaStream_t st);
 int blocks_2d(const StepParams &p);

@@ -86,8 +86,12 @@ def test_parity_2d_nodes_per_thread(name, tx, monkeypatch):
     _compare(sim, family, ["vx", "vy", "sxx", "syy", "sxy"])
 
 
+@pytest.mark.parametrize("palette", ["1", "0"], ids=["palette", "arrays"])
 @pytest.mark.parametrize("name", sorted(CASES_3D))
-def test_parity_3d(name):
+def test_parity_3d(name, palette, monkeypatch):
+    """Both coefficient paths of the 3D kernels: the per-node palette of
+    distinct coefficient tuples and one array per coefficient."""
+    monkeypatch.setenv("TS_3D_COEF_PALETTE", palette)
     sim = Simulator3D(CASES_3D[name]())
     _compare(sim, engine.WGSL3D, ["vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "sxz", "syz"])
 
