@@ -98,8 +98,11 @@ def case_adjoint(w=64, h=64, steps=200, acc=2, visco=1, seed=0, true_model=True,
     return cfg
 
 
-def case_3d(w=30, d=26, h=34, steps=90, acc=2, visco=1, seed=0, q=None, matrix=False):
-    """A 3D experiment: layered block, Ricker point source, receivers on top."""
+def case_3d(w=30, d=26, h=34, steps=90, acc=2, visco=1, seed=0, q=None, matrix=False, probe="point"):
+    """A 3D experiment: layered block, Ricker point source, receivers on top.
+    ``probe="mono"``: one circular element that emits and receives
+    (pulse-echo); ``probe="linear"``: a 4-element linear array, every element
+    emitting and receiving."""
     dx = 0.1
     rng = np.random.default_rng(seed)
     cp = np.empty((w, d, h), np.float32)
@@ -124,6 +127,16 @@ def case_3d(w=30, d=26, h=34, steps=90, acc=2, visco=1, seed=0, q=None, matrix=F
     else:
         cfg["probes"].append({"point": {"id": "r", "emitter": "False", "receiver": "True",
                                         "coord_center": [w * dx / 2 + 0.5, d * dx / 2, 0.2]}})
+    if probe == "mono":
+        cfg["probes"] = [{"mono": {"id": "m", "radius": 0.02, "freq": 3.0, "bw": 0.5, "gain": 1e2,
+                                   "pulse_type": "gaussian", "coord_center": [w * dx / 2, d * dx / 2, 0.2],
+                                   "emitters": "True", "t0_emission": 0.3, "receivers": "True",
+                                   "t0_reception": 0.0}}]
+    elif probe == "linear":
+        cfg["probes"] = [{"linear": {"id": "a", "num_elem": 4, "dim_a": 0.3, "dim_p": 0.5, "inter_elem": 0.1,
+                                     "freq": 3.0, "bw": 0.5, "gain": 1e2,
+                                     "coord_center": [w * dx / 2, d * dx / 2, 0.2], "emitters": "all",
+                                     "receivers": "all", "t0_emission": 0.3, "t0_reception": 0.0}}]
     if q is not None:
         cfg["specimen_params"]["qp"] = 100.0
         cfg["specimen_params"]["qs"] = 60.0

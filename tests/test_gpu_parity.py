@@ -40,6 +40,9 @@ CASES_3D = {
     # deep enough along z for warps that take the interior sweep
     "wgsl3d_visco_deep": lambda: case_3d(visco=1, h=64, seed=6),
     "wgsl3d_acc4_deep": lambda: case_3d(visco=1, acc=4, h=70, seed=7, q=(30.0, 300.0)),
+    # 3D probes: a pulse-echo circular element and a linear array (points summed per element)
+    "wgsl3d_mono": lambda: case_3d(visco=1, probe="mono", h=40, seed=8),
+    "wgsl3d_linear_array": lambda: case_3d(visco=0, probe="linear", h=40, seed=9),
 }
 
 
