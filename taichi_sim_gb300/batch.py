@@ -8,8 +8,10 @@ the shot index is the innermost array axis, so a warp computes 32 shots of
 one grid node and the per-node coefficients are read once for all shots.
 
 :func:`fmc_shot_sources` builds the shots of a full-matrix capture (shot e
-fires element e of a linear array); :func:`autotune` picks the block shape
-by timing each candidate and caches the choice in ``_build/autotune.json``.
+fires element e of a linear array); :func:`focal_law_shot_sources` the shots
+of emission laws (delay rows from a ``.law`` file, :func:`plane_wave_laws`
+or :func:`focused_laws`); :func:`autotune` picks the launch shapes by timing
+each candidate and caches the choice in ``_build/autotune.json``.
 """
 import ctypes
 import json
@@ -97,6 +99,55 @@ def focal_law_shot_sources(sim, laws):
             if t0 is not None:
                 p.set_t0(t0)
     return np.ascontiguousarray(np.stack(tables))
+
+
+def _array_element_x(sim):
+    """Lateral (x) centres, mm from the ROI origin, of the elements of the
+    model's first emitting linear array."""
+    for i in sim._emitting_probes:
+        probe = sim._probes[i]
+        if hasattr(probe, "elem_list"):
+            cx = float(np.asarray(probe.coord_center, np.float64).ravel()[0])
+            return np.array([cx + float(e.coord_center[0]) for e in probe.elem_list], np.float64), probe
+    raise ValueError("the model has no emitting linear array")
+
+
+def _base_t0(probe):
+    t0 = getattr(probe, "_t0_emission", None)
+    return float(np.min(t0)) if t0 is not None else 0.0
+
+
+def plane_wave_laws(sim, angles_deg, c=None):
+    """Emission delays (one row per angle, the probes' t0_emission units)
+    that steer a plane wave from the model's first emitting linear array by
+    each angle (degrees from the array normal, positive towards +x), for a
+    sound speed ``c`` (mm per time unit; default: the specimen's cp).  The
+    earliest element of each law fires at the array's current smallest
+    delay.  An extension: the reference reads and writes laws
+    (sim_support/emission_law.py) but does not compute them."""
+    x, probe = _array_element_x(sim)
+    c = float(sim._configs["specimen_params"]["cp"] if c is None else c)
+    rows = []
+    for a in np.atleast_1d(angles_deg):
+        d = (x - x.min()) * np.sin(np.deg2rad(float(a))) / c
+        rows.append(_base_t0(probe) + d - d.min())
+    return np.asarray(rows, np.float32)
+
+
+def focused_laws(sim, focal_points, c=None):
+    """Emission delays (one row per focal point (x, z), mm from the ROI
+    origin) that focus the model's first emitting linear array at each point:
+    element e fires (r_max - r_e) / c after the array's current smallest
+    delay, r_e its distance to the focus (elements at the depth of the
+    probe centre).  An extension, as :func:`plane_wave_laws`."""
+    x, probe = _array_element_x(sim)
+    c = float(sim._configs["specimen_params"]["cp"] if c is None else c)
+    z0 = float(np.asarray(probe.coord_center, np.float64).ravel()[-1])
+    rows = []
+    for fx, fz in np.atleast_2d(np.asarray(focal_points, np.float64)):
+        r = np.hypot(x - fx, fz - z0)
+        rows.append(_base_t0(probe) + (r.max() - r) / c)
+    return np.asarray(rows, np.float32)
 
 
 def run_emission_laws(sim, laws=None, field="syy"):

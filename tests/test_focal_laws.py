@@ -38,3 +38,25 @@ def test_a_model_without_laws_needs_laws():
     sim = Simulator(case_2d(visco=1, steps=50))
     with pytest.raises(ValueError):
         run_emission_laws(sim)
+
+
+def test_plane_wave_and_focused_laws():
+    from taichi_sim_gb300.batch import focused_laws, plane_wave_laws
+    sim = Simulator(case_2d(visco=1, steps=200))
+    probe = sim._probes[0]
+    n_el = probe.num_elem
+    base = float(np.min(probe._t0_emission))
+    laws = plane_wave_laws(sim, [0.0, 10.0, -10.0], c=5.9)
+    assert laws.shape == (3, n_el)
+    np.testing.assert_allclose(laws[0], base, atol=1e-6)           # normal incidence: all together
+    assert np.all(np.diff(laws[1]) > 0) and np.all(np.diff(laws[2]) < 0)
+    np.testing.assert_allclose(laws[1], laws[2][::-1], atol=1e-6)  # mirror images
+    pitch = float(probe.pitch)
+    np.testing.assert_allclose(np.diff(laws[1]), pitch * np.sin(np.deg2rad(10.0)) / 5.9, rtol=1e-4)
+    assert laws[1].min() == np.float32(base)
+    cx = float(np.asarray(probe.coord_center).ravel()[0])
+    foc = focused_laws(sim, [(cx, 2.0)], c=5.9)[0]
+    np.testing.assert_allclose(foc, foc[::-1], atol=1e-6)           # symmetric about the centre
+    assert foc[n_el // 2] > foc[0] and np.isclose(foc.min(), base)  # the centre fires last
+    tables = focal_law_shot_sources(sim, laws)
+    assert tables.shape[0] == 3 and not np.array_equal(tables[1], tables[2])
