@@ -296,7 +296,6 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     s->n_rows = d->n_steps;
     s->n_rec = d->n_rec;
     const int nx = s->nx, ny = s->ny, nz = s->nz, ord = s->ord;
-    const int64_t ncell = (int64_t)nx * ny * nz;
     auto bail = [&](int code) {
         ts_destroy(s);
         return code;
