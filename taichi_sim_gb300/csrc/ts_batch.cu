@@ -11,7 +11,12 @@
 // Blocks are 32 lanes x CY nodes along y; each thread updates TX consecutive
 // nodes along x, keeping the x-stencil rows in a register window (one new
 // row per node), for SPT shots.  The flat block index runs over (phantom,
-// x-chunk, y-block, shot-block), so phantoms of any size share one launch.
+// x-chunk, y-block, shot-block), so phantoms of any size share one launch;
+// the stress and velocity launches may use different CY and TX (their own
+// block decompositions, Decomp), the shot layout (SPT) being shared.
+// Threads whose nodes all lie in the interior (no region, strip, bounds or
+// source test can fire) take a sweep with those tests compiled out; the
+// velocity kernel's interior sweep issues every load of its nodes first.
 // The phantom records are a __grid_constant__ parameter (constant cache, no
 // aliasing with the fields) and offsets are 32-bit (checked at creation).
 //
@@ -482,6 +487,8 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocksV<CY>::v)) k_bvelocity(cons
             sto<SPT>(v1 + i, vyn);
         }
     };
+    // The general sweep (every region, strip, bounds and source test); the
+    // interior sweep above replaces its FAST instantiation.
     auto sweep = [&](auto fast_tag) {
         constexpr bool FAST = decltype(fast_tag)::value;
         const int syl = FAST ? -1 : sy;

@@ -340,6 +340,8 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
         }
     };
 
+    // The general sweep (every region, strip, bounds and source test); the
+    // interior sweep above replaces its FAST instantiation.
     auto sweep = [&](auto fast_tag) {
         constexpr bool FAST = decltype(fast_tag)::value;
         const int syl = FAST ? -1 : sy;
