@@ -288,6 +288,26 @@ def _key(sims, shot_sources):
 SHAPES = tuple((cy, tx, spt) for spt in (1, 2) for cy in (4, 8) for tx in (1, 2, 4))
 
 
+def pick_shapes(timings):
+    """The launch shapes of the shortest step from per-shape kernel timings
+    ``{"CYxTXxSPT": [stress_ms, velocity_ms]}``: per shot layout (SPT) the
+    stress and velocity launches each take their fastest (CY, TX), and the
+    layout with the smallest sum wins.  Returns BatchStepper keyword
+    arguments."""
+    best, best_ms = None, float("inf")
+    for spt in sorted({int(k.split("x")[2]) for k in timings}):
+        mine = {k: v for k, v in timings.items() if int(k.split("x")[2]) == spt}
+        ks = min(mine, key=lambda k: mine[k][0])
+        kv = min(mine, key=lambda k: mine[k][1])
+        if mine[ks][0] + mine[kv][1] < best_ms:
+            best_ms = mine[ks][0] + mine[kv][1]
+            cs, ts_, _ = (int(v) for v in ks.split("x"))
+            cv, tv, _ = (int(v) for v in kv.split("x"))
+            best = {"block_cells": cs, "nodes_per_thread": ts_, "shots_per_thread": spt,
+                    "velocity_block_cells": cv, "velocity_nodes_per_thread": tv}
+    return best
+
+
 def autotune(sims, shot_sources, candidates=SHAPES, steps=12, use_cache=True):
     """Pick the launch shapes with the shortest measured step on this GPU.
 
@@ -319,17 +339,7 @@ def autotune(sims, shot_sources, candidates=SHAPES, steps=12, use_cache=True):
         with BatchStepper(sims, shot_sources, block_cells=cy, nodes_per_thread=tx, shots_per_thread=spt) as b:
             b.profile_steps(2)
             timings[f"{cy}x{tx}x{spt}"] = [float(v) for v in b.profile_steps(steps)]
-    best, best_ms = None, float("inf")
-    for spt in sorted({c[2] for c in candidates}):
-        mine = {k: v for k, v in timings.items() if int(k.split("x")[2]) == spt}
-        ks = min(mine, key=lambda k: mine[k][0])
-        kv = min(mine, key=lambda k: mine[k][1])
-        if mine[ks][0] + mine[kv][1] < best_ms:
-            best_ms = mine[ks][0] + mine[kv][1]
-            cs, ts_, _ = (int(v) for v in ks.split("x"))
-            cv, tv, _ = (int(v) for v in kv.split("x"))
-            best = {"block_cells": cs, "nodes_per_thread": ts_, "shots_per_thread": spt,
-                    "velocity_block_cells": cv, "velocity_nodes_per_thread": tv}
+    best = pick_shapes(timings)
     cache[key] = {"shape": best, "timings": timings, "when": time.time()}
     os.makedirs(os.path.dirname(path), exist_ok=True)
     with open(path, "w") as f:
