@@ -24,3 +24,40 @@ def test_candidate_shapes():
     assert len(batch.SHAPES) == 12 and len(set(batch.SHAPES)) == 12
     assert {s[0] for s in batch.SHAPES} == {4, 8} and {s[1] for s in batch.SHAPES} == {1, 2, 4}
     assert {s[2] for s in batch.SHAPES} == {1, 2}
+
+
+def test_autotune_times_every_candidate_and_caches(tmp_path, monkeypatch):
+    """autotune with a stand-in stepper (no GPU): every candidate is timed
+    once, the choice follows pick_shapes, and a second call reads the cache."""
+    import numpy as np
+    from _cases import case_2d
+    from taichi_sim_gb300.sim_support.simulator import Simulator
+
+    made = []
+
+    class FakeStepper:
+        def __init__(self, sims, shots, block_cells, nodes_per_thread, shots_per_thread):
+            self.shape = (block_cells, nodes_per_thread, shots_per_thread)
+            made.append(self.shape)
+
+        def profile_steps(self, n):
+            cy, tx, spt = self.shape
+            return [1.0 + 0.1 * cy / spt, 1.0 / tx + 0.01 * cy]   # stress, velocity
+
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *exc):
+            pass
+
+    monkeypatch.setattr(batch, "BatchStepper", FakeStepper)
+    monkeypatch.setattr(batch, "_cache_path", lambda: str(tmp_path / "autotune.json"))
+    sim = Simulator(case_2d(visco=1, steps=40))
+    shots = [np.zeros((3,) + np.shape(sim._source_term), np.float32)]
+    best, timings = batch.autotune([sim], shots, steps=2)
+    assert sorted(set(made)) == sorted(batch.SHAPES) and len(made) == len(batch.SHAPES)
+    assert best == batch.pick_shapes(timings)
+    assert best["shots_per_thread"] == 2 and best["block_cells"] == 4 and best["velocity_nodes_per_thread"] == 4
+    made.clear()
+    again, _ = batch.autotune([sim], shots, steps=2)
+    assert again == best and made == []
