@@ -99,3 +99,47 @@ def test_taichi_family_is_elastic_only(lib):
     h = ctypes.c_void_p()
     assert lib.ts_create(ctypes.byref(d), ctypes.byref(h)) == 1
     assert b"elastic only" in lib.ts_last_error()
+
+
+def _batch_desc(lib, **shape):
+    from taichi_sim_gb300 import batch
+    batch._bind(lib)
+    d = _desc(ord=2)
+    phantoms = (engine.TsDesc * 1)(d)
+    n_shots = (ctypes.c_int32 * 1)(4)
+    tab = np.zeros(4 * 10, np.float32)
+    ptrs = (ctypes.POINTER(ctypes.c_float) * 1)(tab.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    bd = batch.BatchDesc(abi_version=engine.ABI_VERSION, n_phantoms=1, phantoms=phantoms, n_shots=n_shots,
+                         shot_sources=ptrs, **shape)
+    return bd, (phantoms, n_shots, tab, ptrs)
+
+
+@pytest.mark.parametrize("shape,needle", [
+    (dict(block_cells=6), b"block_cells"),
+    (dict(velocity_block_cells=2), b"block_cells"),
+    (dict(nodes_per_thread=3), b"nodes_per_thread"),
+    (dict(velocity_nodes_per_thread=8), b"nodes_per_thread"),
+    (dict(shots_per_thread=3), b"shots_per_thread"),
+])
+def test_batch_create_rejects_bad_launch_shapes(lib, shape, needle):
+    bd, keep = _batch_desc(lib, **shape)
+    h = ctypes.c_void_p()
+    assert lib.ts_batch_create(ctypes.byref(bd), ctypes.byref(h)) == 1
+    assert needle in lib.ts_batch_last_error()
+    assert h.value is None
+
+
+def test_order4_batch_takes_the_default_shape(lib):
+    bd, keep = _batch_desc(lib, velocity_nodes_per_thread=4)
+    keep[0][0].ord = 4
+    h = ctypes.c_void_p()
+    assert lib.ts_batch_create(ctypes.byref(bd), ctypes.byref(h)) == 1
+    assert b"order-4" in lib.ts_batch_last_error()
+
+
+def test_adjoint_entry_points_reject_null(lib):
+    from taichi_sim_gb300 import adjoint
+    adjoint._bind(lib)
+    assert lib.ts_adj_set_record_segments(None, 3) == 1
+    assert lib.ts_adj_forward(None, None, None, None) == 1
+    assert lib.ts_adj_backward(None, None, None, None) == 1
