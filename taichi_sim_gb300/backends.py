@@ -87,6 +87,29 @@ class SimulatorCudaViscoelastic(_CudaBackend, Simulator):
         super().__init__(file_config, sim_type="viscoelastic")
         self._name = "CUDA-viscoelastic"
 
+    def implementation_batched(self, laws):
+        """Every emission law as a shot of one batched launch
+        (:class:`~taichi_sim_gb300.batch.BatchStepper`); ``None`` runs the
+        source term as built.  One result dict per law, with the keys of
+        :meth:`implementation` and ``sim_time`` the launch's share per law."""
+        from .batch import BatchStepper, focal_law_shot_sources
+        laws = list(laws)
+        if len(laws) == 1 and laws[0] is None:
+            st = np.asarray(self._source_term, np.float32)
+            shots = (st[:, None] if st.ndim == 1 else st)[None]
+        else:
+            shots = focal_law_shot_sources(self, laws)
+        t0 = time.time()
+        with BatchStepper([self], [shots]) as b:
+            b.run(self._n_steps)
+            _, vmax, bad = b.status()
+            if bad >= 0:
+                raise engine.StabilityError("Simulacao tornando-se instavel", float(np.sqrt(np.float32(vmax))))
+            traces, fields = b.traces(0), b.field(0, self._field)
+        sim_time = (time.time() - t0) / len(shots)
+        return [{self._keys[0]: fields[k], self._keys[1]: traces[k], "gpu_str": _gpu_name(), "sim_time": sim_time}
+                for k in range(len(shots))]
+
 
 class SimulatorCuda3DViscoelastic(_CudaBackend, Simulator3D):
     """3D (visco)elastic stepper with the WebGPU 3D backend's semantics."""

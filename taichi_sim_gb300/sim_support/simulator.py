@@ -42,8 +42,14 @@ class ExperimentDriver:
             return field[roi.get_ix_min():roi.get_ix_max(), roi.get_iz_min():roi.get_iz_max()]
         return field[roi.get_ix_min():roi.get_ix_max(), :, roi.get_iz_min():roi.get_iz_max()]
 
-    def run(self):
-        """Run every (iteration, emission law) and report; returns the last result dict."""
+    def run(self, batched=False):
+        """Run every (iteration, emission law) and report; returns the last result dict.
+
+        ``batched=True`` (an extension) computes the emission laws of an
+        iteration together, as shots of one batched launch
+        (``implementation_batched``), each law with its own delays; the
+        per-law loop, like the reference's, calls ``set_t0`` but injects the
+        source term the constructor built."""
         now = datetime.now()
         sim_times, total_times, mse_values = list(), list(), list()
         results = dict()
@@ -52,14 +58,23 @@ class ExperimentDriver:
         for n in range(self._n_iter):
             print(f'Iteracao {n}')
             n_laws = self._emission_laws.shape[0] if hasattr(self, "_emission_laws") else 1
+            if batched:
+                t_start = time()
+                batch_results = self.implementation_batched(
+                    list(self._emission_laws) if hasattr(self, "_emission_laws") else [None])
+                t_batch = time() - t_start
             for law in range(n_laws):
                 print(f'\tLaw {law} of {n_laws}')
-                if hasattr(self, "_emission_laws"):
-                    for p in self._probes:
-                        p.set_t0(self._emission_laws[law])
-                t_start = time()
-                results = self.implementation()
-                total_times.append(time() - t_start)
+                if batched:
+                    results = batch_results[law]
+                    total_times.append(t_batch / n_laws)
+                else:
+                    if hasattr(self, "_emission_laws"):
+                        for p in self._probes:
+                            p.set_t0(self._emission_laws[law])
+                    t_start = time()
+                    results = self.implementation()
+                    total_times.append(time() - t_start)
                 sim_times.append(results["sim_time"])
                 print(results["gpu_str"])
                 print(f'{sim_times[-1]:.3}s')
@@ -170,6 +185,11 @@ class ExperimentDriver:
         """Backends override this; the base only announces the run."""
         print(f'Simulacao {self._name}')
         return dict()
+
+    def implementation_batched(self, laws):
+        """One result dict per emission law (``None``: the probes' current
+        delays), all laws computed together; backends that batch override it."""
+        raise NotImplementedError(f"{type(self).__name__} has no batched run")
 
 
 class Simulator(ExperimentDriver, ModelBase):
