@@ -152,3 +152,21 @@ def test_law_file_runs_as_one_batched_launch(tmp_path):
             one.run(sim._n_steps)
             want_tr, want_f = one.read("traces"), one.read("syy")
         assert rel_l2(traces[k], want_tr) <= TOL and rel_l2(fields[k], want_f) <= TOL
+
+
+def test_driver_batched_run_matches_run_emission_laws(tmp_path):
+    """The reference's driver with batched=True (2D viscoelastic backend):
+    the last law's traces equal the batched launch's."""
+    from taichi_sim_gb300.backends import SimulatorCudaViscoelastic
+    from taichi_sim_gb300.batch import run_emission_laws
+    from taichi_sim_gb300.sim_support.emission_law import EmissionLaw
+    cfg = workloads.fmc2d_phantoms(n_steps=120, shapes=((80, 84),), n_elem=6, dx=0.1, pml=8)[0]
+    cfg["probes"][0]["linear"].update(dim_a=0.3, inter_elem=0.1)
+    dt = float(Simulator(cfg)._dt)
+    EmissionLaw().write_law(str(tmp_path / "steer"), np.stack([np.arange(6) * k * dt for k in (0.0, 2.0)]) + 3 * dt)
+    cfg["simul_configs"]["emission_laws"] = str(tmp_path / "steer.law")
+    sim = SimulatorCudaViscoelastic(cfg)
+    out = sim.run(batched=True)
+    traces, _ = run_emission_laws(sim)
+    np.testing.assert_array_equal(out["sens_stress"], traces[-1])
+    assert np.abs(out["sens_stress"]).max() > 0
