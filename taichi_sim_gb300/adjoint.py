@@ -141,9 +141,9 @@ class AdjointProblem:
         self.pitch = p.value
         self._g = None
         if self._per_cell_q:
-            fit = sim._zener_fit
-            self._g = (self._pad(torch.as_tensor(fit.cell_scale(sim._inv_qp_grid), dtype=torch.float32)),
-                       self._pad(torch.as_tensor(fit.cell_scale(sim._inv_qs_grid), dtype=torch.float32)))
+            g_p, g_s = sim.cell_scales()
+            self._g = (self._pad(torch.as_tensor(g_p, dtype=torch.float32)),
+                       self._pad(torch.as_tensor(g_s, dtype=torch.float32)))
         self._token = 0          # identifies the forward the handle holds
         self._next_token = 1
 

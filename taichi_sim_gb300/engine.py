@@ -188,8 +188,9 @@ class Stepper:
                 c, h, m = fit.mechanism_constants(sim._dt)
                 d.n_sls = fit.n_sls
                 d.zc, d.zh, d.zm = self._f32(c), self._f32(h), self._f32(m)
-                d.g_p = self._f32(fit.cell_scale(sim._inv_qp_grid))
-                d.g_s = self._f32(fit.cell_scale(sim._inv_qs_grid))
+                g_p, g_s = sim.cell_scales()
+                d.g_p = self._f32(g_p)
+                d.g_s = self._f32(g_s)
             else:
                 att = AttenuationCoefficients()
                 d.n_sls = att._n_sls

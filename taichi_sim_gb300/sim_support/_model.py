@@ -331,3 +331,17 @@ class ModelBase:
         self._qs = qs
         self._inv_qp_grid = (1.0 / self._material_grid(qp, "qp_map").astype(np.float64)).astype(flt32)
         self._inv_qs_grid = (1.0 / self._material_grid(qs, "qs_map").astype(np.float64)).astype(flt32)
+
+    def cell_scales(self):
+        """Per-cell attenuation scales ``(g_p, g_s)`` of the fitted Zener
+        model (float32 grids), or None without per-cell Q.  Computed once and
+        kept while the 1/Q grids stay the same objects (a stepper is created
+        per shot; the scales are the same for every shot)."""
+        if self._zener_fit is None:
+            return None
+        cached = getattr(self, "_cell_scales_cache", None)
+        if cached is None or cached[0] is not self._inv_qp_grid or cached[1] is not self._inv_qs_grid:
+            g = (self._zener_fit.cell_scale(self._inv_qp_grid), self._zener_fit.cell_scale(self._inv_qs_grid))
+            cached = (self._inv_qp_grid, self._inv_qs_grid, g)
+            self._cell_scales_cache = cached
+        return cached[2]

@@ -41,3 +41,21 @@ def test_tables_bit_identical(name):
                 detail = f" max|diff|={np.max(np.abs(v.astype(np.float64) - ref[key].astype(np.float64)))}"
             bad.append(f"{key}: bytes differ{detail}")
     assert not bad, "\n".join(bad)
+
+
+def test_cell_scales_are_computed_once_and_follow_the_q_grids():
+    """The per-cell attenuation scales a stepper uploads: the fit's formula,
+    cached on the model (one computation for every shot's stepper)."""
+    import numpy as np
+    import sys, os
+    sys.path.insert(0, os.path.dirname(__file__))
+    from _cases import case_2d
+    from taichi_sim_gb300.sim_support.simulator import Simulator
+    sim = Simulator(case_2d(visco=1, q=(30.0, 200.0), seed=1, steps=20))
+    g = sim.cell_scales()
+    np.testing.assert_array_equal(g[0], sim._zener_fit.cell_scale(sim._inv_qp_grid))
+    np.testing.assert_array_equal(g[1], sim._zener_fit.cell_scale(sim._inv_qs_grid))
+    assert sim.cell_scales()[0] is g[0]                     # cached
+    sim._inv_qp_grid = sim._inv_qp_grid * np.float32(2.0)   # a new grid object: recomputed
+    np.testing.assert_array_equal(sim.cell_scales()[0], sim._zener_fit.cell_scale(sim._inv_qp_grid))
+    assert Simulator(case_2d(visco=1, steps=20)).cell_scales() is None
