@@ -44,7 +44,8 @@
 extern "C" {
 #endif
 
-#define TS_ABI_VERSION 1
+/* 2: ts_batch_desc gained the velocity launch shape */
+#define TS_ABI_VERSION 2
 
 /* status codes */
 #define TS_OK 0

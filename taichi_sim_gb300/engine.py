@@ -20,7 +20,7 @@ from .sim_support.attenuation import AttenuationCoefficients
 
 TAICHI2D, WGSL2D, WGSL3D = 0, 1, 2
 VX, VY, VZ, SXX, SYY, SZZ, SXY, SXZ, SYZ, TRACES = range(10)
-ABI_VERSION = 1
+ABI_VERSION = 2
 FIELD_NAMES = {"vx": VX, "vy": VY, "vz": VZ, "sxx": SXX, "syy": SYY, "szz": SZZ, "sxy": SXY, "sxz": SXZ,
                "syz": SYZ}
 
