@@ -294,8 +294,14 @@ const char *ts_adj_last_error(void);
  * 0 clears it (a new simulation); step0 > 0 continues the previous call's
  * simulation.  Calls that overlap on the GPU, or that interleave two
  * simulations, race on it.  The first call on each device looks up the
- * array's device address; make it before any stream capture.  No stability
- * check is made (the caller can inspect the fields).
+ * array's device address; make it before any stream capture.  That address
+ * is kept for the life of the process and does not survive a reset of the
+ * device's context (cudaDeviceReset): do not call this after one.  No
+ * stability check is made (the caller can inspect the fields).
+ *
+ * src_cell and rec_cell are device tables, which the host cannot check: the
+ * kernel ignores any entry outside [0, nx * ny).  Several src_cell entries
+ * naming the same node all inject (their contributions add up).
  */
 #define TS_NOALLOC_SCRATCH_FLOATS (8u << 20)
 

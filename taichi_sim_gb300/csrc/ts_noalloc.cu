@@ -19,7 +19,12 @@
 // left, so calls that overlap on the GPU, or interleave two simulations,
 // race on it.  The host needs the array's device address, which is looked up
 // (cudaGetSymbolAddress) by the first call on each device; make that first
-// call before any stream capture.
+// call before any stream capture.  The looked-up address is kept for the
+// life of the process: it does not survive a reset of the device's context
+// (cudaDeviceReset), after which this entry point must not be called.
+//
+// Source and receiver cells come as device tables the host cannot read, so
+// the kernel range-checks them: entries outside the grid are ignored.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -135,17 +140,27 @@ __global__ void k_na_velocity(const NaParams p) {
 }
 
 // Source injection (after the velocity update, as wgsl:1059-1065) and
-// receiver sampling of syy (wgsl:1118-1134, one node per receiver).
+// receiver sampling of syy (wgsl:1118-1134, one node per receiver).  The
+// cell tables live in device memory, where the host cannot check them, so
+// the kernel does: a source or receiver whose cell lies outside [0, nx*ny)
+// is skipped (its trace row entries are left untouched).  Sources add with
+// atomicAdd, so several entries naming one cell all inject.
 __global__ void k_na_sources_receivers(const NaParams p, int k) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t n = (int64_t)p.nx * p.ny;
     if (t < p.n_src) {
         const int64_t c = p.src_cell[t];
-        const int x = (int)(c / p.ny), y = (int)(c % p.ny);
-        const float r4 =
-            0.25f * (at(p.rho, p, x, y) + at(p.rho, p, x + 1, y) + at(p.rho, p, x + 1, y + 1) + at(p.rho, p, x, y + 1));
-        if (r4 > 0.f) p.vy[c] += p.src_value[(int64_t)k * p.n_src + t] * p.dt / r4;
+        if (c >= 0 && c < n) {
+            const int x = (int)(c / p.ny), y = (int)(c % p.ny);
+            const float r4 = 0.25f * (at(p.rho, p, x, y) + at(p.rho, p, x + 1, y) + at(p.rho, p, x + 1, y + 1) +
+                                      at(p.rho, p, x, y + 1));
+            if (r4 > 0.f) atomicAdd(p.vy + c, p.src_value[(int64_t)k * p.n_src + t] * p.dt / r4);
+        }
     }
-    if (t < p.n_rec && k >= p.rec_first_step[t]) p.traces[(int64_t)k * p.n_rec + t] = p.syy[p.rec_cell[t]];
+    if (t < p.n_rec && k >= p.rec_first_step[t]) {
+        const int64_t c = p.rec_cell[t];
+        if (c >= 0 && c < n) p.traces[(int64_t)k * p.n_rec + t] = p.syy[c];
+    }
 }
 
 int na_fail(const std::string &msg) {

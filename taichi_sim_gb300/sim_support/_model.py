@@ -331,12 +331,17 @@ class ModelBase:
         self._qs = qs
         self._inv_qp_grid = (1.0 / self._material_grid(qp, "qp_map").astype(np.float64)).astype(flt32)
         self._inv_qs_grid = (1.0 / self._material_grid(qs, "qs_map").astype(np.float64)).astype(flt32)
+        # read-only: cell_scales() caches on the grids' identity, so a new Q
+        # model must replace a grid (an in-place edit raises)
+        self._inv_qp_grid.setflags(write=False)
+        self._inv_qs_grid.setflags(write=False)
 
     def cell_scales(self):
         """Per-cell attenuation scales ``(g_p, g_s)`` of the fitted Zener
         model (float32 grids), or None without per-cell Q.  Computed once and
         kept while the 1/Q grids stay the same objects (a stepper is created
-        per shot; the scales are the same for every shot)."""
+        per shot; the scales are the same for every shot).  The 1/Q grids are
+        read-only: assign new arrays to change the Q model."""
         if self._zener_fit is None:
             return None
         cached = getattr(self, "_cell_scales_cache", None)

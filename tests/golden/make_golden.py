@@ -1,9 +1,10 @@
 """Generate the golden fixtures under tests/golden/ from the reference project.
 
-Run in a container that has the reference checkout (read-only) at
-``--ref`` (default /root/reference)::
+Run where a checkout of the reference project is available (read-only is
+enough), naming it with ``--ref`` or the ``TAICHI_SIM_REF`` environment
+variable::
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py --ref <checkout>
 
 What it writes (all small, compressed):
 
@@ -124,8 +125,11 @@ def synthetic_point_line(n=128):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("TAICHI_SIM_REF"),
+                    help="checkout of the reference project (or set TAICHI_SIM_REF)")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("name the reference checkout with --ref or TAICHI_SIM_REF")
     ref = os.path.abspath(args.ref)
     stub_gui()
     sys.path.insert(0, ref)

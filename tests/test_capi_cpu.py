@@ -143,3 +143,71 @@ def test_adjoint_entry_points_reject_null(lib):
     assert lib.ts_adj_set_record_segments(None, 3) == 1
     assert lib.ts_adj_forward(None, None, None, None) == 1
     assert lib.ts_adj_backward(None, None, None, None) == 1
+
+
+def _noalloc_args(**over):
+    """A ts_noalloc2d_args that passes every check, then the overrides.  The
+    pointers are host addresses the entry point never dereferences: each
+    rejection happens before any CUDA call."""
+    buf = np.zeros(16, np.float32)
+    a = engine.NoAlloc2DArgs()
+    a.nx, a.ny, a.ord = 64, 48, 2
+    a.coefs[0], a.coefs[1] = 1.125, -1.0 / 24
+    a.dx, a.dy, a.dt = 0.05, 0.05, 1e-3
+    for n in ("vx", "vy", "sxx", "syy", "sxy", "rho", "cp", "cs", "a_x", "b_x", "k_x", "a_xh", "b_xh", "k_xh",
+              "a_y", "b_y", "k_y", "a_yh", "b_yh", "k_yh", "src_cell", "src_value", "rec_cell",
+              "rec_first_step", "traces"):
+        setattr(a, n, buf.ctypes.data)
+    a.n_src, a.n_rec, a.n_rows, a.step0, a.n_steps = 1, 1, 10, 0, 10
+    for k, v in over.items():
+        setattr(a, k, v)
+    return a, buf
+
+
+@pytest.mark.parametrize("over,needle", [
+    ({"ord": 1}, "ord must be in"),
+    ({"ord": 7}, "ord must be in"),
+    ({"nx": 4}, "grid smaller than the stencil"),
+    ({"ny": 4}, "grid smaller than the stencil"),
+    ({"nx": 2048, "ny": 1024}, "exceeds the no-allocation scratch"),
+    ({"vx": None}, "missing field or material"),
+    ({"cs": None}, "missing field or material"),
+    ({"k_yh": None}, "missing CPML table"),
+    ({"step0": -1}, "steps beyond"),
+    ({"n_steps": -1}, "steps beyond"),
+    ({"step0": 5, "n_steps": 6}, "steps beyond"),
+    ({"n_src": -1}, "bad source list"),
+    ({"src_cell": None}, "bad source list"),
+    ({"src_value": None}, "bad source list"),
+    ({"n_rec": -2}, "bad receiver list"),
+    ({"rec_first_step": None}, "bad receiver list"),
+    ({"traces": None}, "bad receiver list"),
+    ({"dx": 0.0}, "must be positive"),
+    ({"dt": float("nan")}, "must be positive"),
+])
+def test_noalloc_rejects_bad_arguments(lib, over, needle):
+    """Each TS_E_ARG branch of ts_run_noalloc_2d, checked before any CUDA call."""
+    a, keep = _noalloc_args(**over)
+    with pytest.raises(RuntimeError, match=needle):
+        engine.run_noalloc_2d(a)
+
+
+def test_noalloc_rejects_null_arguments(lib):
+    fn = lib.ts_run_noalloc_2d
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    fn.restype = ctypes.c_int
+    assert fn(None, None) == 1
+    lib.ts_noalloc_last_error.restype = ctypes.c_char_p
+    assert b"null arguments" in lib.ts_noalloc_last_error()
+
+
+def test_noalloc_empty_lists_need_no_tables(lib):
+    """n_src = n_rec = 0 needs no source or receiver table: the checks pass.
+    With n_steps = 0 no kernel runs (the host pointers above are never
+    handed to the device); without a GPU the call stops at the device query."""
+    a, keep = _noalloc_args(n_src=0, n_rec=0, src_cell=None, src_value=None, rec_cell=None,
+                            rec_first_step=None, traces=None, n_steps=0)
+    try:
+        engine.run_noalloc_2d(a)
+    except RuntimeError as e:
+        assert "invalid argument" not in str(e)

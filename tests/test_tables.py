@@ -58,4 +58,7 @@ def test_cell_scales_are_computed_once_and_follow_the_q_grids():
     assert sim.cell_scales()[0] is g[0]                     # cached
     sim._inv_qp_grid = sim._inv_qp_grid * np.float32(2.0)   # a new grid object: recomputed
     np.testing.assert_array_equal(sim.cell_scales()[0], sim._zener_fit.cell_scale(sim._inv_qp_grid))
+    import pytest
+    with pytest.raises(ValueError):                         # in-place edits would leave the cache stale
+        sim._inv_qs_grid *= np.float32(2.0)
     assert Simulator(case_2d(visco=1, steps=20)).cell_scales() is None
