@@ -1,6 +1,7 @@
-"""Benchmark: Gcell-updates/s of the GB300 stepper on a benchmark workload.
+"""Benchmark: Gcell-updates/s of the GB300 stepper on the benchmark workloads.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload visco2d|elastic2d|visco3d]
+    python bench.py [--gpus N] [--steps K] [--warmup W]       # visco2d + every other workload as a sub-record
+    python bench.py --workload visco2d|elastic2d|visco3d|fmc2d|adjoint2d ...   # one workload alone
     python bench.py --impl reference ...     # the CPU implementation of the same path
 
 One bench "step" is one complete simulation of the workload (all its time
@@ -11,16 +12,24 @@ flushed (a 256 MiB write) after every simulation, inside the timed region.
 Under torchrun each rank runs its own replica (the path shards over shots;
 a single-shot workload has no exchange), and the time is the max over ranks.
 
-The JSON line adds:
-  roofline     - HBM roofline of the dominant kernel (stress update),
-                 algorithmic bytes per launch / mean launch time (CUDA events
-                 around single launches), against the measured HBM peak;
-  cpu_baseline - the CPU restatement of the reference kernels (all host
-                 cores) on a bounded sample of the same workload;
-  e2e          - the same metric through the public C-ABI call sequence with
-                 host buffers: ts_create (uploads) + ts_run + ts_read of the
-                 traces and final field + ts_destroy, wall clock;
-  clocks       - SM clocks and throttle reasons sampled during the timing.
+The default line is the 2D viscoelastic workload (1024^2, L = 3, per-cell Q,
+4000 steps); under "workloads" it carries one record per other benchmark
+target, each timed the same way with its own step count: elastic2d (512^2,
+Taichi semantics, 2000 steps), visco3d (256^3, 1000 steps), fmc2d (64 shots
+x 3 phantoms, 3000 steps, with the per-shot loop it replaces) and adjoint2d
+(16-shot gradient on 512x1024, 3000 steps, with t_grad / t_forward).
+
+Each record adds:
+  roofline      - HBM roofline of the dominant kernel, algorithmic bytes per
+                  launch / mean launch time (CUDA events around single
+                  launches), against the measured HBM peak, with the ncu DRAM
+                  traffic per launch from profiles/traffic_<workload>.json;
+  step_roofline - the whole time step at the benchmark's bytes per cell-update;
+  e2e           - the same metric through the public C-ABI call sequence with
+                  host buffers (creation with uploads, run, readback, destroy);
+  clocks        - SM clocks and throttle reasons sampled during the timing;
+and the headline a cpu_baseline: the CPU restatement of the reference
+kernels (all host cores) on a bounded sample of the same workload.
 """
 import argparse
 import json
@@ -143,17 +152,37 @@ def cpu_baseline(sim, name, target_s=12.0):
                       f"(C restatement of the reference kernels, OpenMP, {dt:.1f} s)"}
 
 
+def traffic(name, kernel):
+    """ncu DRAM bytes (read + write) per launch of a workload's kernel, from
+    the committed profile summary profiles/traffic_<name>.json, or None."""
+    path = os.path.join(ROOT, "profiles", f"traffic_{name}.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def workload_config(name, sim):
+    """The ``config`` of a workload's line (shared with the reference arm)."""
+    return {"workload": name, "grid": list(sim.grid_shape()), "time_steps_per_step": int(sim._n_steps),
+            "family": FAMILY[name], "receivers": int(sim._n_rec),
+            "zener": "L=3 fitted 2-8 MHz, per-cell Q" if name != "elastic2d" else None,
+            "l2": "256 MiB flush written after every simulation (inside the timed region)"}
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU path (the oracle port: the
     reference's own kernels need Taichi/wgpu, absent here) on the same metric."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    name = args.workload
+    name = args.workload or "visco2d"
     if name == "adjoint2d":
         print(json.dumps({"impl": "reference", "unavailable": "the reference computes no gradients"}))
         return
-    if name == "fmc2d":
+    per_shot = name == "fmc2d"
+    if per_shot:
         name = "visco2d"   # the reference runs one shot at a time: its per-shot path
     sim = build_model(name, args.time_steps)
     from oracle import oracle
@@ -168,18 +197,118 @@ def run_reference(args):
         oracle.run(sim, fam, n_steps=sample)
     dt = time.time() - t
     value = cells * sample * args.steps / dt / 1e9
+    cfg = workload_config(name, sim)
+    cfg["parallelism"] = "single GPU"
+    desc = (f"{sample} of the {sim._n_steps} time steps of the full {'x'.join(map(str, sim.grid_shape()))} grid "
+            f"per bench step (C restatement of the reference kernels, OpenMP, {cores} threads)")
     line = {"impl": "reference", "metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": name, "grid": list(sim.grid_shape()), "time_steps_per_step": sample},
-            "cpu_baseline": {"value": value, "unit": "Gcell/s", "cores": cores, "kind": "port",
-                             "sample": f"{sample} time steps of the full grid per step"},
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded numpy default_rng(0); no public dataset exists)",
+            "config": cfg,
+            "cpu_baseline": {"value": value, "unit": "Gcell/s", "cores": cores, "kind": "port", "sample": desc},
             "e2e": {"value": value, "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if per_shot:
+        line["note"] = "fmc2d: the reference runs one shot at a time; its per-shot rate on the 1024x1024 model"
     print(json.dumps(line))
 
 
-def run_fmc(args):
+def stepper_record(name, args, steps, warmup, world=1, rank=0, local=0, dist=None, with_cpu=False):
+    """One workload on the single-simulation stepper: K complete simulations
+    timed with CUDA events, the dominant kernel's roofline, the whole-step
+    roofline at the benchmark's bytes per cell-update, and the same metric
+    end to end through the C ABI with host buffers."""
+    import torch
+    from taichi_sim_gb300 import engine, shards
+
+    sim = build_model(name, args.time_steps)
+    n_t = int(sim._n_steps)
+    cells = int(np.prod(sim.grid_shape()))
+    fam = getattr(engine, FAMILY[name])
+    st = engine.Stepper(sim, family=fam)
+    stream = torch.cuda.Stream()
+    h = stream.cuda_stream
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def one_simulation():
+        st.reset(stream=h, wait=False)
+        st.run(n_t, stream=h)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    for _ in range(warmup):
+        one_simulation()
+    torch.cuda.synchronize()
+    _, _, bad = st.status()
+    if bad >= 0:
+        raise RuntimeError(f"{name}: workload unstable at step {bad}")
+    launches0 = st.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        start.record(stream)
+        for _ in range(steps):
+            one_simulation()
+        end.record(stream)
+        torch.cuda.synchronize()
+    launches = st.launch_count() - launches0
+    ms = start.elapsed_time(end)
+    ms = shards.max_over_ranks(ms, device="cuda")   # the job's time: its slowest replica
+    value = cells * n_t * steps * world / (ms / 1e3) / 1e9
+
+    # ---- roofline of the dominant kernel (single launches between events) ----
+    st.reset()
+    k_ms = st.profile_steps(min(args.profile_steps, n_t), stream=h)
+    kb = KERNEL_BYTES[name]
+    frac = strip_fraction(sim)
+    strip_share = sum(frac) / len(frac)
+    bytes_stress = cells * (kb["stress"] + kb["psi_stress"] * 2 * strip_share)
+    bytes_vel = cells * (kb["velocity"] + kb["psi_vel"] * 2 * strip_share)
+    peak, peak_kind = peaks()
+    dom = 0 if k_ms[0] >= k_ms[1] else 1
+    dom_bytes = [bytes_stress, bytes_vel][dom]
+    achieved = dom_bytes / (k_ms[dom] / 1e3) / 1e9
+    kname = ["stress", "velocity"][dom]
+    roofline = {"kernel": kname, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic(name, kname), "peak_kind": peak_kind,
+                "bytes_per_launch": int(dom_bytes),
+                "kernel_ms": {"stress": round(k_ms[0], 5), "velocity": round(k_ms[1], 5)}}
+    b_alg = workloads.B_ALG[name]
+    step_roofline = {"b_alg_per_cell_update": b_alg, "achieved": round(value / world * b_alg, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(value / world * b_alg / peak, 4), "peak_kind": peak_kind,
+                     "note": "whole time step (all kernels) at the benchmark's algorithmic bytes per cell-update"}
+    st.close()
+
+    # ---- end to end through the C ABI with host buffers ----
+    e2e_times, h2d, d2h = [], 0, 0
+    for _ in range(args.e2e_steps):
+        torch.cuda.synchronize()
+        t0 = time.time()
+        with engine.Stepper(sim, family=fam) as s2:
+            s2.run(n_t)
+            tr = s2.read("traces")
+            fld = s2.read("szz" if sim._dims == 3 else "syy")
+            h2d, d2h = s2.transfer_bytes()
+        torch.cuda.synchronize()
+        e2e_times.append(time.time() - t0)
+    e2e_s = float(np.mean(e2e_times))
+    e2e = {"value": cells * n_t * world / e2e_s / 1e9, "unit": "Gcell/s", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "seconds_per_step": round(e2e_s, 4),
+           "path": "ts_create + ts_run + ts_read(traces, field) + ts_destroy"}
+    cpu = cpu_baseline(sim, name) if with_cpu and rank == 0 and world == 1 and not args.no_cpu_baseline else None
+    cfg = workload_config(name, sim)
+    cfg["parallelism"] = f"replicas x{world}" if world > 1 else "single GPU"
+    return {"metric": "Gcell-updates/s", "value": round(value, 3), "unit": "Gcell/s", "n_gpus": world,
+            "steps": steps, "warmup": warmup, "ms_per_step": round(ms / steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded numpy default_rng(0); no public dataset exists)", "config": cfg,
+            "roofline": roofline, "step_roofline": step_roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(launches), "clocks": clk.summary()}
+
+
+def fmc_record(args, steps, warmup):
     """Batched full-matrix capture: 64 shots x 3 phantoms (512x768, 768x768,
     1024x768) in one launch per kernel per step, against the per-shot loop
     (the regular stepper run once per shot, as the reference's shot loop does)."""
@@ -204,23 +333,36 @@ def run_fmc(args):
         with torch.cuda.stream(stream):
             flush.zero_()
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         one()
     torch.cuda.synchronize()
+    if b.status()[2] >= 0:
+        raise RuntimeError("fmc2d: unstable")
     launches0 = b.launch_count()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(0) as clk:
         start.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             one()
         end.record(stream)
         torch.cuda.synchronize()
     ms = start.elapsed_time(end)
     launches = b.launch_count() - launches0
-    value = cell_shots * n_t * args.steps / (ms / 1e3) / 1e9
+    value = cell_shots * n_t * steps / (ms / 1e3) / 1e9
     b.reset()
     k_ms = b.profile_steps(min(50, n_t))
     b.close()
+
+    # end to end: a batch created from the host models (uploads), run, every trace read back
+    torch.cuda.synchronize()
+    t0 = time.time()
+    with BatchStepper(sims, shots, **shape) as be:
+        be.run(n_t)
+        for q in range(len(sims)):
+            be.traces(q)
+        h2d, d2h = be.transfer_bytes()
+    torch.cuda.synchronize()
+    e2e_s = time.time() - t0
 
     # per-shot loop on a sample of shots of every phantom
     per_shot_s, sample = 0.0, 0
@@ -231,7 +373,6 @@ def run_fmc(args):
             st = engine.Stepper(sim, family=engine.WGSL2D)
         finally:
             sim._source_term, sim._n_src = saved
-        cells = int(np.prod(sim.grid_shape()))
         st.set_sources(sh[0])
         st.reset()
         st.run(n_t)
@@ -249,23 +390,37 @@ def run_fmc(args):
         st.close()
     loop_value = cell_shots * n_t / per_shot_s / 1e9
     peak, peak_kind = peaks()
-    line = {"metric": "Gcell-updates/s", "value": round(value, 3), "unit": "Gcell/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+    b_alg = 115.6
+    # stress launch: v 8, stresses 24 r/w, memory variables 72 r/w per cell-shot
+    # (coefficients shared by the shots); velocity launch: stresses 12, v 16
+    kb = {"stress": 8 + 24 + 72, "velocity": 12 + 16}
+    dom = 0 if k_ms[0] >= k_ms[1] else 1
+    kname = ["stress", "velocity"][dom]
+    dom_bytes = cell_shots * kb[kname]
+    achieved = dom_bytes / (k_ms[dom] / 1e3) / 1e9
+    return {"metric": "Gcell-updates/s", "value": round(value, 3), "unit": "Gcell/s", "n_gpus": 1,
+            "steps": steps, "warmup": warmup, "ms_per_step": round(ms / steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded numpy default_rng)",
             "config": {"workload": "fmc2d", "phantoms": [list(s.grid_shape()) for s in sims],
                        "shots_per_phantom": [int(sh.shape[0]) for sh in shots], "time_steps_per_step": n_t,
                        "launch_shape": shape, "autotune_ms": tune,
                        "l2": "256 MiB flush written after every batch (inside the timed region)"},
-            "kernel_ms": {"stress": round(k_ms[0], 4), "velocity": round(k_ms[1], 4)},
+            "roofline": {"kernel": f"batched {kname}", "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic("fmc2d", kname),
+                         "peak_kind": peak_kind, "bytes_per_launch": int(dom_bytes),
+                         "kernel_ms": {"stress": round(k_ms[0], 4), "velocity": round(k_ms[1], 4)}},
             "per_shot_loop": {"value": round(loop_value, 3), "unit": "Gcell/s",
                               "sample": f"{args.loop_shots} shots per phantom ({sample} total), extrapolated",
                               "path": "Stepper per phantom; per shot ts_set_sources + ts_reset + ts_run + ts_read"},
             "speedup_vs_per_shot_loop": round(value / loop_value, 3),
-            "step_roofline": {"b_alg_per_cell_update": 115.6, "achieved": round(value * 115.6, 1), "peak": peak,
-                              "unit": "GB/s", "frac": round(value * 115.6 / peak, 4), "peak_kind": peak_kind},
+            "step_roofline": {"b_alg_per_cell_update": b_alg, "achieved": round(value * b_alg, 1), "peak": peak,
+                              "unit": "GB/s", "frac": round(value * b_alg / peak, 4), "peak_kind": peak_kind},
+            "e2e": {"value": round(cell_shots * n_t / e2e_s / 1e9, 3), "unit": "Gcell/s",
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "seconds_per_step": round(e2e_s, 4),
+                    "path": "ts_batch_create + ts_batch_run + ts_batch_read_traces (every phantom) + ts_batch_destroy"},
             "gpu_launches": int(launches), "clocks": clk.summary()}
-    print(json.dumps(line))
 
 
 ADJ_BYTES = {
@@ -280,7 +435,7 @@ ADJ_BYTES = {
 }
 
 
-def run_adjoint(args):
+def adjoint_record(args, steps, warmup, with_cpu=False):
     """Adjoint gradient: 16 shots of a 512 x 1024 viscoelastic model (3000
     steps, 256 receivers), gradient of the L2 trace misfit w.r.t. per-cell
     lambda, mu, rho summed over shots, checkpointing every ceil(sqrt(3000))
@@ -347,14 +502,14 @@ def run_adjoint(args):
     segs = int(min(n_seg, max(1, args.adjoint_record_gb * 1e9 // seg_bytes)))
     with torch.cuda.stream(stream), AdjointProblem(start, checkpoint_every=ckpt, record_segments=segs) as prob:
         m = [t.clone().requires_grad_(True) for t in prob.material()]
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             gradient(prob, m)
         torch.cuda.synchronize()
         l0 = prob.launch_count()
         start_ev, end_ev = ev(), ev()
         with ClockSampler(0) as clk:
             start_ev.record(stream)
-            for _ in range(args.steps):
+            for _ in range(steps):
                 gradient(prob, m)
             end_ev.record(stream)
             torch.cuda.synchronize()
@@ -413,17 +568,17 @@ def run_adjoint(args):
         torch.cuda.synchronize()
         sweep_ms = a.elapsed_time(b)
 
-    t_grad_ms = ms / args.steps / n_shots
+    t_grad_ms = ms / steps / n_shots
     ratio = t_grad_ms / t_fwd_ms
-    value = cells * n_t * n_shots * args.steps / (ms / 1e3) / 1e9
+    value = cells * n_t * n_shots * steps / (ms / 1e3) / 1e9
     peak, peak_kind = peaks()
     adj_bytes = cells * ADJ_BYTES["adjoint_step"]
     achieved = adj_bytes / (sweep_ms / n_t / 1e3) / 1e9
-    cpu = None if args.no_cpu_baseline else cpu_baseline(start, "visco2d")
+    cpu = None if (args.no_cpu_baseline or not with_cpu) else cpu_baseline(start, "visco2d")
     if cpu:
         cpu["sample"] += "; the reference computes no gradient: this is its forward on the same grid"
     line = {"metric": "Gcell-updates/s", "value": round(value, 3), "unit": "Gcell/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+            "steps": steps, "warmup": warmup, "ms_per_step": round(ms / steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded numpy default_rng(0); no public dataset exists)",
             "config": {"workload": "adjoint2d", "grid": list(start.grid_shape()), "time_steps": n_t,
@@ -447,7 +602,7 @@ def run_adjoint(args):
                         "adjoint_step_ms": round(sweep_ms / n_t, 5)},
             "roofline": {"kernel": "adjoint step (k_adj_velocity + k_adj_stress)", "bound": "hbm",
                          "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
+                         "frac": round(achieved / peak, 4), "traffic": traffic("adjoint2d", "adjoint_step"), "peak_kind": peak_kind,
                          "bytes_per_launch_pair": int(adj_bytes)},
             "cpu_baseline": cpu,
             "e2e": {"value": cells * n_t * n_shots / e2e_s / 1e9, "unit": "Gcell/s", "h2d_bytes_per_step": int(h2d),
@@ -455,15 +610,22 @@ def run_adjoint(args):
                     "path": "material + observed traces from pinned host memory, 16 x (traces, misfit, "
                             "backward), gradient to host"},
             "gpu_launches": int(launches), "clocks": clk.summary()}
-    print(json.dumps(line))
+    return line
+
+
+# Sub-records of the default line: (bench steps, warm-up steps) of each
+# workload, sized so that the whole default run takes a few minutes.
+SUB_RECORDS = {"elastic2d": (20, 3), "visco3d": (5, 3), "fmc2d": (2, 3), "adjoint2d": (1, 3)}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="visco2d", choices=sorted(workloads.WORKLOADS) + ["fmc2d", "adjoint2d"])
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--workload", default=None, choices=sorted(workloads.WORKLOADS) + ["fmc2d", "adjoint2d"],
+                    help="one workload alone (default: visco2d, with every other workload as a sub-record)")
+    ap.add_argument("--no-sub", action="store_true", help="default run without the sub-records")
     ap.add_argument("--loop-shots", type=int, default=4, help="fmc2d: shots per phantom timed in the per-shot loop")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ref-sample-steps", type=int, default=200)
@@ -480,124 +642,38 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
-    if args.workload == "fmc2d":
-        return run_fmc(args)
-    if args.workload == "adjoint2d":
-        return run_adjoint(args)
 
     import torch
-    from taichi_sim_gb300 import engine, shards
-
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    if args.workload == "fmc2d":
+        print(json.dumps(fmc_record(args, args.steps, args.warmup)))
+        return
+    if args.workload == "adjoint2d":
+        print(json.dumps(adjoint_record(args, args.steps, args.warmup, with_cpu=True)))
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-
-    name = args.workload
-    sim = build_model(name, args.time_steps)
-    n_t = int(sim._n_steps)
-    cells = int(np.prod(sim.grid_shape()))
-    fam = getattr(engine, FAMILY[name])
-    st = engine.Stepper(sim, family=fam)
-    stream = torch.cuda.Stream()
-    h = stream.cuda_stream
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-
-    def one_simulation():
-        st.reset(stream=h, wait=False)
-        st.run(n_t, stream=h)
-        with torch.cuda.stream(stream):
-            flush.zero_()
-
-    for _ in range(args.warmup):
-        one_simulation()
-    torch.cuda.synchronize()
-    _, _, bad = st.status()
-    if bad >= 0:
-        raise RuntimeError(f"workload unstable at step {bad}")
-    launches0 = st.launch_count()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        start.record(stream)
-        for _ in range(args.steps):
-            one_simulation()
-        end.record(stream)
-        torch.cuda.synchronize()
-    launches = st.launch_count() - launches0
-    ms = start.elapsed_time(end)
-    ms = shards.max_over_ranks(ms, device="cuda")   # the job's time: its slowest replica
-    ms_per_step = ms / args.steps
-    value = cells * n_t * args.steps * world / (ms / 1e3) / 1e9
-    clocks = clk.summary()
-
-    # ---- roofline of the dominant kernel (single launches between events) ----
-    st.reset()
-    k_ms = st.profile_steps(min(args.profile_steps, n_t), stream=h)
-    kb = KERNEL_BYTES[name]
-    frac = strip_fraction(sim)
-    strip_share = sum(frac) / len(frac)
-    bytes_stress = cells * (kb["stress"] + kb["psi_stress"] * 2 * strip_share)
-    bytes_vel = cells * (kb["velocity"] + kb["psi_vel"] * 2 * strip_share)
-    peak, peak_kind = peaks()
-    dom = 0 if k_ms[0] >= k_ms[1] else 1
-    dom_bytes = [bytes_stress, bytes_vel][dom]
-    achieved = dom_bytes / (k_ms[dom] / 1e3) / 1e9
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", f"traffic_{name}.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get(["stress", "velocity"][dom])
-    roofline = {"kernel": ["stress", "velocity"][dom], "bound": "hbm", "achieved": round(achieved, 1),
-                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
-                "peak_kind": peak_kind, "bytes_per_launch": int(dom_bytes),
-                "kernel_ms": {"stress": round(k_ms[0], 5), "velocity": round(k_ms[1], 5)}}
-    b_alg = workloads.B_ALG[name]
-    step_roofline = {"b_alg_per_cell_update": b_alg, "achieved": round(value * b_alg, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(value * b_alg / peak, 4),
-                     "note": "whole time step (both kernels) at the benchmark's algorithmic bytes per cell-update"}
-
-    # ---- end to end through the C ABI with host buffers ----
-    e2e_times, h2d, d2h = [], 0, 0
-    st.close()
-    for _ in range(args.e2e_steps):
-        torch.cuda.synchronize()
-        t0 = time.time()
-        with engine.Stepper(sim, family=fam) as s2:
-            s2.run(n_t)
-            tr = s2.read("traces")
-            fld = s2.read("szz" if sim._dims == 3 else "syy")
-            h2d, _ = s2.transfer_bytes()
-        torch.cuda.synchronize()
-        e2e_times.append(time.time() - t0)
-        d2h = tr.nbytes + fld.nbytes
-    e2e_s = float(np.mean(e2e_times))
-    e2e = {"value": cells * n_t * world / e2e_s / 1e9, "unit": "Gcell/s", "h2d_bytes_per_step": int(h2d),
-           "d2h_bytes_per_step": int(d2h), "seconds_per_step": round(e2e_s, 4),
-           "path": "ts_create + ts_run + ts_read(traces, field) + ts_destroy"}
-
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(sim, name)
-
+    name = args.workload or "visco2d"
+    line = stepper_record(name, args, args.steps, args.warmup, world, rank, local, dist, with_cpu=True)
+    if args.workload is None and world == 1 and not args.no_sub:
+        # every other benchmark target, measured in the same run with its own
+        # CUDA-event timing, rooflines, clocks and end-to-end figure
+        subs = {}
+        for sub, (k, w) in SUB_RECORDS.items():
+            if sub == "fmc2d":
+                subs[sub] = fmc_record(args, k, w)
+            elif sub == "adjoint2d":
+                subs[sub] = adjoint_record(args, k, w)
+            else:
+                subs[sub] = stepper_record(sub, args, k, w)
+            torch.cuda.empty_cache()
+        line["workloads"] = subs
     if rank == 0:
-        line = {"metric": "Gcell-updates/s", "value": round(value, 3), "unit": "Gcell/s", "n_gpus": world,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic (seeded numpy default_rng(0); no public dataset exists)",
-                "config": {"workload": name, "grid": list(sim.grid_shape()), "time_steps_per_step": n_t,
-                           "family": FAMILY[name], "receivers": int(sim._n_rec),
-                           "zener": "L=3 fitted 2-8 MHz, per-cell Q" if name != "elastic2d" else None,
-                           "l2": "256 MiB flush written after every simulation (inside the timed region)",
-                           "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-                "roofline": roofline, "step_roofline": step_roofline, "cpu_baseline": cpu, "e2e": e2e,
-                "gpu_launches": int(launches), "clocks": clocks}
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

@@ -210,6 +210,8 @@ int ts_batch_read_traces(ts_batch *b, int32_t phantom, void *host_dst, size_t by
 int ts_batch_read_field(ts_batch *b, int32_t phantom, int32_t what, void *host_dst, size_t bytes);
 int ts_batch_profile_steps(ts_batch *b, int32_t n_steps, void *stream, float *ms_per_kernel);
 int ts_batch_launch_count(const ts_batch *b, int64_t *launches);
+/* bytes this batch has copied host->device (creation, sources) and device->host */
+int ts_batch_transfer_bytes(const ts_batch *b, int64_t *h2d, int64_t *d2h);
 void ts_batch_destroy(ts_batch *b);
 const char *ts_batch_last_error(void);
 

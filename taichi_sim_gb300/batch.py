@@ -46,6 +46,8 @@ def _bind(lib):
         "ts_batch_read_field": ([P, ctypes.c_int32, ctypes.c_int32, P, ctypes.c_size_t], ctypes.c_int),
         "ts_batch_profile_steps": ([P, ctypes.c_int32, P, _f], ctypes.c_int),
         "ts_batch_launch_count": ([P, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+        "ts_batch_transfer_bytes": ([P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)],
+                                    ctypes.c_int),
         "ts_batch_destroy": ([P], None),
         "ts_batch_last_error": ([], ctypes.c_char_p),
     }
@@ -253,6 +255,13 @@ class BatchStepper:
         n = ctypes.c_int64()
         _check(self._lib, self._lib.ts_batch_launch_count(self._h, ctypes.byref(n)), "ts_batch_launch_count")
         return n.value
+
+    def transfer_bytes(self):
+        """``(host->device, device->host)`` bytes this batch has copied so far."""
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        _check(self._lib, self._lib.ts_batch_transfer_bytes(self._h, ctypes.byref(a), ctypes.byref(b)),
+               "ts_batch_transfer_bytes")
+        return a.value, b.value
 
     def close(self):
         if getattr(self, "_h", None):

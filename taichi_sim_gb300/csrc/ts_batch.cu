@@ -677,7 +677,7 @@ struct ts_batch {
     int device = 0, ord = 2, spt = 1, zen_mode = 0, rows = 0;
     int cy[2] = {8, 8}, tx[2] = {2, 2}, n_blocks[2] = {0, 0};  // stress, velocity launch shapes
     int steps_done = 0, n_ph = 0;
-    int64_t launches = 0;
+    int64_t launches = 0, h2d_bytes = 0, d2h_bytes = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
     cudaGraphExec_t graph = nullptr;
@@ -704,6 +704,7 @@ struct ts_batch {
         if (rc) return rc;
         if (!h.empty() && cudaMemcpy(*ptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
             return bfail(TS_E_CUDA, "cudaMemcpy");
+        h2d_bytes += (int64_t)(h.size() * sizeof(T));
         return TS_OK;
     }
 };
@@ -1023,6 +1024,7 @@ int ts_batch_read_traces(ts_batch *b, int32_t phantom, void *dst, size_t bytes) 
     if (bytes < need) return bfail(TS_E_ARG, "destination too small");
     if (need && cudaMemcpy(dst, b->ph[phantom].traces, need, cudaMemcpyDeviceToHost) != cudaSuccess)
         return bfail(TS_E_CUDA, "cudaMemcpy");
+    b->d2h_bytes += (int64_t)need;
     return TS_OK;
 }
 
@@ -1038,6 +1040,7 @@ int ts_batch_read_field(ts_batch *b, int32_t phantom, int32_t what, void *dst, s
     // device layout [S/W][nx][ny][W] -> host [n_shots][nx][ny]
     std::vector<float> tmp((size_t)h.G);
     if (cudaMemcpy(tmp.data(), src, tmp.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return bfail(TS_E_CUDA, "cudaMemcpy");
+    b->d2h_bytes += (int64_t)(tmp.size() * 4);
     float *o = static_cast<float *>(dst);
     const int64_t cells = (int64_t)h.nx * h.ny;
     for (int s = 0; s < h.n_shots; ++s)
@@ -1079,6 +1082,13 @@ int ts_batch_profile_steps(ts_batch *b, int32_t n_steps, void *stream, float *ms
 int ts_batch_launch_count(const ts_batch *b, int64_t *n) {
     if (!b || !n) return bfail(TS_E_ARG, "null argument");
     *n = b->launches;
+    return TS_OK;
+}
+
+int ts_batch_transfer_bytes(const ts_batch *b, int64_t *h2d, int64_t *d2h) {
+    if (!b) return bfail(TS_E_ARG, "null handle");
+    if (h2d) *h2d = b->h2d_bytes;
+    if (d2h) *d2h = b->d2h_bytes;
     return TS_OK;
 }
 

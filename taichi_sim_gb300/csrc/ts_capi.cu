@@ -235,6 +235,53 @@ void ts_destroy(ts_sim *s) {
     delete s;
 }
 
+// Index of the first non-finite value of a float table, or -1.  (Exponent
+// bits all set: Inf or NaN; the loop vectorises.)
+static int64_t first_non_finite(const float *a, int64_t n) {
+    const uint32_t *u = reinterpret_cast<const uint32_t *>(a);
+    uint32_t any = 0;
+    for (int64_t i = 0; i < n; ++i) any |= ((u[i] & 0x7f800000u) == 0x7f800000u);
+    if (!any) return -1;
+    for (int64_t i = 0; i < n; ++i)
+        if ((u[i] & 0x7f800000u) == 0x7f800000u) return i;
+    return -1;
+}
+
+// Material, coefficients and CPML tables must be finite.  The reference
+// does not check them: a NaN there turns the wavefield into NaN, which its
+// `norm > threshold` stability test never catches.
+static int check_finite(const ts_desc *d, int dims) {
+    const int64_t cells = (int64_t)d->nx * d->ny * (dims == 3 ? d->nz : 1);
+    struct {
+        const char *name;
+        const float *a;
+        int64_t n;
+    } tabs[] = {
+        {"rho", d->rho, cells}, {"cp", d->cp, cells}, {"cs", d->cs, cells},
+        {"coefs", d->coefs, d->ord},
+        {"a_x", d->a_x, d->nx - 2 * (d->ord - 1)}, {"b_x", d->b_x, d->nx - 2 * (d->ord - 1)},
+        {"k_x", d->k_x, d->nx - 2 * (d->ord - 1)}, {"a_x_half", d->a_xh, d->nx - 2 * (d->ord - 1)},
+        {"b_x_half", d->b_xh, d->nx - 2 * (d->ord - 1)}, {"k_x_half", d->k_xh, d->nx - 2 * (d->ord - 1)},
+        {"a_y", d->a_y, d->ny - 2 * (d->ord - 1)}, {"b_y", d->b_y, d->ny - 2 * (d->ord - 1)},
+        {"k_y", d->k_y, d->ny - 2 * (d->ord - 1)}, {"a_y_half", d->a_yh, d->ny - 2 * (d->ord - 1)},
+        {"b_y_half", d->b_yh, d->ny - 2 * (d->ord - 1)}, {"k_y_half", d->k_yh, d->ny - 2 * (d->ord - 1)},
+        {"a_z", dims == 3 ? d->a_z : nullptr, d->nz - 2 * (d->ord - 1)},
+        {"b_z", dims == 3 ? d->b_z : nullptr, d->nz - 2 * (d->ord - 1)},
+        {"k_z", dims == 3 ? d->k_z : nullptr, d->nz - 2 * (d->ord - 1)},
+        {"a_z_half", dims == 3 ? d->a_zh : nullptr, d->nz - 2 * (d->ord - 1)},
+        {"b_z_half", dims == 3 ? d->b_zh : nullptr, d->nz - 2 * (d->ord - 1)},
+        {"k_z_half", dims == 3 ? d->k_zh : nullptr, d->nz - 2 * (d->ord - 1)},
+        {"g_p", d->visco ? d->g_p : nullptr, cells}, {"g_s", d->visco ? d->g_s : nullptr, cells},
+    };
+    for (const auto &t : tabs) {
+        if (!t.a) continue;
+        const int64_t i = first_non_finite(t.a, t.n);
+        if (i >= 0)
+            return fail(TS_E_ARG, std::string("non-finite value in ") + t.name + " at flat index " + std::to_string(i));
+    }
+    return TS_OK;
+}
+
 static int validate(const ts_desc *d) {
     if (!d) return fail(TS_E_ARG, "null descriptor");
     if (d->abi_version != TS_ABI_VERSION) return fail(TS_E_ARG, "abi_version mismatch");
@@ -265,7 +312,7 @@ static int validate(const ts_desc *d) {
     if (d->n_rec > 0 && d->family == TS_TAICHI2D && !d->pos_sensors) return fail(TS_E_ARG, "missing sensor map");
     if (d->n_rec > 0 && d->family != TS_TAICHI2D && (!d->info_rec_pt || !d->offset_sensors))
         return fail(TS_E_ARG, "missing receiver point table");
-    return TS_OK;
+    return check_finite(d, dims);
 }
 
 int ts_create(const ts_desc *d, ts_sim **out) {

@@ -211,3 +211,27 @@ def test_noalloc_empty_lists_need_no_tables(lib):
         engine.run_noalloc_2d(a)
     except RuntimeError as e:
         assert "invalid argument" not in str(e)
+
+
+@pytest.mark.parametrize("attr,value,needle", [
+    ("_rho_grid_vx", np.nan, "rho"),
+    ("_cp_grid_vx", np.inf, "cp"),
+    ("_cs_grid_vx", -np.inf, "cs"),
+    ("_a_x", np.nan, "a_x"),
+    ("_k_y_half", np.inf, "k_y_half"),
+    ("_inv_qp_grid", np.nan, "g_p"),
+])
+def test_create_rejects_non_finite_tables(lib, attr, value, needle):
+    """A NaN or Inf in the material, CPML or per-cell Q tables is refused by
+    ts_create before any device work (the reference would run and fill the
+    wavefield with NaN, which its stability test does not catch)."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from _cases import case_2d
+    from taichi_sim_gb300.sim_support.simulator import Simulator
+    sim = Simulator(case_2d(visco=1, q=(30.0, 200.0), seed=1, steps=20))
+    a = np.array(getattr(sim, attr), dtype=np.float32, copy=True)
+    a.flat[a.size // 2] = value
+    setattr(sim, attr, a)
+    with pytest.raises(engine.TsError, match=f"non-finite value in {needle} at flat index"):
+        engine.Stepper(sim)

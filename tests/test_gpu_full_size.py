@@ -1,0 +1,145 @@
+"""GPU parity at the benchmark workloads' full grid sizes, and against the
+reference's own known-answer B-scan.
+
+The small parity cases (test_gpu_parity.py) cover every code path; these
+cover what only shows at size: 32-bit offset paths, the share of warps that
+take the interior sweep, the 3D coefficient palette of a full model, the
+batched layout of 64 shots, long-run error growth.  Every comparison goes
+through the C ABI (``ts_create``/``ts_run``/``ts_read``, ``ts_batch_*``,
+``ts_adj_*``) and checks fields and traces against the float CPU oracle
+within relative L2 1e-5, the parity tolerance.  Time steps are bounded where
+the oracle would take minutes (3D: 64 steps; batched and adjoint: 300), and
+the tests are ordered and named by workload.
+
+``test_golden_teste_pedro`` runs the reference's own experiment
+``pedro/teste_pedro.json`` (725 x 572 nodes, 10000 steps, 64 receivers)
+with the Taichi semantics (sim_taichi_elastic.py:311-351) and compares the
+traces with the B-scan the reference shipped
+(``pedro/results/result_teste_aco.npy``, a Taichi GPU run with fast math):
+relative L2 <= 1e-5 (the float oracle reaches 7.4e-6 over the same 10000
+steps), the same first non-zero row (335) and the same arrival row of the
+largest sample in every column.
+"""
+import numpy as np
+import pytest
+
+from _cases import rel_l2
+from _golden import config_with_maps, golden_bscan
+from oracle import oracle
+from taichi_sim_gb300 import engine, workloads
+from taichi_sim_gb300.sim_support.simulator import Simulator
+from taichi_sim_gb300.sim_support.Simulator3D import Simulator3D
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+F2 = ("vx", "vy", "sxx", "syy", "sxy")
+F3 = ("vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "sxz", "syz")
+
+
+def test_golden_teste_pedro():
+    dims, cfg = config_with_maps("teste_pedro")
+    sim = Simulator(cfg)
+    assert sim.grid_shape() == (725, 572) and sim._n_steps == 10000
+    with engine.Stepper(sim, family=engine.TAICHI2D) as st:
+        st.simulate()
+        tr = st.read("traces")
+    g = golden_bscan()
+    assert tr.shape == g.shape
+    err = rel_l2(tr, g)
+    assert int(np.nonzero(np.abs(tr).sum(1))[0][0]) == 335
+    assert err <= TOL, err
+    np.testing.assert_array_equal(np.argmax(np.abs(tr), axis=0), np.argmax(np.abs(g), axis=0))
+    assert np.isclose(np.abs(tr).max(), np.abs(g).max(), rtol=1e-4)
+
+
+def _check_stepper(sim, family, names, n_steps):
+    fam_oracle = {engine.TAICHI2D: oracle.TAICHI2D, engine.WGSL2D: oracle.WGSL2D, engine.WGSL3D: oracle.WGSL3D}[family]
+    with engine.Stepper(sim, family=family) as st:
+        st.run(n_steps)
+        n, vmax, bad = st.status()
+        assert n == n_steps and bad == -1
+        got = {k: st.read(k) for k in names}
+        tr = st.read("traces")[:n_steps]
+    ref = oracle.run(sim, fam_oracle, n_steps=n_steps)
+    errs = {k: rel_l2(got[k], ref[k]) for k in names}
+    errs["traces"] = rel_l2(tr, ref["sens"])
+    for k in names:
+        assert np.abs(ref[k]).max() > 0, k
+    assert np.abs(ref["sens"]).max() > 0, "nothing recorded"
+    assert max(errs.values()) <= TOL, errs
+    # gated samples stay exactly zero
+    np.testing.assert_array_equal(tr[ref["sens"] == 0] != 0, False)
+    return errs
+
+
+def test_full_elastic2d_512_2000_steps():
+    sim = Simulator(workloads.elastic2d_512())
+    assert sim.grid_shape() == (512, 512)
+    _check_stepper(sim, engine.TAICHI2D, F2, 2000)
+
+
+def test_full_visco2d_1024_4000_steps():
+    sim = Simulator(workloads.visco2d_1024())
+    assert sim.grid_shape() == (1024, 1024)
+    _check_stepper(sim, engine.WGSL2D, F2, 4000)
+
+
+@pytest.mark.parametrize("palette", ["1", "0"], ids=["palette", "arrays"])
+def test_full_visco3d_256_64_steps(palette, monkeypatch):
+    monkeypatch.setenv("TS_3D_COEF_PALETTE", palette)
+    sim = Simulator3D(workloads.visco3d_256())
+    assert sim.grid_shape() == (256, 256, 256)
+    _check_stepper(sim, engine.WGSL3D, F3, 64)
+
+
+def _with_shot(sim, table, fn):
+    """Run fn with the model's source term replaced by one shot's table (the
+    stride the kernels read is the table's width)."""
+    saved = sim._source_term, sim._n_src
+    sim._source_term, sim._n_src = table, table.shape[1]
+    try:
+        return fn()
+    finally:
+        sim._source_term, sim._n_src = saved
+
+
+def test_full_fmc2d_three_phantoms_300_steps():
+    """The batched launch over 64 shots of each of the three full-size
+    phantoms; shots 0 and 63 of each against the oracle run on that shot."""
+    from taichi_sim_gb300.batch import BatchStepper, fmc_shot_sources
+    n_t = 300
+    sims = [Simulator(c) for c in workloads.fmc2d_phantoms(n_steps=n_t)]
+    shots = [fmc_shot_sources(s) for s in sims]
+    assert [s.grid_shape() for s in sims] == [(512, 768), (768, 768), (1024, 768)]
+    assert [sh.shape[0] for sh in shots] == [64, 64, 64]
+    with BatchStepper(sims, shots) as b:
+        b.run(n_t)
+        n, _, bad = b.status()
+        assert n == n_t and bad == -1
+        got = [(b.traces(q), b.field(q, "syy")) for q in range(len(sims))]
+    for q, sim in enumerate(sims):
+        for s in (0, 63):
+            ref = _with_shot(sim, shots[q][s], lambda: oracle.run(sim, oracle.WGSL2D, n_steps=n_t))
+            assert np.abs(ref["sens"]).max() > 0
+            e_tr, e_f = rel_l2(got[q][0][s], ref["sens"]), rel_l2(got[q][1][s], ref["syy"])
+            assert e_tr <= TOL and e_f <= TOL, (q, s, e_tr, e_f)
+
+
+def test_full_adjoint2d_512x1024_forward_300_steps():
+    """The adjoint's forward (checkpointed, through ts_adj_forward) on the
+    full 512 x 1024 model, one shot, against the oracle."""
+    import torch
+    from taichi_sim_gb300.adjoint import AdjointProblem
+    from taichi_sim_gb300.batch import fmc_shot_sources
+    n_t = 300
+    sim = Simulator(workloads.adjoint2d_512x1024(n_steps=n_t))
+    assert sim.grid_shape() == (512, 1024)
+    table = fmc_shot_sources(sim)[5]
+    with AdjointProblem(sim, checkpoint_every=int(np.ceil(np.sqrt(n_t)))) as prob:
+        prob.set_source_term(table)
+        with torch.no_grad():
+            tr = prob.traces(*prob.material()).cpu().numpy()
+    ref = _with_shot(sim, table, lambda: oracle.run(sim, oracle.WGSL2D, n_steps=n_t))
+    assert np.abs(ref["sens"]).max() > 0
+    assert rel_l2(tr, ref["sens"]) <= TOL, rel_l2(tr, ref["sens"])

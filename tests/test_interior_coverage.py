@@ -21,6 +21,6 @@ def test_2d_cases_have_interior_warps(name):
 
 def test_3d_cases_have_interior_warps():
     deep = [n for n in CASES_3D if interior_warps(Simulator3D(CASES_3D[n]()), 4) > 0]
-    assert sorted(deep) == ["wgsl3d_acc4_deep", "wgsl3d_visco_deep"]
+    assert sorted(deep) == ["wgsl3d_acc4_deep", "wgsl3d_acc6_visco", "wgsl3d_visco_deep"]
     for n in deep:
         assert interior_warps(Simulator3D(CASES_3D[n]()), 2) > 0

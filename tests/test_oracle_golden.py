@@ -42,6 +42,29 @@ def test_oracle_reproduces_golden_bscan(pedro):
     np.testing.assert_array_equal(np.argmax(np.abs(s), axis=0), np.argmax(np.abs(g), axis=0))
 
 
+def test_wgsl_oracle_reproduces_golden_bscan(pedro):
+    """Cross-family pin: the WGSL 2D restatement (shader_webgpu_viscoelastic.wgsl
+    :829-1072, receivers :1118-1134) with attenuation off, on the same
+    teste_pedro tables, against the Taichi-made golden B-scan.
+
+    The two backends differ only where the reference's own code differs
+    (Dirichlet zeroing of both velocities outside the vy region against each
+    component outside its own, the WGSL receiver gate ``it >= delay`` on the
+    0-based step against Taichi's 1-based one, ``/dx`` against ``* (1/dx)``
+    and ``(l+2m) d + l d'`` against ``l div + 2m d``).  On this experiment
+    the receivers' delay is 1 step and the signal starts at row 335, so the
+    gate change touches only silent rows and no row shift appears: the
+    bound is the same order as the Taichi restatement's own."""
+    out = oracle.run(pedro, oracle.WGSL2D, n_steps=N_STEPS, visco=False)
+    g = golden_bscan()[:N_STEPS]
+    s = out["sens"]
+    assert int(np.nonzero(np.abs(s).sum(1))[0][0]) == 335
+    assert rel_l2(s, g) < 2e-6
+    np.testing.assert_array_equal(np.argmax(np.abs(s), axis=0), np.argmax(np.abs(g), axis=0))
+    # a one-row shift would cost six orders of magnitude: the rows align
+    assert rel_l2(s[1:], g[:-1]) > 1e-2
+
+
 def test_oracle_float_error_is_small(pedro):
     """The float oracle's own rounding error against its double run."""
     a = oracle.run(pedro, oracle.TAICHI2D, n_steps=500)
