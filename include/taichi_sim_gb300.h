@@ -54,6 +54,7 @@ extern "C" {
 #define TS_E_NOMEM 3      /* device allocation failed */
 #define TS_E_NODEV 4      /* no usable sm_103 device */
 #define TS_E_STATE 5      /* call not valid in the handle's state */
+#define TS_E_TIMEOUT 6    /* a bounded wait between thread blocks gave up (state invalid until ts_reset) */
 
 /* kernel families: which reference backend's semantics to follow */
 #define TS_TAICHI2D 0     /* sim_taichi_elastic.py:138-309 (2D elastic) */
@@ -162,8 +163,19 @@ int ts_transfer_bytes(const ts_sim *sim, int64_t *h2d, int64_t *d2h);
  * by a caller on the same device. */
 int ts_device_buffer(ts_sim *sim, int32_t what, void **dev_ptr, size_t *pitch_bytes);
 
-/* Number of kernel launches one time step issues (for launch accounting). */
+/* Number of kernel launches one time step issues (for launch accounting;
+ * the persistent path issues its launches per ts_run call instead). */
 int ts_launches_per_step(const ts_sim *sim, int32_t *launches);
+
+/* How ts_run advances this handle: TS_PATH_STEPPED, the step's kernels
+ * launched once per time step (replayed from a CUDA graph), or
+ * TS_PATH_PERSISTENT, every step of the call in one cooperative launch that
+ * keeps the wavefield on chip (2D elastic models of order 2 whose row slabs
+ * fit shared memory; TS_2D_PERSISTENT=0 in the environment at ts_create
+ * turns it off).  Both give the same bits. */
+#define TS_PATH_STEPPED 0
+#define TS_PATH_PERSISTENT 1
+int ts_step_path(const ts_sim *sim, int32_t *path);
 
 void ts_destroy(ts_sim *sim);
 

@@ -114,6 +114,10 @@ struct ts_sim {
     std::vector<size_t> state_bytes;
     std::vector<void *> state_ptrs;
     StepParams p{};
+    // persistent path (2D elastic, order 2; ts_persist2d.cu)
+    int persist = 0, p_rows = 0, p_blocks = 0, p_threads = 0;
+    size_t p_smem = 0;
+    ts::PersistArgs pa{};
 
     template <typename T>
     int alloc(T **ptr, size_t count, bool state) {
@@ -214,6 +218,7 @@ const char *ts_strerror(int code) {
     case TS_E_NOMEM: return "device memory exhausted";
     case TS_E_NODEV: return "no usable sm_103 device";
     case TS_E_STATE: return "invalid state";
+    case TS_E_TIMEOUT: return "wait between thread blocks timed out";
     default: return "unknown error";
     }
 }
@@ -384,6 +389,9 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     const float steps[3] = {d->dx, d->dy, d->dz};
     for (int a = 0; a < 3; ++a)
         for (int c = 0; c < ts::kMaxOrd; ++c) p.cd[a][c] = c < ord ? d->coefs[c] / steps[a] : 0.f;
+    for (int c = 0; c < ts::kMaxOrd; ++c) p.coef[c] = c < ord ? d->coefs[c] : 0.f;
+    for (int a = 0; a < 3; ++a) p.od[a] = steps[a] > 0.f ? 1.f / steps[a] : 0.f;
+    p.dt = d->dt;
 
     // ---- CPML tables and strips ----
     Axis axes[3];
@@ -443,11 +451,19 @@ int ts_create(const ts_desc *d, ts_sim **out) {
             for (int y = 0; y < ny; ++y) {
                 const int64_t i = s->at(x, y);
                 const ts::Coef2D c = ts::coef_2d(d, x, y);
-                lam[i] = c.lam;
-                mu[i] = c.mu;
-                mus[0][i] = c.mus;
-                dtr0[i] = c.dtr_vx;
-                dtr1[i] = c.dtr_vy;
+                if (s->family == TS_TAICHI2D) {   // the kernels keep the reference's operation order
+                    lam[i] = c.lam_raw;
+                    mu[i] = c.mu_raw;
+                    mus[0][i] = c.mus_raw;
+                    dtr0[i] = c.rho_vx;
+                    dtr1[i] = c.rho_vy;
+                } else {
+                    lam[i] = c.lam;
+                    mu[i] = c.mu;
+                    mus[0][i] = c.mus;
+                    dtr0[i] = c.dtr_vx;
+                    dtr1[i] = c.dtr_vy;
+                }
             }
     } else {
         for (int x = 0; x < nx; ++x)
@@ -539,6 +555,11 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         return s->dims == 2 ? ts::block_of_2d(p, x, y) : ts::block_of_3d(p, x, y, z);
     };
 
+    // host copies the persistent path rebuilds its own lists from
+    std::vector<Source> src_list_h;
+    std::vector<int> rec_start_h;
+    std::vector<int64_t> rec_cells_h;
+
     // ---- sources ----
     {
         s->src_rows = d->src_rows;
@@ -566,15 +587,16 @@ int ts_create(const ts_desc *d, ts_sim **out) {
                         r = 0.5f * (rho(x, y + 1, z) + rho(x, y, z));
                     }
                     if (!(r > 0.f)) continue;
+                    const float scale = s->family == TS_TAICHI2D ? r : dt / r;
                     if (!col_of.count(idx)) {
                         const int c = (int)col_of.size();
                         col_of[idx] = c;
                         s->src_col_idx.push_back(idx);
                     }
-                    cands.push_back({block_of(x, y, z), Source{s->at(x, y, z), col_of[idx], dt / r}});
+                    cands.push_back({block_of(x, y, z), Source{s->at(x, y, z), col_of[idx], scale}});
                 }
         std::stable_sort(cands.begin(), cands.end(), [](const Cand &a, const Cand &b) { return a.blk < b.blk; });
-        std::vector<Source> list;
+        std::vector<Source> &list = src_list_h;
         std::vector<int> start(s->n_blocks + 1, 0);
         for (const Cand &c : cands) {
             list.push_back(c.s);
@@ -626,6 +648,8 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         int *ds = nullptr, *df = nullptr;
         int64_t *dc = nullptr;
         if ((rc = s->upload(&ds, start)) || (rc = s->upload(&df, first)) || (rc = s->upload(&dc, cells))) return bail(rc);
+        rec_start_h = start;
+        rec_cells_h = cells;
         p.n_rec = d->n_rec;
         p.rec_start = ds;
         p.rec_first_step = df;
@@ -642,6 +666,64 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     p.block_max = s->block_max;
     p.first_bad = s->first_bad;
     p.step_base = s->step_base;
+
+    // ---- persistent path: 2D elastic order-2 models whose row slabs fit on chip ----
+    if (s->dims == 2) {
+        const char *env = getenv("TS_2D_PERSISTENT");
+        int rows = 0, blocks = 0, threads = 0;
+        size_t smem = 0;
+        if (!(env && env[0] == '0') &&
+            ts::persist_2d_plan(s->family, ord, s->zen_mode, nx, ny, p.strip[1].width, prop.multiProcessorCount,
+                                &rows, &blocks, &threads, &smem)) {
+            ts::PersistArgs &a = s->pa;
+            constexpr int NH = 3;   // 2 ORD - 1 edge rows per side
+            const int64_t n_pts = (int64_t)rec_cells_h.size();
+            if ((rc = s->alloc(&a.mail, (size_t)blocks * 2 * 2 * 2 * NH * threads, false)) ||
+                (rc = s->alloc(&a.flags, blocks, true)) || (rc = s->alloc(&a.err, 4, true)) ||
+                (rc = s->alloc(&a.samples, (size_t)s->n_rows * std::max<int64_t>(n_pts, 1), false)))
+                return bail(rc);
+            // receiver points and source nodes, each by the block whose slab holds its row
+            std::vector<std::vector<int4>> by_pt(blocks), by_src(blocks);
+            for (int64_t q = 0; q < n_pts; ++q) {
+                const int x = (int)(rec_cells_h[q] / s->pitch), y = (int)(rec_cells_h[q] % s->pitch);
+                by_pt[x / rows].push_back(make_int4(x % rows, y, (int)q, 0));
+            }
+            for (const Source &src : src_list_h) {
+                const int x = (int)(src.cell / s->pitch), y = (int)(src.cell % s->pitch);
+                int bits;
+                std::memcpy(&bits, &src.scale, 4);
+                by_src[x / rows].push_back(make_int4(x % rows, y, src.col, bits));
+            }
+            std::vector<int4> pts, srcs;
+            std::vector<int> pts_start(1, 0), src_start(1, 0);
+            for (int b = 0; b < blocks; ++b) {
+                pts.insert(pts.end(), by_pt[b].begin(), by_pt[b].end());
+                srcs.insert(srcs.end(), by_src[b].begin(), by_src[b].end());
+                pts_start.push_back((int)pts.size());
+                src_start.push_back((int)srcs.size());
+            }
+            int4 *dpts = nullptr, *dsrcs = nullptr;
+            int *dps = nullptr, *dss = nullptr;
+            if ((rc = s->upload(&dpts, pts)) || (rc = s->upload(&dps, pts_start)) || (rc = s->upload(&dsrcs, srcs)) ||
+                (rc = s->upload(&dss, src_start)))
+                return bail(rc);
+            a.pts = dpts;
+            a.pts_start = dps;
+            a.srcs = dsrcs;
+            a.src_start = dss;
+            a.n_pts = (int)n_pts;
+            a.n_blocks = s->n_blocks;
+            a.wait_ns = 1000000000LL;   // 1 s
+            if (const char *w = getenv("TS_PERSIST_WAIT_NS")) a.wait_ns = std::max(1000LL, atoll(w));
+            a.stall_block = -1;
+            if (const char *b = getenv("TS_PERSIST_STALL_BLOCK")) a.stall_block = atoi(b);
+            s->persist = 1;
+            s->p_rows = rows;
+            s->p_blocks = blocks;
+            s->p_threads = threads;
+            s->p_smem = smem;
+        }
+    }
 
     cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
@@ -702,6 +784,42 @@ int ts_profile_steps(ts_sim *s, int32_t n_steps, void *stream, float *ms_per_ker
         return fail(TS_E_ARG, "steps beyond the source/trace length");
     TS_CUDA(cudaSetDevice(s->device));
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : s->stream;
+    if (s->persist) {   // one launch for all steps: [0] its time per step, [1] the receiver sums' per step
+        cudaEvent_t e0, e1, e2;
+        TS_CUDA(cudaEventCreate(&e0));
+        TS_CUDA(cudaEventCreate(&e1));
+        TS_CUDA(cudaEventCreate(&e2));
+        s->pa.p = s->p;
+        s->pa.n_steps = n_steps;
+        const int n_rec = s->pa.p.n_rec;
+        s->pa.p.n_rec = 0;   // the kernel alone, then the receiver sums
+        TS_CUDA(cudaEventRecord(e0, st));
+        cudaError_t e = ts::launch_persist_2d(s->pa, s->family, s->p_rows, s->p_blocks, s->p_threads, s->p_smem, st);
+        s->pa.p.n_rec = n_rec;
+        if (e != cudaSuccess) return cuda_fail(e, "persistent step launch");
+        TS_CUDA(cudaEventRecord(e1, st));
+        if (n_rec > 0) {
+            // receiver sums of the same steps: the kernel's samples, summed by the same launch helper
+            ts::PersistArgs r = s->pa;
+            r.n_steps = 0;
+            TS_CUDA(ts::launch_persist_2d_receivers(r, n_steps, st));
+        }
+        TS_CUDA(cudaEventRecord(e2, st));
+        ts::launch_advance(s->step_base, n_steps, st);
+        s->launches += 2 + (n_rec > 0 ? 1 : 0);
+        TS_CUDA(cudaEventSynchronize(e2));
+        float a = 0.f, b = 0.f;
+        TS_CUDA(cudaEventElapsedTime(&a, e0, e1));
+        TS_CUDA(cudaEventElapsedTime(&b, e1, e2));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaEventDestroy(e2);
+        ms_per_kernel[0] = a / n_steps;
+        ms_per_kernel[1] = b / n_steps;
+        TS_CUDA(cudaEventRecord(s->done, st));
+        s->steps_done += n_steps;
+        return TS_OK;
+    }
     std::vector<cudaEvent_t> ev(2 * n_steps + 1);
     for (auto &e : ev) TS_CUDA(cudaEventCreate(&e));
     TS_CUDA(cudaEventRecord(ev[0], st));
@@ -750,6 +868,20 @@ int ts_run(ts_sim *s, int32_t n_steps, void *stream) {
         return fail(TS_E_ARG, "steps beyond the source/trace length");
     TS_CUDA(cudaSetDevice(s->device));
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : s->stream;
+    if (s->persist) {   // every step of this call in one cooperative launch
+        if (n_steps > 0) {
+            s->pa.p = s->p;
+            s->pa.n_steps = n_steps;
+            cudaError_t e = ts::launch_persist_2d(s->pa, s->family, s->p_rows, s->p_blocks, s->p_threads, s->p_smem, st);
+            if (e != cudaSuccess) return cuda_fail(e, "persistent step launch");
+            ts::launch_advance(s->step_base, n_steps, st);
+            s->launches += 2 + (s->n_rec > 0 ? 1 : 0);
+        }
+        TS_CUDA(cudaGetLastError());
+        TS_CUDA(cudaEventRecord(s->done, st));
+        s->steps_done += n_steps;
+        return TS_OK;
+    }
     auto launch_steps = [&](int count, cudaStream_t where) {
         for (int j = 0; j < count; ++j) {
             if (s->dims == 2) ts::launch_step_2d(s->p, s->ord, s->zen_mode, j, where);
@@ -787,6 +919,14 @@ int ts_status(ts_sim *s, int32_t *steps_done, float *max_v2, int32_t *first_unst
     TS_CUDA(cudaSetDevice(s->device));
     TS_CUDA(cudaEventSynchronize(s->done));
     if (steps_done) *steps_done = s->steps_done;
+    if (s->persist) {
+        int err[4] = {0, 0, 0, 0};
+        TS_CUDA(cudaMemcpy(err, s->pa.err, sizeof err, cudaMemcpyDeviceToHost));
+        if (err[0])
+            return fail(TS_E_TIMEOUT, "persistent step kernel: block " + std::to_string(err[2]) +
+                                          " gave up waiting for a neighbouring block at step " + std::to_string(err[1]) +
+                                          "; the wavefield is invalid until ts_reset");
+    }
     if (max_v2) {
         std::vector<unsigned> bm(s->n_blocks);
         TS_CUDA(cudaMemcpy(bm.data(), s->block_max, bm.size() * sizeof(unsigned), cudaMemcpyDeviceToHost));
@@ -836,6 +976,12 @@ int ts_device_buffer(ts_sim *s, int32_t what, void **dev_ptr, size_t *pitch_byte
     if (what < TS_VX || what > TS_SYZ || !s->field[what]) return fail(TS_E_ARG, "no such field");
     *dev_ptr = s->field[what];
     if (pitch_bytes) *pitch_bytes = (size_t)s->pitch * sizeof(float);
+    return TS_OK;
+}
+
+int ts_step_path(const ts_sim *s, int32_t *path) {
+    if (!s || !path) return fail(TS_E_ARG, "null argument");
+    *path = s->persist ? TS_PATH_PERSISTENT : TS_PATH_STEPPED;
     return TS_OK;
 }
 

@@ -24,9 +24,10 @@ namespace ts {
 constexpr int kMaxOrd = 6;
 constexpr int kMaxSls = 8;
 
-// CPML coefficients of one node along one axis: a, b, 1/k.
+// CPML coefficients of one node along one axis: a, b, 1/k and k (the
+// Taichi family divides by k, as the reference does).
 struct Cpml {
-    float a, b, ik, pad;
+    float a, b, ik, k;
 };
 
 // Prefix/suffix strip of one axis: index `i` maps to compact `i` (i < lo)
@@ -49,7 +50,7 @@ struct Zener {
 struct Source {
     int64_t cell;   // flat padded offset
     int col;        // column of the device source table
-    float scale;    // dt / rho at the node (the reference divides by rho)
+    float scale;    // dt / rho at the node (the reference divides by rho); TS_TAICHI2D: rho
 };
 
 // Everything a 2D or 3D kernel reads, passed by value.
@@ -69,6 +70,11 @@ struct StepParams {
     int pitch;             // padded last-axis length (floats)
     int64_t plane;         // ny * pitch (3D x stride); 2D: pitch
     float cd[3][kMaxOrd];  // coef[c] / d_axis (x, y, z)
+    // the reference's own factors, for the family whose kernels keep its
+    // operation order (TS_TAICHI2D): coef[c], 1 / d_axis (float), dt
+    float coef[kMaxOrd];
+    float od[3];
+    float dt;
 
     // fields
     float *v[3];           // vx, vy, vz
@@ -81,7 +87,9 @@ struct StepParams {
     // velocity kernel psi of stress derivatives (see ts_stepper*.cu)
     float *psi[18];
 
-    // per-cell coefficients
+    // per-cell coefficients (family TS_TAICHI2D: lambda, mu, mu at the
+    // shear node, rho at the vx node and the averaged rho at the vy node,
+    // not folded with dt)
     const float *lam_dt, *mu_dt;          // normal node
     const float *mus_dt[3];               // shear nodes xy, xz, yz (2D: xy)
     const float *dtr[3];                  // dt / rho at vx, vy, vz nodes (0: no update)
@@ -116,6 +124,61 @@ struct StepParams {
     // 2D adjoint record of one step, [kFeat][grid_elems] (launch_step_2d_feat)
     float *feat;
 };
+
+// Arguments of the persistent 2D elastic step kernel (ts_persist2d.cu): the
+// regular kernels' parameters plus the exchange buffers between blocks.
+struct PersistArgs {
+    StepParams p;
+    int n_steps;               // steps of this launch, from *p.step_base
+    int n_blocks;              // slots of p.block_max
+    float *mail;               // [blocks][2 edges][2 step parities][vx, vy][2 ORD - 1 rows][threads]
+    unsigned *flags;           // [blocks]: last step whose edge rows are in the mailbox, plus 1
+    int *err;                  // [4]: 1 when a wait gave up, its step, its block
+    float *samples;            // [rows][n_pts]: syy at each receiver point (CSR position)
+    int n_pts;
+    const int4 *pts;           // per block: (row in the slab, column, CSR position, 0)
+    const int *pts_start;      // [blocks + 1]
+    const int4 *srcs;          // per block: (row in the slab, column, table column, dt / rho bits)
+    const int *src_start;      // [blocks + 1]
+    long long wait_ns;         // bound of every wait on a neighbour
+    int stall_block;           // test hook: this block never releases its counter (-1: none)
+};
+
+// Persistent path: whether it serves a 2D model (elastic, order 2, a slab of
+// rows per block fitting shared memory, every block resident), and its
+// shape; and its launch (the kernel, then the receiver sums).
+int persist_2d_plan(int family, int ord, int zen_mode, int nx, int ny, int strip_y, int n_sms, int *rows,
+                    int *blocks, int *threads, size_t *smem);
+cudaError_t launch_persist_2d(const PersistArgs &a, int family, int rows, int blocks, int threads, size_t smem,
+                              cudaStream_t st);
+// the receiver sums alone: traces of steps [*step_base, *step_base + n_steps) from the samples
+cudaError_t launch_persist_2d_receivers(const PersistArgs &a, int n_steps, cudaStream_t st);
+
+// Family TS_TAICHI2D keeps the reference's operation order
+// (sim_taichi_elastic.py:152-157, 181-182, 226-229, 263-268, 293-304):
+// every product, sum and quotient rounded on its own (the _rn intrinsics are
+// never contracted to fma), derivatives as sum of coef * (hi - lo) * (1/d),
+// the CPML update as b psi + a d then d / k + psi.  Its results are then the
+// bits of a strict IEEE evaluation of the reference's expressions.
+__device__ __forceinline__ float taichi_term(float acc, float coef, float hi, float lo, float od) {
+    return __fadd_rn(acc, __fmul_rn(__fmul_rn(coef, __fsub_rn(hi, lo)), od));
+}
+__device__ __forceinline__ float taichi_cpml(float d, float psi_old, float &psi_new, const Cpml &t) {
+    psi_new = __fadd_rn(__fmul_rn(t.b, psi_old), __fmul_rn(t.a, d));
+    return __fadd_rn(__fdiv_rn(d, t.k), psi_new);
+}
+// sigma += (lambda div + 2 mu d) dt
+__device__ __forceinline__ float taichi_normal(float s, float lam_div, float mu, float d, float dt) {
+    return __fadd_rn(s, __fmul_rn(__fadd_rn(lam_div, __fmul_rn(__fmul_rn(2.f, mu), d)), dt));
+}
+// sigma_xy += (dvx/dy + dvy/dx) mu dt
+__device__ __forceinline__ float taichi_shear(float s, float e, float mu, float dt) {
+    return __fadd_rn(s, __fmul_rn(__fmul_rn(e, mu), dt));
+}
+// v += src + f dt / rho (src: the source's force dt / rho, or 0); no update where rho <= 0
+__device__ __forceinline__ float taichi_velocity(float v, float f, float src, float rho, float dt) {
+    return rho > 0.f ? __fadd_rn(v, __fadd_rn(src, __fdiv_rn(__fmul_rn(f, dt), rho))) : v;
+}
 
 // Slots of the 2D adjoint record: what the stress and velocity updates
 // multiply lambda*dt, mu*dt (normal node: x and y rows), mu*dt (shear node)

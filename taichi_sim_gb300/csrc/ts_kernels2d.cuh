@@ -26,10 +26,12 @@
 //
 // Semantics follow the reference (family TS_TAICHI2D:
 // sim_taichi_elastic.py:138-309; family TS_WGSL2D:
-// shader_webgpu_viscoelastic.wgsl:829-1072 and :1118-1134) with the
-// divisions by dx/dy/rho/k replaced by multiplications with precomputed
-// reciprocals and a*b+c contracted to fma: results agree with the
-// reference's float arithmetic to rounding (checked against the CPU oracle).
+// shader_webgpu_viscoelastic.wgsl:829-1072 and :1118-1134).  Family
+// TS_WGSL2D replaces the divisions by dx/dy/rho/k with multiplications by
+// precomputed reciprocals and contracts a*b+c to fma: it agrees with the
+// reference's float arithmetic to rounding.  Family TS_TAICHI2D keeps the
+// reference's operation order with every operation rounded on its own
+// (taichi_* in ts_internal.cuh): bit for bit the strict-IEEE oracle.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -166,22 +168,27 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
                     float ddx = 0.f, ddy = 0.f, np_;
 #pragma unroll
                     for (int c = 0; c < ORD; ++c) {
-                        ddx = fmaf(p.cd[0][c], wvx[c + ORD] - wvx[ORD - 1 - c], ddx);
                         const float hi = c == 0 ? wvy[ORD] : ny_hi[c > 0 ? c - 1 : 0];
-                        ddy = fmaf(p.cd[1][c], hi - ny_lo[c], ddy);
+                        if (FAM == kTaichi) {
+                            ddx = taichi_term(ddx, p.coef[c], wvx[c + ORD], wvx[ORD - 1 - c], p.od[0]);
+                            ddy = taichi_term(ddy, p.coef[c], hi, ny_lo[c], p.od[1]);
+                        } else {
+                            ddx = fmaf(p.cd[0][c], wvx[c + ORD] - wvx[ORD - 1 - c], ddx);
+                            ddy = fmaf(p.cd[1][c], hi - ny_lo[c], ddy);
+                        }
                     }
                     if (sx >= 0) {
-                        ddx = cpml(ddx, pn0, np_, p.tab_h[0][x]);
+                        ddx = FAM == kTaichi ? taichi_cpml(ddx, pn0, np_, p.tab_h[0][x]) : cpml(ddx, pn0, np_, p.tab_h[0][x]);
                         p.psi[0][ix] = np_;
                     }
                     if (syl >= 0) {
-                        ddy = cpml(ddy, pn1, np_, p.tab_f[1][y]);
+                        ddy = FAM == kTaichi ? taichi_cpml(ddy, pn1, np_, p.tab_f[1][y]) : cpml(ddy, pn1, np_, p.tab_f[1][y]);
                         p.psi[2][iy] = np_;
                     }
                     if (FAM == kTaichi) {
-                        const float dl = L * (ddx + ddy);
-                        sxx += fmaf(2.f * M, ddx, dl);
-                        syy += fmaf(2.f * M, ddy, dl);
+                        const float dl = __fmul_rn(L, __fadd_rn(ddx, ddy));
+                        sxx = taichi_normal(sxx, dl, M, ddx, p.dt);
+                        syy = taichi_normal(syy, dl, M, ddy, p.dt);
                     } else {
                         const float L2M = fmaf(2.f, M, L);
                         float ux = fmaf(L2M, ddx, L * ddy), uy = fmaf(L, ddx, L2M * ddy);
@@ -219,32 +226,41 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
                     float a = 0.f, b = 0.f, np_;
 #pragma unroll
                     for (int c = 0; c < ORD; ++c) {
-                        a = fmaf(p.cd[0][c], wvy[c + ORD] - wvy[ORD - 1 - c], a);
                         const float lo = c == 0 ? wvx[ORD - 1] : sx_lo[c > 0 ? c - 1 : 0];
-                        b = fmaf(p.cd[1][c], sx_hi[c] - lo, b);
+                        if (FAM == kTaichi) {
+                            a = taichi_term(a, p.coef[c], wvy[c + ORD], wvy[ORD - 1 - c], p.od[0]);
+                            b = taichi_term(b, p.coef[c], sx_hi[c], lo, p.od[1]);
+                        } else {
+                            a = fmaf(p.cd[0][c], wvy[c + ORD] - wvy[ORD - 1 - c], a);
+                            b = fmaf(p.cd[1][c], sx_hi[c] - lo, b);
+                        }
                     }
                     if (sx >= 0) {
-                        a = cpml(a, ps0, np_, p.tab_f[0][x]);
+                        a = FAM == kTaichi ? taichi_cpml(a, ps0, np_, p.tab_f[0][x]) : cpml(a, ps0, np_, p.tab_f[0][x]);
                         p.psi[1][ix] = np_;
                     }
                     if (syl >= 0) {
-                        b = cpml(b, ps1, np_, p.tab_h[1][y]);
+                        b = FAM == kTaichi ? taichi_cpml(b, ps1, np_, p.tab_h[1][y]) : cpml(b, ps1, np_, p.tab_h[1][y]);
                         p.psi[3][iy] = np_;
                     }
-                    const float e = a + b;
-                    float u = Ms * e, sr = 0.f;
-                    if (FAM != kTaichi && ZM != 0) {
+                    if (FAM == kTaichi) {
+                        p.s[3][i] = taichi_shear(sxy, __fadd_rn(a, b), Ms, p.dt);
+                    } else {
+                        const float e = a + b;
+                        float u = Ms * e, sr = 0.f;
+                        if (ZM != 0) {
 #pragma unroll
-                        for (int l = 0; l < R; ++l)
-                            if (l < n_mech) {
-                                const float n_ = fmaf(p.zen.As[l], rxy[l], (p.zen.Bs[l] * gs) * e);
-                                sr += rxy[l] + n_;
-                                p.r[2][l * p.grid_elems + i] = n_;
-                            }
-                        u = fmaf(0.5f * Ms, sr, u);
+                            for (int l = 0; l < R; ++l)
+                                if (l < n_mech) {
+                                    const float n_ = fmaf(p.zen.As[l], rxy[l], (p.zen.Bs[l] * gs) * e);
+                                    sr += rxy[l] + n_;
+                                    p.r[2][l * p.grid_elems + i] = n_;
+                                }
+                            u = fmaf(0.5f * Ms, sr, u);
+                        }
+                        if (FEAT) p.feat[kFeatShear * p.grid_elems + i] = fmaf(0.5f, sr, e);
+                        p.s[3][i] = sxy + u;
                     }
-                    if (FEAT) p.feat[kFeatShear * p.grid_elems + i] = fmaf(0.5f, sr, e);
-                    p.s[3][i] = sxy + u;
                 }
             }
             if (t + 1 < TX) {
@@ -315,19 +331,31 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             float a = 0.f, b = 0.f;
 #pragma unroll
             for (int c = 0; c < ORD; ++c) {
-                a = fmaf(p.cd[0][c], rxx[t + ORD + c] - rxx[t + ORD - 1 - c], a);
                 const float hi = c == 0 ? rxy[t + ORD - 1] : bh[t][c > 0 ? c - 1 : 0];
-                b = fmaf(p.cd[1][c], hi - bl[t][c], b);
+                if (FAM == kTaichi) {
+                    a = taichi_term(a, p.coef[c], rxx[t + ORD + c], rxx[t + ORD - 1 - c], p.od[0]);
+                    b = taichi_term(b, p.coef[c], hi, bl[t][c], p.od[1]);
+                } else {
+                    a = fmaf(p.cd[0][c], rxx[t + ORD + c] - rxx[t + ORD - 1 - c], a);
+                    b = fmaf(p.cd[1][c], hi - bl[t][c], b);
+                }
             }
-            const float fax = a + b, vxn = fmaf(fax, dx0[t], vx0[t]);
+            const float fax = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
+            const float vxn = FAM == kTaichi ? taichi_velocity(vx0[t], fax, 0.f, dx0[t], p.dt) : fmaf(fax, dx0[t], vx0[t]);
             a = 0.f;
             b = 0.f;
 #pragma unroll
             for (int c = 0; c < ORD; ++c) {
-                a = fmaf(p.cd[0][c], rxy[t + ORD + c] - rxy[t + ORD - 1 - c], a);
-                b = fmaf(p.cd[1][c], by[t][ORD + c] - by[t][ORD - 1 - c], b);
+                if (FAM == kTaichi) {
+                    a = taichi_term(a, p.coef[c], rxy[t + ORD + c], rxy[t + ORD - 1 - c], p.od[0]);
+                    b = taichi_term(b, p.coef[c], by[t][ORD + c], by[t][ORD - 1 - c], p.od[1]);
+                } else {
+                    a = fmaf(p.cd[0][c], rxy[t + ORD + c] - rxy[t + ORD - 1 - c], a);
+                    b = fmaf(p.cd[1][c], by[t][ORD + c] - by[t][ORD - 1 - c], b);
+                }
             }
-            const float fay = a + b, vyn = fmaf(fay, dy0[t], vy0[t]);
+            const float fay = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
+            const float vyn = FAM == kTaichi ? taichi_velocity(vy0[t], fay, 0.f, dy0[t], p.dt) : fmaf(fay, dy0[t], vy0[t]);
             p.v[0][i] = vxn;
             p.v[1][i] = vyn;
             if (FEAT) {
@@ -385,40 +413,63 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                 float a = 0.f, b = 0.f;
 #pragma unroll
                 for (int c = 0; c < ORD; ++c) {
-                    a = fmaf(p.cd[0][c], wxx[c + ORD] - wxx[ORD - 1 - c], a);
                     const float hi = c == 0 ? wxy[ORD - 1] : bx_hi[c > 0 ? c - 1 : 0];
-                    b = fmaf(p.cd[1][c], hi - bx_lo[c], b);
+                    if (FAM == kTaichi) {
+                        a = taichi_term(a, p.coef[c], wxx[c + ORD], wxx[ORD - 1 - c], p.od[0]);
+                        b = taichi_term(b, p.coef[c], hi, bx_lo[c], p.od[1]);
+                    } else {
+                        a = fmaf(p.cd[0][c], wxx[c + ORD] - wxx[ORD - 1 - c], a);
+                        b = fmaf(p.cd[1][c], hi - bx_lo[c], b);
+                    }
                 }
                 if (sx >= 0) {
-                    a = cpml(a, pxa, np_, p.tab_f[0][x]);
+                    a = FAM == kTaichi ? taichi_cpml(a, pxa, np_, p.tab_f[0][x]) : cpml(a, pxa, np_, p.tab_f[0][x]);
                     p.psi[4][ix] = np_;
                 }
                 if (syl >= 0) {
-                    b = cpml(b, pxb, np_, p.tab_f[1][y]);
+                    b = FAM == kTaichi ? taichi_cpml(b, pxb, np_, p.tab_f[1][y]) : cpml(b, pxb, np_, p.tab_f[1][y]);
                     p.psi[6][iy] = np_;
                 }
-                fax = a + b;
-                vxn = fmaf(fax, dx0, vx0);
+                fax = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
+                vxn = FAM == kTaichi ? taichi_velocity(vx0, fax, 0.f, dx0, p.dt) : fmaf(fax, dx0, vx0);
             }
             if (in_vy) {
                 float a = 0.f, b = 0.f;
 #pragma unroll
                 for (int c = 0; c < ORD; ++c) {
-                    a = fmaf(p.cd[0][c], wxy[c + ORD] - wxy[ORD - 1 - c], a);
-                    b = fmaf(p.cd[1][c], by[ORD + c] - by[ORD - 1 - c], b);
+                    if (FAM == kTaichi) {
+                        a = taichi_term(a, p.coef[c], wxy[c + ORD], wxy[ORD - 1 - c], p.od[0]);
+                        b = taichi_term(b, p.coef[c], by[ORD + c], by[ORD - 1 - c], p.od[1]);
+                    } else {
+                        a = fmaf(p.cd[0][c], wxy[c + ORD] - wxy[ORD - 1 - c], a);
+                        b = fmaf(p.cd[1][c], by[ORD + c] - by[ORD - 1 - c], b);
+                    }
                 }
                 if (sx >= 0) {
-                    a = cpml(a, pya, np_, p.tab_h[0][x]);
+                    a = FAM == kTaichi ? taichi_cpml(a, pya, np_, p.tab_h[0][x]) : cpml(a, pya, np_, p.tab_h[0][x]);
                     p.psi[5][ix] = np_;
                 }
                 if (syl >= 0) {
-                    b = cpml(b, pyb, np_, p.tab_h[1][y]);
+                    b = FAM == kTaichi ? taichi_cpml(b, pyb, np_, p.tab_h[1][y]) : cpml(b, pyb, np_, p.tab_h[1][y]);
                     p.psi[7][iy] = np_;
                 }
-                fay = a + b;
-                vyn = fmaf(fay, dy0, vy0);
+                fay = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
+                if (FAM == kTaichi) {
+                    // the source's force dt / rho joins the update inside it (sim_taichi_elastic.py:294-304)
+                    float src = 0.f;
+                    if constexpr (!FAST) {
+                        for (int q = q0; q < q1; ++q) {
+                            const Source s = p.src[q];
+                            if (s.cell == i && k < p.src_rows)
+                                src = __fdiv_rn(__fmul_rn(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), p.dt), s.scale);
+                        }
+                    }
+                    vyn = taichi_velocity(vy0, fay, src, dy0, p.dt);
+                } else {
+                    vyn = fmaf(fay, dy0, vy0);
+                }
             }
-            if constexpr (!FAST) {
+            if constexpr (!FAST && FAM != kTaichi) {
                 for (int q = q0; q < q1; ++q) {
                     const Source s = p.src[q];
                     if (s.cell == i && k < p.src_rows)

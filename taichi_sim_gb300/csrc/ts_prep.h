@@ -24,14 +24,14 @@ inline Axis make_axis(int n, int ord, const float *a, const float *b, const floa
                       const float *bh, const float *kh) {
     Axis ax;
     const int off = ord - 1, ntab = n - 2 * (ord - 1);
-    ax.full.assign(n, Cpml{0.f, 1.f, 1.f, 0.f});
-    ax.half.assign(n, Cpml{0.f, 1.f, 1.f, 0.f});
+    ax.full.assign(n, Cpml{0.f, 1.f, 1.f, 1.f});
+    ax.half.assign(n, Cpml{0.f, 1.f, 1.f, 1.f});
     std::vector<char> nonid(n, 0);
     for (int x = 0; x < n; ++x) {
         const int t = x - off;
         if (t < 0 || t >= ntab || !a) continue;
-        ax.full[x] = Cpml{a[t], b[t], 1.f / k[t], 0.f};
-        ax.half[x] = Cpml{ah[t], bh[t], 1.f / kh[t], 0.f};
+        ax.full[x] = Cpml{a[t], b[t], 1.f / k[t], k[t]};
+        ax.half[x] = Cpml{ah[t], bh[t], 1.f / kh[t], kh[t]};
         nonid[x] = !cpml_identity(ax.full[x]) || !cpml_identity(ax.half[x]);
     }
     int lo = 0, hi = n;
@@ -64,6 +64,7 @@ inline int receiver_first_point(const ts_desc *d, int r, int cols) {
 // shader_webgpu_viscoelastic.wgsl:863-868, 948-950, 1020, 1032).
 struct Coef2D {
     float lam, mu, mus, dtr_vx, dtr_vy, rho_vy;
+    float lam_raw, mu_raw, mus_raw, rho_vx;   // the same before folding with dt
 };
 
 inline Coef2D coef_2d(const ts_desc *d, int x, int y) {
@@ -78,13 +79,17 @@ inline Coef2D coef_2d(const ts_desc *d, int x, int y) {
     const float c1 = g(d->cs, x + 1, y), c0 = g(d->cs, x, y);
     const float csl = 0.5f * (c1 + c0);
     const float csm = std::min(c1, c0) == 0.f ? 0.f : csl;
-    c.lam = rh * (cph * cph - 2.f * csl * csl) * dt;
-    c.mu = rh * (csm * csm) * dt;
+    c.lam_raw = rh * (cph * cph - 2.f * csl * csl);
+    c.mu_raw = rh * (csm * csm);
+    c.lam = c.lam_raw * dt;
+    c.mu = c.mu_raw * dt;
     const float rhy = 0.5f * (g(d->rho, x, y + 1) + g(d->rho, x, y));
     const float s1 = g(d->cs, x, y + 1), s0 = g(d->cs, x, y);
     const float csh = std::min(s1, s0) == 0.f ? 0.f : 0.5f * (s1 + s0);
-    c.mus = rhy * (csh * csh) * dt;
+    c.mus_raw = rhy * (csh * csh);
+    c.mus = c.mus_raw * dt;
     const float r = g(d->rho, x, y);
+    c.rho_vx = r;
     c.dtr_vx = r > 0.f ? dt / r : 0.f;
     c.rho_vy = d->family == TS_TAICHI2D
                    ? 0.25f * (g(d->rho, x, y + 1) + g(d->rho, x, y) + g(d->rho, x + 1, y + 1) + g(d->rho, x + 1, y))

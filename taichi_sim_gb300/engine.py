@@ -82,6 +82,7 @@ def load_library(build_if_missing=True):
             "ts_device_buffer": ([P, ctypes.c_int32, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_size_t)],
                                  ctypes.c_int),
             "ts_launches_per_step": ([P, _i], ctypes.c_int),
+            "ts_step_path": ([P, _i], ctypes.c_int),
             "ts_destroy": ([P], None),
             "ts_strerror": ([ctypes.c_int], ctypes.c_char_p),
             "ts_last_error": ([], ctypes.c_char_p),
@@ -146,6 +147,9 @@ class Stepper:
         n = ctypes.c_int32()
         _check(self._lib.ts_launches_per_step(self._h, ctypes.byref(n)), "ts_launches_per_step")
         self.launches_per_step = n.value
+        _check(self._lib.ts_step_path(self._h, ctypes.byref(n)), "ts_step_path")
+        # "persistent": every step of a run() in one launch, the wavefield on chip
+        self.path = "persistent" if n.value == 1 else "stepped"
 
     # -- descriptor -----------------------------------------------------------
     def _f32(self, a):

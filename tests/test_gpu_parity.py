@@ -1,11 +1,13 @@
 """GPU parity: the CUDA stepper (through the C ABI) against the CPU oracle.
 
 The oracle restates the reference's kernels in IEEE float with the
-reference's operation order; the CUDA kernels fold divisions into
-reciprocals and contract to fma, so they agree to rounding.  Tolerance:
+reference's operation order.  The WGSL-family CUDA kernels fold divisions
+into reciprocals and contract to fma, so they agree to rounding.  Tolerance:
 relative L2 <= 1e-5 on fields and receiver traces (the bound the reference
 comparison uses), and the float error of each implementation is also
-measured against the oracle's double-precision run.
+measured against the oracle's double-precision run.  The Taichi-family
+kernels keep the reference's operation order and must match the float
+oracle bit for bit.
 """
 import numpy as np
 import pytest
@@ -89,13 +91,38 @@ def test_parity_2d(name):
 
 
 @pytest.mark.parametrize("tx", [1, 2, 4])
-@pytest.mark.parametrize("name", ["taichi_elastic", "wgsl_visco_q", "wgsl_visco_acc6"])
+@pytest.mark.parametrize("name", ["taichi_elastic", "wgsl_elastic", "wgsl_visco_q", "wgsl_visco_acc6"])
 def test_parity_2d_nodes_per_thread(name, tx, monkeypatch):
-    """Every variant of the x-marching 2D kernels (1, 2, 4 nodes per thread)."""
+    """Every variant of the x-marching 2D kernels (1, 2, 4 nodes per thread);
+    the regular two-kernel step (elastic order-2 models otherwise take the
+    persistent path)."""
     monkeypatch.setenv("TS_2D_NODES_PER_THREAD", str(tx))
+    monkeypatch.setenv("TS_2D_PERSISTENT", "0")
     build, family = CASES_2D[name]
     sim = Simulator(build())
     _compare(sim, family, ["vx", "vy", "sxx", "syy", "sxy"])
+
+
+TAICHI_CASES = sorted(n for n, (_, f) in CASES_2D.items() if f == engine.TAICHI2D)
+
+
+@pytest.mark.parametrize("persistent", ["0", "1"], ids=["regular", "persistent"])
+@pytest.mark.parametrize("name", TAICHI_CASES)
+def test_taichi_family_is_bit_exact(name, persistent, monkeypatch):
+    """The Taichi family keeps the reference's operation order with every
+    operation rounded on its own, so every field and trace equals the
+    strict-IEEE float oracle bit for bit, on both 2D paths (order 2 models
+    take the persistent path unless it is switched off; other orders always
+    take the regular one)."""
+    monkeypatch.setenv("TS_2D_PERSISTENT", persistent)
+    build, family = CASES_2D[name]
+    sim = Simulator(build())
+    ref = oracle.run(sim, oracle.TAICHI2D)
+    with engine.Stepper(sim, family=family) as st:
+        st.run(sim._n_steps)
+        for k in ("vx", "vy", "sxx", "syy", "sxy"):
+            np.testing.assert_array_equal(st.read(k), ref[k], err_msg=k)
+        np.testing.assert_array_equal(st.read("traces"), ref["sens"])
 
 
 @pytest.mark.parametrize("palette", ["1", "0"], ids=["palette", "arrays"])
