@@ -163,6 +163,15 @@ int ts_transfer_bytes(const ts_sim *sim, int64_t *h2d, int64_t *d2h);
  * by a caller on the same device. */
 int ts_device_buffer(ts_sim *sim, int32_t what, void **dev_ptr, size_t *pitch_bytes);
 
+/* Enqueue on `stream` (NULL: the handle's own stream) a copy of one field,
+ * as it stands after the steps queued so far, to caller memory `dst`
+ * (device or pinned host) as [nx][ny][nz] floats with rows dst_pitch bytes
+ * apart (0: packed).  Does not wait.  Replaces the reference's live view,
+ * which reads the field back every it_display steps
+ * (sim_taichi_elastic.py:320-329, sim_webgpu_viscoelastic.py:519-530):
+ * the caller records snapshots without a synchronisation per frame. */
+int ts_copy_field(ts_sim *sim, int32_t what, void *dst, size_t dst_pitch, void *stream);
+
 /* Number of kernel launches one time step issues (for launch accounting;
  * the persistent path issues its launches per ts_run call instead). */
 int ts_launches_per_step(const ts_sim *sim, int32_t *launches);

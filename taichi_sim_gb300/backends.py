@@ -15,6 +15,11 @@ and the three backends): construct with a config path, ``run()`` calls
 
 ``sim_time`` is the wall time of the step loop, as in the reference.
 ``StabilityError`` is raised when the velocity norm breaks the threshold.
+With ``show_anim`` or ``save_snapshots`` set, ``implementation()`` also
+returns ``"snapshots"``: the ROI of the field (3D: its middle y plane) after
+every step the reference's live view shows, copied on the device as the run
+goes (``ts_copy_field``, no synchronisation per frame), and
+``"snapshot_steps"``.
 The device state is created once and reset between shots; a new emission
 law only re-uploads the source term.
 """
@@ -23,7 +28,8 @@ import time
 import numpy as np
 
 from . import engine
-from .sim_support.simulator import Simulator
+from .sim_support import StabilityError
+from .sim_support.simulator import Simulator, snapshot_steps
 from .sim_support.Simulator3D import Simulator3D
 
 
@@ -59,12 +65,60 @@ class _CudaBackend:
         super().implementation()
         st = self._stepper()
         t0 = time.time()
-        st.simulate()
+        snaps = None
+        if getattr(self, "_show_anim", False) or getattr(self, "_save_snapshots", False):
+            snaps, steps = self._simulate_with_snapshots(st)
+        else:
+            st.simulate()
         st.status()
         sim_time = time.time() - t0
         field = st.read(self._field)
         traces = st.read("traces")
-        return {self._keys[0]: field, self._keys[1]: traces, "gpu_str": _gpu_name(), "sim_time": sim_time}
+        res = {self._keys[0]: field, self._keys[1]: traces, "gpu_str": _gpu_name(), "sim_time": sim_time}
+        if snaps is not None:
+            res["snapshots"], res["snapshot_steps"] = snaps, steps
+        return res
+
+    def _snapshot_view(self, t):
+        """The part of a field the live view shows: the ROI (3D: its middle y plane)."""
+        roi = self._roi
+        if self._dims == 2:
+            return t[roi.get_ix_min():roi.get_ix_max(), roi.get_iz_min():roi.get_iz_max()]
+        return t[roi.get_ix_min():roi.get_ix_max(), t.shape[1] // 2, roi.get_iz_min():roi.get_iz_max()]
+
+    def _simulate_with_snapshots(self, st, check_every=256):
+        """Run every step, copying the field on the device after each step
+        the live view would show; stability is checked every
+        ``check_every`` steps as in :meth:`engine.Stepper.simulate`."""
+        import torch
+        steps = snapshot_steps(self._n_steps, self._it_display)
+        stream = torch.cuda.Stream()
+        h = stream.cuda_stream
+        stage = torch.empty(tuple(st.shape), dtype=torch.float32, device="cuda")
+        stack = torch.empty((len(steps),) + tuple(self._snapshot_view(stage).shape), dtype=torch.float32,
+                            device="cuda")
+        done = checked = 0
+
+        def check():
+            _, vmax, bad = st.status()
+            if bad >= 0:
+                value = vmax if st.family == engine.TAICHI2D else float(np.sqrt(np.float32(vmax)))
+                raise StabilityError("Simulacao tornando-se instavel", value)
+
+        for i, s in enumerate(steps):
+            st.run(s - done, stream=h)
+            done = s
+            st.copy_field(self._field, stage.data_ptr(), stream=h)
+            with torch.cuda.stream(stream):
+                stack[i].copy_(self._snapshot_view(stage))
+            if done - checked >= check_every:
+                check()
+                checked = done
+        if done < self._n_steps:
+            st.run(self._n_steps - done, stream=h)
+        check()
+        stream.synchronize()
+        return stack.cpu().numpy(), steps
 
 
 class SimulatorCudaElastic(_CudaBackend, Simulator):

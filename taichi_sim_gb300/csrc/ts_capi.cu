@@ -115,6 +115,7 @@ struct ts_sim {
     std::vector<void *> state_ptrs;
     StepParams p{};
     // persistent path (2D elastic, order 2; ts_persist2d.cu)
+    ts::RecChunks rc{};   // receivers with many points (stepped path)
     int persist = 0, p_rows = 0, p_blocks = 0, p_threads = 0;
     size_t p_smem = 0;
     ts::PersistArgs pa{};
@@ -206,7 +207,7 @@ using ts::round_up;
 
 // Kernel launches of one time step: 2D stress + velocity; 3D normal stress,
 // shear stress, velocity.
-static int kernels_per_step(const ts_sim *s) { return s->dims == 3 ? 3 : 2; }
+static int kernels_per_step(const ts_sim *s) { return (s->dims == 3 ? 3 : 2) + (s->rc.n_chunks > 0 ? 1 : 0); }
 
 extern "C" {
 
@@ -379,6 +380,8 @@ int ts_create(const ts_desc *d, ts_sim **out) {
             const int v = atoi(env);
             if (v == 1 || v == 2 || v == 4) p.tx = v;
         }
+        const char *xy = getenv("TS_3D_XY_SWEEP");
+        p.xy_sweep_3d = !(xy && xy[0] == '0');
     }
     p.nx = nx;
     p.ny = ny;
@@ -725,6 +728,41 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         }
     }
 
+    // ---- receivers with many points: summed in chunks after each step (stepped path) ----
+    if (!s->persist && d->n_rec > 0) {
+        const char *force = getenv("TS_RECEIVER_CHUNKS");          // 1: every receiver chunked
+        const char *cp = getenv("TS_RECEIVER_CHUNK_POINTS");      // chunk size
+        const bool all = force && force[0] == '1';
+        const int per = cp ? std::max(1, atoi(cp)) : ts::kChunkPoints;
+        std::vector<unsigned char> flag(d->n_rec, 0);
+        std::vector<int2> chunks;
+        std::vector<int> recv, rchunk(1, 0);
+        for (int r = 0; r < d->n_rec; ++r) {
+            const int a = rec_start_h[r], b = rec_start_h[r + 1];
+            if (!(all || b - a > ts::kChunkedMinPoints)) continue;
+            flag[r] = 1;
+            recv.push_back(r);
+            for (int q = a; q < b; q += per) chunks.push_back(make_int2(q, std::min(b, q + per)));
+            rchunk.push_back((int)chunks.size());
+        }
+        if (!chunks.empty()) {
+            unsigned char *dflag = nullptr;
+            int2 *dch = nullptr;
+            int *drecv = nullptr, *drch = nullptr;
+            if ((rc = s->upload(&dflag, flag)) || (rc = s->upload(&dch, chunks)) || (rc = s->upload(&drecv, recv)) ||
+                (rc = s->upload(&drch, rchunk)) || (rc = s->alloc(&s->rc.partial, chunks.size(), false)) ||
+                (rc = s->alloc(&s->rc.counter, 1, true)))
+                return bail(rc);
+            p.rec_chunked = dflag;
+            s->rc.n_chunks = (int)chunks.size();
+            s->rc.n_chunked = (int)recv.size();
+            s->rc.chunk = dch;
+            s->rc.receiver = drecv;
+            s->rc.rchunk = drch;
+            s->rc.cell = p.rec_cell;
+        }
+    }
+
     cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
     e = cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming);
@@ -827,6 +865,7 @@ int ts_profile_steps(ts_sim *s, int32_t n_steps, void *stream, float *ms_per_ker
         for (int part = 0; part < 2; ++part) {
             if (s->dims == 2) ts::launch_step_2d(s->p, s->ord, s->zen_mode, j, st, 1 << part);
             else ts::launch_step_3d(s->p, s->ord, s->zen_mode, j, st, 1 << part);
+            if (part == 1) ts::launch_receiver_chunks(s->p, s->rc, j, st);   // with the velocity update
             TS_CUDA(cudaEventRecord(ev[2 * j + part + 1], st));
         }
     }
@@ -886,6 +925,7 @@ int ts_run(ts_sim *s, int32_t n_steps, void *stream) {
         for (int j = 0; j < count; ++j) {
             if (s->dims == 2) ts::launch_step_2d(s->p, s->ord, s->zen_mode, j, where);
             else ts::launch_step_3d(s->p, s->ord, s->zen_mode, j, where);
+            ts::launch_receiver_chunks(s->p, s->rc, j, where);
         }
         ts::launch_advance(s->step_base, count, where);
     };
@@ -976,6 +1016,21 @@ int ts_device_buffer(ts_sim *s, int32_t what, void **dev_ptr, size_t *pitch_byte
     if (what < TS_VX || what > TS_SYZ || !s->field[what]) return fail(TS_E_ARG, "no such field");
     *dev_ptr = s->field[what];
     if (pitch_bytes) *pitch_bytes = (size_t)s->pitch * sizeof(float);
+    return TS_OK;
+}
+
+int ts_copy_field(ts_sim *s, int32_t what, void *dst, size_t dst_pitch, void *stream) {
+    if (!s || !dst) return fail(TS_E_ARG, "null argument");
+    if (what < TS_VX || what > TS_SYZ || !s->field[what]) return fail(TS_E_ARG, "no such field");
+    TS_CUDA(cudaSetDevice(s->device));
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : s->stream;
+    const int last = s->dims == 2 ? s->ny : s->nz;
+    const size_t rows = (size_t)s->nx * (s->dims == 2 ? 1 : s->ny);
+    const size_t width = (size_t)last * sizeof(float);
+    if (dst_pitch == 0) dst_pitch = width;
+    if (dst_pitch < width) return fail(TS_E_ARG, "dst_pitch smaller than a row");
+    TS_CUDA(cudaMemcpy2DAsync(dst, dst_pitch, s->field[what], (size_t)s->pitch * sizeof(float), width, rows,
+                              cudaMemcpyDefault, st));
     return TS_OK;
 }
 

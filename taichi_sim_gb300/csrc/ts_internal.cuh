@@ -66,6 +66,7 @@ struct alignas(16) Pal3 {
 struct StepParams {
     int family;
     int tx;                // 2D: nodes each thread updates along x (1, 2 or 4)
+    int xy_sweep_3d;       // 3D velocity kernel: warps interior in x and y take the x-y sweep
     int nx, ny, nz;        // nz = 1 in 2D
     int pitch;             // padded last-axis length (floats)
     int64_t plane;         // ny * pitch (3D x stride); 2D: pitch
@@ -114,6 +115,7 @@ struct StepParams {
     const int64_t *rec_cell;
     const int *rec_first_step;  // record at step k if k >= rec_first_step[s]
     float *traces;              // [rows][n_rec]
+    const unsigned char *rec_chunked;  // [n_rec] or null: 1 = summed by k_receiver_chunks, not inline
 
     // stability bookkeeping
     float v2_threshold;     // a step is unstable when !(v2 <= threshold)
@@ -124,6 +126,22 @@ struct StepParams {
     // 2D adjoint record of one step, [kFeat][grid_elems] (launch_step_2d_feat)
     float *feat;
 };
+
+// Receivers with many points, summed after the velocity kernel of every
+// step in chunks (ts_receivers.cu).
+constexpr int kChunkedMinPoints = 64;   // more points than this: chunked
+constexpr int kChunkPoints = 1024;      // points per chunk
+struct RecChunks {
+    int n_chunks;               // blocks of k_receiver_chunks
+    int n_chunked;              // receivers it sums
+    const int2 *chunk;          // [n_chunks]: point range [x, y) of the receiver CSR
+    const int *receiver;        // [n_chunked]: receiver index
+    const int *rchunk;          // [n_chunked + 1]: chunk range of each
+    const int64_t *cell;        // the CSR's node offsets
+    float *partial;             // [n_chunks]: this step's chunk sums
+    unsigned *counter;          // blocks done this step (the last one resets it)
+};
+void launch_receiver_chunks(const StepParams &p, const RecChunks &rc, int j, cudaStream_t st);
 
 // Arguments of the persistent 2D elastic step kernel (ts_persist2d.cu): the
 // regular kernels' parameters plus the exchange buffers between blocks.

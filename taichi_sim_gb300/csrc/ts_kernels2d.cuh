@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
 
     // receivers: global thread g samples receiver g (syy is final for step k)
     const int g = blk * (kBX2 * kBY2) + tid;
-    if (g < p.n_rec && k >= __ldg(p.rec_first_step + g)) {
+    if (g < p.n_rec && k >= __ldg(p.rec_first_step + g) && !(p.rec_chunked && p.rec_chunked[g])) {
         float acc = 0.f;
         for (int q = __ldg(p.rec_start + g); q < __ldg(p.rec_start + g + 1); ++q) acc += ldf(syy + __ldg(p.rec_cell + q));
         p.traces[(int64_t)k * p.n_rec + g] = acc;

@@ -106,6 +106,17 @@ __device__ __forceinline__ bool interior_warp(const StepParams &p, int y, int z,
     return __all_sync(0xffffffffu, lane);
 }
 
+// A warp interior along x and y (its TX-node chunk and its y row outside
+// the x and y strips and away from those grid edges) whose z run may cross
+// a z strip or the z edge: its per-node x and y tests compile out, the z
+// tests are per lane.
+template <int ORD, int TX>
+__device__ __forceinline__ bool xy_interior_warp(const StepParams &p, int y, int z, int x0, int sy) {
+    const bool lane = y < p.ny && sy < 0 && y >= ORD && y < p.ny - ORD && x0 >= ORD && x0 >= p.strip[0].lo &&
+                      x0 + TX + ORD <= p.nx && x0 + TX <= p.strip[0].hi;
+    return __all_sync(0xffffffffu, lane);
+}
+
 // sum_c cd[c] (w[ORD + c] - w[ORD - 1 - c])
 template <int ORD>
 __device__ __forceinline__ float wderiv(const float (&w)[2 * ORD], const float *cd) {
@@ -418,28 +429,34 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
     // vz region in (y, z); outside the vz region all three components are zero (wgsl:1754-1758)
     const bool yz_vz = col && y >= ORD && y < p.ny - ORD + 1 && z >= ORD - 1 && z < p.nz - ORD;
     const int q0 = __ldg(p.src_block_start + blk), q1 = __ldg(p.src_block_start + blk + 1);
-    const bool fast = interior_warp<ORD, TX>(p, y, z, x0, sy, sz) && q0 == q1;   // no source node in the block
+    // interior sweep (every test compiled out), x-y interior sweep (z tests
+    // per lane) or the general sweep; blocks with a source node take the
+    // general one
+    const bool fast = interior_warp<ORD, TX>(p, y, z, x0, sy, sz) && q0 == q1;
+    const bool fast_xy = !fast && q0 == q1 && p.xy_sweep_3d && xy_interior_warp<ORD, TX>(p, y, z, x0, sy);
     pdl_wait();
     const int k = *p.step_base + j;
     unsigned vmax = 0u;  // max |v|^2 as float bits (v2 >= 0 or NaN: NaN ranks highest)
     bool bad = false;
-    auto sweep = [&](auto fast_tag) {
-        constexpr bool FAST = decltype(fast_tag)::value;
-        const int syl = FAST ? -1 : sy, szl = FAST ? -1 : sz;
+    // MODE 2: interior warp; 1: x-y interior warp; 0: general
+    auto sweep = [&](auto mode_tag) {
+        constexpr int MODE = decltype(mode_tag)::value;
+        constexpr bool FAST = MODE == 2, XY = MODE >= 1;
+        const int syl = XY ? -1 : sy, szl = FAST ? -1 : sz;
         // sxx planes [x-ORD, x+ORD-1] (vx), sxy and sxz planes [x-ORD+1, x+ORD] (vy, vz)
         float wa[2 * ORD], wb[2 * ORD], wc[2 * ORD];
-        xwindow<ORD, !FAST>(wa, sxx, x0 - ORD, p.nx, X, yz);
-        xwindow<ORD, !FAST>(wb, sxy, x0 - ORD + 1, p.nx, X, yz);
-        xwindow<ORD, !FAST>(wc, sxz, x0 - ORD + 1, p.nx, X, yz);
+        xwindow<ORD, !XY>(wa, sxx, x0 - ORD, p.nx, X, yz);
+        xwindow<ORD, !XY>(wb, sxy, x0 - ORD + 1, p.nx, X, yz);
+        xwindow<ORD, !XY>(wc, sxz, x0 - ORD + 1, p.nx, X, yz);
 #pragma unroll
         for (int t = 0; t < TX; ++t) {
             const int x = x0 + t;
-            if (!FAST && x >= p.nx) break;
+            if (!XY && x >= p.nx) break;
             const I i = (I)x * X + yz;
-            const bool in_vz = FAST || (yz_vz && x >= ORD - 1 && x < p.nx - ORD);
-            const bool in_vx = FAST || (in_vz && x >= ORD && z >= ORD);        // vx region within the vz region
-            const bool in_vy = FAST || (in_vz && y < p.ny - ORD && z >= ORD);  // vy region within the vz region
-            const int sx = FAST ? -1 : strip_index(p.strip[0], x);
+            const bool in_vz = FAST || (yz_vz && (XY || (x >= ORD - 1 && x < p.nx - ORD)));
+            const bool in_vx = FAST || (in_vz && (XY || x >= ORD) && z >= ORD);        // vx region within the vz region
+            const bool in_vy = FAST || (in_vz && (XY || y < p.ny - ORD) && z >= ORD);  // vy region within the vz region
+            const int sx = XY ? -1 : strip_index(p.strip[0], x);
             const I ix = ((I)sx * p.ny + y) * Y + z;
             const I iy = ((I)x * p.strip[1].width + syl) * Y + z;
             const I iz = ((I)x * p.ny + y) * p.strip[2].width + szl;
@@ -526,7 +543,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
                 }
                 vzn = fmaf(a + b + e, dty, v0[2]);  // the vy-node density (wgsl3d:1748)
             }
-            if constexpr (!FAST) {
+            if constexpr (MODE == 0) {
                 for (int q = q0; q < q1; ++q) {
                     const Source s = p.src[q];
                     if (s.cell == i && k < p.src_rows)
@@ -540,18 +557,20 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
             bad |= !(v2 <= p.v2_threshold);
             vmax = max(vmax, __float_as_uint(v2));
             if (t + 1 < TX) {
-                xshift<ORD, !FAST>(wa, sxx, x + ORD, p.nx, X, yz);
-                xshift<ORD, !FAST>(wb, sxy, x + ORD + 1, p.nx, X, yz);
-                xshift<ORD, !FAST>(wc, sxz, x + ORD + 1, p.nx, X, yz);
+                xshift<ORD, !XY>(wa, sxx, x + ORD, p.nx, X, yz);
+                xshift<ORD, !XY>(wb, sxy, x + ORD + 1, p.nx, X, yz);
+                xshift<ORD, !XY>(wc, sxz, x + ORD + 1, p.nx, X, yz);
             }
         }
     };
-    if (fast) sweep(std::true_type{});
-    else if (col && x0 < p.nx) sweep(std::false_type{});
+    if (fast) sweep(std::integral_constant<int, 2>{});
+    else if (fast_xy) {
+        if (col) sweep(std::integral_constant<int, 1>{});
+    } else if (col && x0 < p.nx) sweep(std::integral_constant<int, 0>{});
 
     // receivers: global thread g samples receiver g (szz is final for step k)
     const int g = blk * (kBX3 * kBY3) + tid;
-    if (g < p.n_rec && k >= __ldg(p.rec_first_step + g)) {
+    if (g < p.n_rec && k >= __ldg(p.rec_first_step + g) && !(p.rec_chunked && p.rec_chunked[g])) {
         float acc = 0.f;
         for (int q = __ldg(p.rec_start + g); q < __ldg(p.rec_start + g + 1); ++q) acc += fld(szz + __ldg(p.rec_cell + q));
         p.traces[(int64_t)k * p.n_rec + g] = acc;

@@ -7,24 +7,29 @@
 namespace ts {
 namespace {
 
-template <int ORD, int MINB>
+template <int ORD, int MINB, int MINB_Q>
 void launch_feat_mb(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
     constexpr int TX = 2;
     const dim3 block(kBX2, kBY2), grid((p.ny + kBX2 - 1) / kBX2, (p.nx + kBY2 * TX - 1) / (kBY2 * TX));
     const bool three = p.zen.n == 3;
     if (zen_mode == 0) launch_pdl(k_stress2d<ORD, 1, 0, 0, TX, true, MINB>, grid, block, st, p);
     else if (zen_mode == 1 && three) launch_pdl(k_stress2d<ORD, 1, 1, 3, TX, true, MINB>, grid, block, st, p);
-    else if (zen_mode == 1) launch_pdl(k_stress2d<ORD, 1, 1, kMaxSls, TX, true, MINB>, grid, block, st, p);
-    else if (three) launch_pdl(k_stress2d<ORD, 1, 2, 3, TX, true, MINB>, grid, block, st, p);
-    else launch_pdl(k_stress2d<ORD, 1, 2, kMaxSls, TX, true, MINB>, grid, block, st, p);
+    else if (zen_mode == 1) launch_pdl(k_stress2d<ORD, 1, 1, kMaxSls, TX, true, MINB_Q>, grid, block, st, p);
+    else if (three) launch_pdl(k_stress2d<ORD, 1, 2, 3, TX, true, MINB_Q>, grid, block, st, p);
+    else launch_pdl(k_stress2d<ORD, 1, 2, kMaxSls, TX, true, MINB_Q>, grid, block, st, p);
     launch_pdl(k_velocity2d<ORD, 1, TX, true, MINB>, grid, block, st, p, j);
 }
 
-// Register budget: 3 resident blocks per SM (ord 2 to 4), which spills
-// nothing; ord 5, 6 keep the compiler's choice (0: no constraint).
+// Register budget: order 2 takes 4 resident blocks per SM (64 registers:
+// the velocity kernel and the elastic and three-mechanism stress kernels
+// spill at most 12 bytes) except where the per-cell scales or eight
+// mechanisms would spill more (3 blocks); orders 3 and 4 take 3 blocks,
+// which spills nothing; orders 5 and 6 keep the compiler's choice.
 template <int ORD>
 void launch_feat(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
-    launch_feat_mb<ORD, ORD <= 4 ? 3 : 0>(p, zen_mode, j, st);
+    constexpr int mb = ORD == 2 ? 4 : (ORD <= 4 ? 3 : 0);
+    constexpr int mbq = ORD <= 4 ? 3 : 0;
+    launch_feat_mb<ORD, mb, mbq>(p, zen_mode, j, st);
 }
 
 }  // namespace

@@ -83,6 +83,7 @@ def load_library(build_if_missing=True):
                                  ctypes.c_int),
             "ts_launches_per_step": ([P, _i], ctypes.c_int),
             "ts_step_path": ([P, _i], ctypes.c_int),
+            "ts_copy_field": ([P, ctypes.c_int32, P, ctypes.c_size_t, P], ctypes.c_int),
             "ts_destroy": ([P], None),
             "ts_strerror": ([ctypes.c_int], ctypes.c_char_p),
             "ts_last_error": ([], ctypes.c_char_p),
@@ -273,6 +274,14 @@ class Stepper:
         p, pitch = ctypes.c_void_p(), ctypes.c_size_t()
         _check(self._lib.ts_device_buffer(self._h, code, ctypes.byref(p), ctypes.byref(pitch)), "ts_device_buffer")
         return p.value, pitch.value
+
+    def copy_field(self, what, dst_ptr, dst_pitch=0, stream=None):
+        """Enqueue a copy of a field (after the steps queued so far) to device
+        or pinned host memory at ``dst_ptr`` (packed rows unless
+        ``dst_pitch`` bytes); does not wait (``ts_copy_field``)."""
+        code = FIELD_NAMES.get(what, what) if isinstance(what, str) else what
+        _check(self._lib.ts_copy_field(self._h, code, ctypes.c_void_p(dst_ptr), int(dst_pitch),
+                                       ctypes.c_void_p(stream or 0)), "ts_copy_field")
 
     def close(self):
         if getattr(self, "_h", None):

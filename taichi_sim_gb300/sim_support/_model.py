@@ -32,9 +32,11 @@ from .emission_law import EmissionLaw
 from .simul_classes import (SimulationROI, SimulationProbeLinearArray, SimulationProbePoint,
                             SimulationProbeMonoCirc, SimulationProbeMatrix)
 
+# (save_snapshots is an addition: the headless stand-in for the live view,
+# which show_anim also turns on)
 _CONFIG_FLAGS = ("show_anim", "show_debug", "show_figs", "plot_results", "plot_error", "plot_sensors",
                  "plot_bscan", "save_results", "save_field", "save_sensors", "save_bscan", "save_sources",
-                 "source_env")
+                 "source_env", "save_snapshots")
 
 
 def load_config(file_config):

@@ -10,7 +10,12 @@ and the step-loop time.
 
 ``run()`` here is headless: the reference's matplotlib figures and Qt live
 view need a graphics stack, so figures are produced only when matplotlib is
-importable, and the live view is replaced by nothing.  Result files keep the
+importable, and the live view (sim_taichi_elastic.py:320-329,
+sim_support/windows_qt.py) is replaced by field snapshots: with
+``show_anim`` (or ``save_snapshots``) set, a backend returns the ROI of the
+field at every step the live view would show (``it % it_display == 0`` or
+``it == 5``, 1-based) under ``"snapshots"``/``"snapshot_steps"``, and
+``run()`` saves them next to the other results.  Result files keep the
 reference's names.
 """
 import os.path
@@ -20,6 +25,17 @@ from time import time
 import numpy as np
 
 from ._model import ModelBase
+
+
+def snapshot_steps(n_steps, it_display):
+    """The 1-based steps after which the reference's live view shows the
+    field: ``it % it_display == 0`` or ``it == 5``
+    (sim_taichi_elastic.py:320, sim_webgpu_viscoelastic.py:519)."""
+    every = max(1, int(it_display))
+    steps = set(range(every, int(n_steps) + 1, every))
+    if n_steps >= 5:
+        steps.add(5)
+    return sorted(steps)
 
 
 def _field_and_traces(results):
@@ -96,6 +112,9 @@ class ExperimentDriver:
                     np.save(name + ('_field_pressure' if kind == "pressure" else '_field_stress_yy'), field)
                 if self._save_bscan:
                     np.save(name + f'_bscan_{kind}', traces)
+                if "snapshots" in results:   # the live view's frames, headless
+                    np.save(name + f'_snapshots_{kind}', results["snapshots"])
+                    np.save(name + '_snapshot_steps', np.asarray(results["snapshot_steps"], np.int32))
                 self._maybe_plot(law, field, traces, name, kind)
 
         sim_times, total_times = np.array(sim_times), np.array(total_times)
@@ -198,4 +217,4 @@ class Simulator(ExperimentDriver, ModelBase):
     _dims = 2
 
 
-__all__ = ["Simulator", "ExperimentDriver"]
+__all__ = ["Simulator", "ExperimentDriver", "snapshot_steps"]

@@ -137,3 +137,37 @@ def test_cuda_backend_batches_the_laws_through_the_batched_stepper(tmp_path, mon
     assert [set(r) for r in out] == [{"stress", "sens_stress", "gpu_str", "sim_time"}] * 2
     np.testing.assert_array_equal(seen["shots"], batch.focal_law_shot_sources(sim, laws))
     assert out[1]["sens_stress"][0, 0] == 1.0
+
+
+def test_snapshot_steps_follow_the_live_view():
+    from taichi_sim_gb300.sim_support.simulator import snapshot_steps
+    assert snapshot_steps(240, 50) == [5, 50, 100, 150, 200]
+    assert snapshot_steps(100, 5) == list(range(5, 101, 5))
+    assert snapshot_steps(4, 10) == []
+    assert snapshot_steps(30, 0) == list(range(1, 31))
+
+
+class SnapshotBackend(FakeBackend):
+    """A stand-in backend that returns the live view's frames."""
+
+    def _result(self, k):
+        from taichi_sim_gb300.sim_support.simulator import snapshot_steps
+        res = super()._result(k)
+        steps = snapshot_steps(self._n_steps, self._it_display)
+        res["snapshots"] = np.stack([np.full((3, 4), float(s), np.float32) for s in steps])
+        res["snapshot_steps"] = steps
+        return res
+
+
+def test_run_saves_snapshots_when_a_backend_returns_them(tmp_path):
+    cfg = _cfg(tmp_path)
+    cfg["simul_configs"]["save_snapshots"] = 1
+    sim = SnapshotBackend(cfg)
+    assert sim._save_snapshots
+    sim.run()
+    snaps = glob.glob(str(tmp_path / "result_fake_*_snapshots_stress.npy"))
+    steps = glob.glob(str(tmp_path / "result_fake_*_snapshot_steps.npy"))
+    assert len(snaps) == 1 and len(steps) == 1
+    s, k = np.load(snaps[0]), np.load(steps[0])
+    np.testing.assert_array_equal(k, [5, 50])   # 50 steps, it_display 50
+    np.testing.assert_array_equal(s[:, 0, 0], [5.0, 50.0])
