@@ -497,7 +497,7 @@ struct ts_adj {
     void forward_step(int k, float *rec, cudaStream_t st) {
         sp.feat = rec;
         if (rec) launch_step_2d_feat(sp, ord, zm, k, st);
-        else launch_step_2d(sp, ord, zm, k, st);
+        else launch_step_2d_folded(sp, ord, zm, k, st);
         sp.feat = nullptr;
         launches += 2;
     }

@@ -394,6 +394,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         for (int c = 0; c < ts::kMaxOrd; ++c) p.cd[a][c] = c < ord ? d->coefs[c] / steps[a] : 0.f;
     for (int c = 0; c < ts::kMaxOrd; ++c) p.coef[c] = c < ord ? d->coefs[c] : 0.f;
     for (int a = 0; a < 3; ++a) p.od[a] = steps[a] > 0.f ? 1.f / steps[a] : 0.f;
+    for (int a = 0; a < 3; ++a) p.dd[a] = steps[a];
     p.dt = d->dt;
 
     // ---- CPML tables and strips ----
@@ -446,7 +447,6 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     std::vector<float> mus[3];
     const int n_shear = s->dims == 2 ? 1 : 3;
     for (int k = 0; k < n_shear; ++k) mus[k].assign(s->grid_elems, 0.f);
-    auto inv_or0 = [&](float r) { return r > 0.f ? dt / r : 0.f; };
     if (s->dims == 2) {
         // normal node x-averaged (mu zero where either cs is zero), shear
         // node y-averaged, vy node 4-point averaged (ts_prep.h)
@@ -454,19 +454,13 @@ int ts_create(const ts_desc *d, ts_sim **out) {
             for (int y = 0; y < ny; ++y) {
                 const int64_t i = s->at(x, y);
                 const ts::Coef2D c = ts::coef_2d(d, x, y);
-                if (s->family == TS_TAICHI2D) {   // the kernels keep the reference's operation order
-                    lam[i] = c.lam_raw;
-                    mu[i] = c.mu_raw;
-                    mus[0][i] = c.mus_raw;
-                    dtr0[i] = c.rho_vx;
-                    dtr1[i] = c.rho_vy;
-                } else {
-                    lam[i] = c.lam;
-                    mu[i] = c.mu;
-                    mus[0][i] = c.mus;
-                    dtr0[i] = c.dtr_vx;
-                    dtr1[i] = c.dtr_vy;
-                }
+                // raw moduli and densities: the kernels multiply by dt and
+                // divide by rho as the reference does
+                lam[i] = c.lam_raw;
+                mu[i] = c.mu_raw;
+                mus[0][i] = c.mus_raw;
+                dtr0[i] = c.rho_vx;
+                dtr1[i] = c.rho_vy;
             }
     } else {
         for (int x = 0; x < nx; ++x)
@@ -474,19 +468,19 @@ int ts_create(const ts_desc *d, ts_sim **out) {
                 for (int z = 0; z < nz; ++z) {
                     const int64_t i = s->at(x, y, z);
                     const float r = rho(x, y, z), cp = cpv(x, y, z), cs = csv(x, y, z);
-                    lam[i] = r * (cp * cp - 2.f * cs * cs) * dt;
-                    mu[i] = r * (cs * cs) * dt;
+                    lam[i] = r * (cp * cp - 2.f * cs * cs);   // raw: the kernels multiply by dt
+                    mu[i] = r * (cs * cs);
                     const float rxy = 0.25f * (rho(x + 1, y, z) + rho(x, y, z) + rho(x, y + 1, z) + rho(x + 1, y + 1, z));
                     const float cxy = 0.25f * (csv(x + 1, y, z) + csv(x, y, z) + csv(x, y + 1, z) + csv(x + 1, y + 1, z));
                     const float rxz = 0.25f * (rho(x + 1, y, z) + rho(x, y, z) + rho(x, y, z + 1) + rho(x + 1, y, z + 1));
                     const float cxz = 0.25f * (csv(x + 1, y, z) + csv(x, y, z) + csv(x, y, z + 1) + csv(x + 1, y, z + 1));
                     const float ryz = 0.25f * (rho(x, y + 1, z) + rho(x, y, z) + rho(x, y, z + 1) + rho(x, y + 1, z + 1));
                     const float cyz = 0.25f * (csv(x, y + 1, z) + csv(x, y, z) + csv(x, y, z + 1) + csv(x, y + 1, z + 1));
-                    mus[0][i] = rxy * (cxy * cxy) * dt;
-                    mus[1][i] = rxz * (cxz * cxz) * dt;
-                    mus[2][i] = ryz * (cyz * cyz) * dt;
-                    dtr0[i] = inv_or0(0.5f * (rho(x + 1, y, z) + r));
-                    dtr1[i] = inv_or0(0.5f * (rho(x, y + 1, z) + r));
+                    mus[0][i] = rxy * (cxy * cxy);
+                    mus[1][i] = rxz * (cxz * cxz);
+                    mus[2][i] = ryz * (cyz * cyz);
+                    dtr0[i] = 0.5f * (rho(x + 1, y, z) + r);   // raw: the kernels divide by rho
+                    dtr1[i] = 0.5f * (rho(x, y + 1, z) + r);
                 }
     }
     // ---- attenuation ----
@@ -590,7 +584,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
                         r = 0.5f * (rho(x, y + 1, z) + rho(x, y, z));
                     }
                     if (!(r > 0.f)) continue;
-                    const float scale = s->family == TS_TAICHI2D ? r : dt / r;
+                    const float scale = r;   // the kernels divide by rho
                     if (!col_of.count(idx)) {
                         const int c = (int)col_of.size();
                         col_of[idx] = c;

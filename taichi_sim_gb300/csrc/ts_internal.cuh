@@ -50,7 +50,7 @@ struct Zener {
 struct Source {
     int64_t cell;   // flat padded offset
     int col;        // column of the device source table
-    float scale;    // dt / rho at the node (the reference divides by rho); TS_TAICHI2D: rho
+    float scale;    // rho at the node (stepper), or dt / rho (adjoint forward, batched kernels)
 };
 
 // Everything a 2D or 3D kernel reads, passed by value.
@@ -71,10 +71,12 @@ struct StepParams {
     int pitch;             // padded last-axis length (floats)
     int64_t plane;         // ny * pitch (3D x stride); 2D: pitch
     float cd[3][kMaxOrd];  // coef[c] / d_axis (x, y, z)
-    // the reference's own factors, for the family whose kernels keep its
-    // operation order (TS_TAICHI2D): coef[c], 1 / d_axis (float), dt
+    // the reference's own factors, for the arithmetic that divides as the
+    // reference does (TS_TAICHI2D, and TS_WGSL2D/3D through the stepper):
+    // coef[c], 1 / d_axis (float), d_axis, dt
     float coef[kMaxOrd];
     float od[3];
+    float dd[3];           // the grid steps themselves
     float dt;
 
     // fields
@@ -88,9 +90,9 @@ struct StepParams {
     // velocity kernel psi of stress derivatives (see ts_stepper*.cu)
     float *psi[18];
 
-    // per-cell coefficients (family TS_TAICHI2D: lambda, mu, mu at the
-    // shear node, rho at the vx node and the averaged rho at the vy node,
-    // not folded with dt)
+    // per-cell coefficients (the stepper's families: lambda, mu, mu at the
+    // shear node(s), rho at the velocity nodes, not folded with dt; the
+    // adjoint's forward and the batched kernels: lambda dt, mu dt, dt / rho)
     const float *lam_dt, *mu_dt;          // normal node
     const float *mus_dt[3];               // shear nodes xy, xz, yz (2D: xy)
     const float *dtr[3];                  // dt / rho at vx, vy, vz nodes (0: no update)
@@ -198,6 +200,24 @@ __device__ __forceinline__ float taichi_velocity(float v, float f, float src, fl
     return rho > 0.f ? __fadd_rn(v, __fadd_rn(src, __fdiv_rn(__fmul_rn(f, dt), rho))) : v;
 }
 
+// x / b without a division instruction, rounded as the division almost
+// always is (Markstein's correction step with r = RN(1/b)): q = x r,
+// e = x - q b exactly (fma), q + e r.
+__device__ __forceinline__ float qdiv(float x, float b, float r) {
+    const float q = x * r;
+    const float e = fmaf(-q, b, x);
+    return fmaf(e, r, q);
+}
+// WGSL velocity update v + (f dt) / rho, none where rho <= 0
+// (shader_webgpu_viscoelastic.wgsl:1020-1024, 1049-1052)
+__device__ __forceinline__ float wgsl_velocity(float v, float f, float rho, float dt) {
+    return rho > 0.f ? v + qdiv(f * dt, rho, __frcp_rn(rho)) : v;
+}
+// WGSL source force src dt / rho (wgsl:1059-1065)
+__device__ __forceinline__ float wgsl_source(float src, float rho, float dt) {
+    return qdiv(src * dt, rho, __frcp_rn(rho));
+}
+
 // Slots of the 2D adjoint record: what the stress and velocity updates
 // multiply lambda*dt, mu*dt (normal node: x and y rows), mu*dt (shear node)
 // and dt/rho (vx, vy nodes) by.
@@ -244,8 +264,10 @@ inline void launch_pdl(void (*kern)(Params...), dim3 grid, dim3 block, cudaStrea
 // Launch helpers (defined per dimension).  `parts` selects the kernels of
 // one step: 1 = stress, 2 = velocity, 3 = both (in that order).
 void launch_step_2d(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st, int parts = 3);
-// Family TS_WGSL2D step that also writes the adjoint record to p.feat
-// (p.tx must be 2).
+// Family TS_WGSL2D step with coefficients folded with dt (the adjoint's
+// forward; p.tx must be 2, ord 2 or 4), without and with the adjoint record
+// written to p.feat.
+void launch_step_2d_folded(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st);
 void launch_step_2d_feat(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st);
 void launch_step_3d(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st, int parts = 3);
 // the palette instantiations of the stress kernels (p.pal set; 32-bit offsets)

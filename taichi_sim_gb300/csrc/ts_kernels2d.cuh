@@ -41,7 +41,27 @@
 namespace ts {
 namespace {
 
-constexpr int kTaichi = 0;
+// Arithmetic families of the 2D kernels: kTaichi keeps the Taichi kernels'
+// operation order exactly (coefficient arrays hold lambda, mu, rho); kWgsl
+// is the WGSL semantics with the grid-step and density divisions done once
+// per derivative and per update, each rounded as a division (coefficient
+// arrays hold lambda, mu, rho; sums contract to fma), so no step of the
+// update carries a rounding bias that repeats at every node and time step;
+// kWgslFolded is the WGSL semantics with dt, 1/dx and 1/rho folded into the
+// coefficients (arrays hold lambda dt, mu dt, dt / rho), the form the
+// adjoint differentiates (ts_adjoint.cu).
+constexpr int kTaichi = 0, kWgslFolded = 1, kWgsl = 2;
+
+// weight of derivative term c along axis a: coef / d (folded) or coef
+template <int FAM>
+__device__ __forceinline__ float dw(const StepParams &p, int a, int c) {
+    return FAM == kWgsl ? p.coef[c] : p.cd[a][c];
+}
+// a derivative's sum of weighted differences, divided by the grid step (kWgsl)
+template <int FAM>
+__device__ __forceinline__ float dfin(float s, const StepParams &p, int a) {
+    return FAM == kWgsl ? qdiv(s, p.dd[a], p.od[a]) : s;
+}
 
 // Loads.  ldg: data no kernel writes (coefficients, tables), through the
 // read-only path.  ldf: fields the previous kernel of the stream wrote.  With
@@ -56,6 +76,17 @@ __device__ __forceinline__ float ldf(const float *p) { return __ldca(p); }
 __device__ __forceinline__ float cpml(float d, float psi_old, float &psi_new, const Cpml &t) {
     psi_new = fmaf(t.b, psi_old, t.a * d);
     return fmaf(d, t.ik, psi_new);
+}
+
+// CPML update in the family's arithmetic
+template <int FAM>
+__device__ __forceinline__ float cpmlf(float d, float psi_old, float &psi_new, const Cpml &t) {
+    if (FAM == kTaichi) return taichi_cpml(d, psi_old, psi_new, t);
+    if (FAM == kWgsl) {
+        psi_new = fmaf(t.b, psi_old, t.a * d);
+        return qdiv(d, t.k, t.ik) + psi_new;
+    }
+    return cpml(d, psi_old, psi_new, t);
 }
 
 // Window of 2*ORD rows of one field at column y, first row `r0`; rows
@@ -173,16 +204,18 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
                             ddx = taichi_term(ddx, p.coef[c], wvx[c + ORD], wvx[ORD - 1 - c], p.od[0]);
                             ddy = taichi_term(ddy, p.coef[c], hi, ny_lo[c], p.od[1]);
                         } else {
-                            ddx = fmaf(p.cd[0][c], wvx[c + ORD] - wvx[ORD - 1 - c], ddx);
-                            ddy = fmaf(p.cd[1][c], hi - ny_lo[c], ddy);
+                            ddx = fmaf(dw<FAM>(p, 0, c), wvx[c + ORD] - wvx[ORD - 1 - c], ddx);
+                            ddy = fmaf(dw<FAM>(p, 1, c), hi - ny_lo[c], ddy);
                         }
                     }
+                    ddx = dfin<FAM>(ddx, p, 0);
+                    ddy = dfin<FAM>(ddy, p, 1);
                     if (sx >= 0) {
-                        ddx = FAM == kTaichi ? taichi_cpml(ddx, pn0, np_, p.tab_h[0][x]) : cpml(ddx, pn0, np_, p.tab_h[0][x]);
+                        ddx = cpmlf<FAM>(ddx, pn0, np_, p.tab_h[0][x]);
                         p.psi[0][ix] = np_;
                     }
                     if (syl >= 0) {
-                        ddy = FAM == kTaichi ? taichi_cpml(ddy, pn1, np_, p.tab_f[1][y]) : cpml(ddy, pn1, np_, p.tab_f[1][y]);
+                        ddy = cpmlf<FAM>(ddy, pn1, np_, p.tab_f[1][y]);
                         p.psi[2][iy] = np_;
                     }
                     if (FAM == kTaichi) {
@@ -209,8 +242,13 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
                             ux = fmaf(hl, srxx, fmaf(M, sryy, ux));
                             uy = fmaf(hl, srxx, fmaf(-M, sryy, uy));
                         }
-                        sxx += ux;
-                        syy += uy;
+                        if (FAM == kWgsl) {   // (...) dt, wgsl:915-916
+                            sxx += ux * p.dt;
+                            syy += uy * p.dt;
+                        } else {
+                            sxx += ux;
+                            syy += uy;
+                        }
                         if (FEAT) {
                             const float h = 0.5f * srxx;
                             p.feat[kFeatLam * p.grid_elems + i] = ddx + ddy + h;
@@ -231,16 +269,18 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
                             a = taichi_term(a, p.coef[c], wvy[c + ORD], wvy[ORD - 1 - c], p.od[0]);
                             b = taichi_term(b, p.coef[c], sx_hi[c], lo, p.od[1]);
                         } else {
-                            a = fmaf(p.cd[0][c], wvy[c + ORD] - wvy[ORD - 1 - c], a);
-                            b = fmaf(p.cd[1][c], sx_hi[c] - lo, b);
+                            a = fmaf(dw<FAM>(p, 0, c), wvy[c + ORD] - wvy[ORD - 1 - c], a);
+                            b = fmaf(dw<FAM>(p, 1, c), sx_hi[c] - lo, b);
                         }
                     }
+                    a = dfin<FAM>(a, p, 0);
+                    b = dfin<FAM>(b, p, 1);
                     if (sx >= 0) {
-                        a = FAM == kTaichi ? taichi_cpml(a, ps0, np_, p.tab_f[0][x]) : cpml(a, ps0, np_, p.tab_f[0][x]);
+                        a = cpmlf<FAM>(a, ps0, np_, p.tab_f[0][x]);
                         p.psi[1][ix] = np_;
                     }
                     if (syl >= 0) {
-                        b = FAM == kTaichi ? taichi_cpml(b, ps1, np_, p.tab_h[1][y]) : cpml(b, ps1, np_, p.tab_h[1][y]);
+                        b = cpmlf<FAM>(b, ps1, np_, p.tab_h[1][y]);
                         p.psi[3][iy] = np_;
                     }
                     if (FAM == kTaichi) {
@@ -259,7 +299,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
                             u = fmaf(0.5f * Ms, sr, u);
                         }
                         if (FEAT) p.feat[kFeatShear * p.grid_elems + i] = fmaf(0.5f, sr, e);
-                        p.s[3][i] = sxy + u;
+                        p.s[3][i] = FAM == kWgsl ? sxy + u * p.dt : sxy + u;
                     }
                 }
             }
@@ -336,12 +376,15 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                     a = taichi_term(a, p.coef[c], rxx[t + ORD + c], rxx[t + ORD - 1 - c], p.od[0]);
                     b = taichi_term(b, p.coef[c], hi, bl[t][c], p.od[1]);
                 } else {
-                    a = fmaf(p.cd[0][c], rxx[t + ORD + c] - rxx[t + ORD - 1 - c], a);
-                    b = fmaf(p.cd[1][c], hi - bl[t][c], b);
+                    a = fmaf(dw<FAM>(p, 0, c), rxx[t + ORD + c] - rxx[t + ORD - 1 - c], a);
+                    b = fmaf(dw<FAM>(p, 1, c), hi - bl[t][c], b);
                 }
             }
+            a = dfin<FAM>(a, p, 0);
+            b = dfin<FAM>(b, p, 1);
             const float fax = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
-            const float vxn = FAM == kTaichi ? taichi_velocity(vx0[t], fax, 0.f, dx0[t], p.dt) : fmaf(fax, dx0[t], vx0[t]);
+            const float vxn = FAM == kTaichi ? taichi_velocity(vx0[t], fax, 0.f, dx0[t], p.dt) : FAM == kWgsl ? wgsl_velocity(vx0[t], fax, dx0[t], p.dt)
+                                                   : fmaf(fax, dx0[t], vx0[t]);
             a = 0.f;
             b = 0.f;
 #pragma unroll
@@ -350,12 +393,15 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                     a = taichi_term(a, p.coef[c], rxy[t + ORD + c], rxy[t + ORD - 1 - c], p.od[0]);
                     b = taichi_term(b, p.coef[c], by[t][ORD + c], by[t][ORD - 1 - c], p.od[1]);
                 } else {
-                    a = fmaf(p.cd[0][c], rxy[t + ORD + c] - rxy[t + ORD - 1 - c], a);
-                    b = fmaf(p.cd[1][c], by[t][ORD + c] - by[t][ORD - 1 - c], b);
+                    a = fmaf(dw<FAM>(p, 0, c), rxy[t + ORD + c] - rxy[t + ORD - 1 - c], a);
+                    b = fmaf(dw<FAM>(p, 1, c), by[t][ORD + c] - by[t][ORD - 1 - c], b);
                 }
             }
+            a = dfin<FAM>(a, p, 0);
+            b = dfin<FAM>(b, p, 1);
             const float fay = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
-            const float vyn = FAM == kTaichi ? taichi_velocity(vy0[t], fay, 0.f, dy0[t], p.dt) : fmaf(fay, dy0[t], vy0[t]);
+            const float vyn = FAM == kTaichi ? taichi_velocity(vy0[t], fay, 0.f, dy0[t], p.dt) : FAM == kWgsl ? wgsl_velocity(vy0[t], fay, dy0[t], p.dt)
+                                                   : fmaf(fay, dy0[t], vy0[t]);
             p.v[0][i] = vxn;
             p.v[1][i] = vyn;
             if (FEAT) {
@@ -418,20 +464,24 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                         a = taichi_term(a, p.coef[c], wxx[c + ORD], wxx[ORD - 1 - c], p.od[0]);
                         b = taichi_term(b, p.coef[c], hi, bx_lo[c], p.od[1]);
                     } else {
-                        a = fmaf(p.cd[0][c], wxx[c + ORD] - wxx[ORD - 1 - c], a);
-                        b = fmaf(p.cd[1][c], hi - bx_lo[c], b);
+                        a = fmaf(dw<FAM>(p, 0, c), wxx[c + ORD] - wxx[ORD - 1 - c], a);
+                        b = fmaf(dw<FAM>(p, 1, c), hi - bx_lo[c], b);
                     }
                 }
+                a = dfin<FAM>(a, p, 0);
+                b = dfin<FAM>(b, p, 1);
                 if (sx >= 0) {
-                    a = FAM == kTaichi ? taichi_cpml(a, pxa, np_, p.tab_f[0][x]) : cpml(a, pxa, np_, p.tab_f[0][x]);
+                    a = cpmlf<FAM>(a, pxa, np_, p.tab_f[0][x]);
                     p.psi[4][ix] = np_;
                 }
                 if (syl >= 0) {
-                    b = FAM == kTaichi ? taichi_cpml(b, pxb, np_, p.tab_f[1][y]) : cpml(b, pxb, np_, p.tab_f[1][y]);
+                    b = cpmlf<FAM>(b, pxb, np_, p.tab_f[1][y]);
                     p.psi[6][iy] = np_;
                 }
                 fax = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
-                vxn = FAM == kTaichi ? taichi_velocity(vx0, fax, 0.f, dx0, p.dt) : fmaf(fax, dx0, vx0);
+                vxn = FAM == kTaichi ? taichi_velocity(vx0, fax, 0.f, dx0, p.dt)
+                      : FAM == kWgsl   ? wgsl_velocity(vx0, fax, dx0, p.dt)
+                                       : fmaf(fax, dx0, vx0);
             }
             if (in_vy) {
                 float a = 0.f, b = 0.f;
@@ -441,16 +491,18 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                         a = taichi_term(a, p.coef[c], wxy[c + ORD], wxy[ORD - 1 - c], p.od[0]);
                         b = taichi_term(b, p.coef[c], by[ORD + c], by[ORD - 1 - c], p.od[1]);
                     } else {
-                        a = fmaf(p.cd[0][c], wxy[c + ORD] - wxy[ORD - 1 - c], a);
-                        b = fmaf(p.cd[1][c], by[ORD + c] - by[ORD - 1 - c], b);
+                        a = fmaf(dw<FAM>(p, 0, c), wxy[c + ORD] - wxy[ORD - 1 - c], a);
+                        b = fmaf(dw<FAM>(p, 1, c), by[ORD + c] - by[ORD - 1 - c], b);
                     }
                 }
+                a = dfin<FAM>(a, p, 0);
+                b = dfin<FAM>(b, p, 1);
                 if (sx >= 0) {
-                    a = FAM == kTaichi ? taichi_cpml(a, pya, np_, p.tab_h[0][x]) : cpml(a, pya, np_, p.tab_h[0][x]);
+                    a = cpmlf<FAM>(a, pya, np_, p.tab_h[0][x]);
                     p.psi[5][ix] = np_;
                 }
                 if (syl >= 0) {
-                    b = FAM == kTaichi ? taichi_cpml(b, pyb, np_, p.tab_h[1][y]) : cpml(b, pyb, np_, p.tab_h[1][y]);
+                    b = cpmlf<FAM>(b, pyb, np_, p.tab_h[1][y]);
                     p.psi[7][iy] = np_;
                 }
                 fay = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
@@ -466,14 +518,15 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                     }
                     vyn = taichi_velocity(vy0, fay, src, dy0, p.dt);
                 } else {
-                    vyn = fmaf(fay, dy0, vy0);
+                    vyn = FAM == kWgsl ? wgsl_velocity(vy0, fay, dy0, p.dt) : fmaf(fay, dy0, vy0);
                 }
             }
             if constexpr (!FAST && FAM != kTaichi) {
                 for (int q = q0; q < q1; ++q) {
                     const Source s = p.src[q];
                     if (s.cell == i && k < p.src_rows)
-                        vyn = fmaf(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), s.scale, vyn);
+                        vyn = FAM == kWgsl ? vyn + wgsl_source(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), s.scale, p.dt)
+                                           : fmaf(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), s.scale, vyn);
                 }
             }
             p.v[0][i] = vxn;

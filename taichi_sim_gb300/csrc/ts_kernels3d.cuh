@@ -20,6 +20,12 @@
 // cs == 0 test, vz uses the vy-node density, all three velocities are zeroed
 // outside the vz region, the source drives vz).
 //
+// Arithmetic: as the shaders, every derivative divided by its grid step,
+// every update multiplied by dt and every velocity update divided by rho,
+// each division done once per derivative or update and rounded as a division
+// (qdiv), so that no folded constant (coef / d, lambda dt, dt / rho) biases
+// every node and step alike; sums contract to fma.
+//
 // Coefficients: with PAL the stress kernels take the per-node coefficients
 // from a palette (one 16-bit index per node into a table of the model's
 // distinct coefficient tuples, ts_internal.cuh: Pal3), otherwise from one
@@ -33,9 +39,10 @@
 namespace ts {
 namespace {
 
+// b * psi + a * d, then d / k + psi (the division as the shader's)
 __device__ __forceinline__ float cpml(float d, float psi_old, float &psi_new, const Cpml &t) {
     psi_new = fmaf(t.b, psi_old, t.a * d);
-    return fmaf(d, t.ik, psi_new);
+    return qdiv(d, t.k, t.ik) + psi_new;
 }
 
 // Load of a field value written by an earlier kernel of the stream.  With
@@ -64,12 +71,15 @@ __device__ __forceinline__ Pairs<ORD> load_pairs(const float *f, I i, I s) {
     return r;
 }
 
+// sum_c coef[c] (hi[c] - lo[c]) / d_axis: the shader divides every term by
+// the grid step (wgsl3d:1367-1369); the sum is divided once, so that no
+// rounding of coef / d biases every derivative alike
 template <int ORD>
-__device__ __forceinline__ float deriv(const Pairs<ORD> &q, const float *cd) {
+__device__ __forceinline__ float deriv(const Pairs<ORD> &q, const StepParams &p, int axis) {
     float a = 0.f;
 #pragma unroll
-    for (int c = 0; c < ORD; ++c) a = fmaf(cd[c], q.hi[c] - q.lo[c], a);
-    return a;
+    for (int c = 0; c < ORD; ++c) a = fmaf(p.coef[c], q.hi[c] - q.lo[c], a);
+    return qdiv(a, p.dd[axis], p.od[axis]);
 }
 
 // Resident blocks per SM the kernels are compiled for (register budgets 64
@@ -117,13 +127,13 @@ __device__ __forceinline__ bool xy_interior_warp(const StepParams &p, int y, int
     return __all_sync(0xffffffffu, lane);
 }
 
-// sum_c cd[c] (w[ORD + c] - w[ORD - 1 - c])
+// sum_c coef[c] (w[ORD + c] - w[ORD - 1 - c]) / dx
 template <int ORD>
-__device__ __forceinline__ float wderiv(const float (&w)[2 * ORD], const float *cd) {
+__device__ __forceinline__ float wderiv(const float (&w)[2 * ORD], const StepParams &p) {
     float a = 0.f;
 #pragma unroll
-    for (int c = 0; c < ORD; ++c) a = fmaf(cd[c], w[ORD + c] - w[ORD - 1 - c], a);
-    return a;
+    for (int c = 0; c < ORD; ++c) a = fmaf(p.coef[c], w[ORD + c] - w[ORD - 1 - c], a);
+    return qdiv(a, p.dd[0], p.od[0]);
 }
 
 // Normal stresses (sxx, syy, szz, their Zener memory variables and CPML
@@ -197,7 +207,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_normal3d(const
                 }
             }
             // ---- update: vx[x+c+1]-vx[x-c] from the window ----
-            float ddx = wderiv<ORD>(wx, p.cd[0]), ddy = deriv(n_y, p.cd[1]), ddz = deriv(n_z, p.cd[2]);
+            float ddx = wderiv<ORD>(wx, p), ddy = deriv(n_y, p, 1), ddz = deriv(n_z, p, 2);
             float np_;
             if (sx >= 0) {
                 ddx = cpml(ddx, pz0, np_, p.tab_h[0][x]);
@@ -238,9 +248,9 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_normal3d(const
                 uy = fmaf(hl23, srxx, fmaf(M, srzz, uy));
                 uz = fmaf(0.5f * L2M, srxx, fmaf(-M * (1.f / 3.f), sryy + srzz, uz));
             }
-            p.s[0][i] = s0 + ux;
-            p.s[1][i] = s1 + uy;
-            p.s[2][i] = s2 + uz;
+            p.s[0][i] = s0 + ux * p.dt;   // (...) dt, wgsl3d:1442-1449
+            p.s[1][i] = s1 + uy * p.dt;
+            p.s[2][i] = s2 + uz * p.dt;
         }
         if (t + 1 < kTX3S) xshift<ORD>(wx, vx, x + ORD + 1, p.nx, X, yz);
     }
@@ -336,8 +346,8 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_shear3d(const 
             float np_;
             // ---- sigma_xy: vy[x+c]-vy[x-c-1] (window), sigma_xz: vz[x+c]-vz[x-c-1] (window) ----
             if (in_xy) {
-                float a1 = wderiv<ORD>(wy, p.cd[0]), a2 = deriv(a_vx, p.cd[1]);
-                float b1 = wderiv<ORD>(wz, p.cd[0]), b2 = deriv(b_vx, p.cd[2]);
+                float a1 = wderiv<ORD>(wy, p), a2 = deriv(a_vx, p, 1);
+                float b1 = wderiv<ORD>(wz, p), b2 = deriv(b_vx, p, 2);
                 if (sx >= 0) {
                     a1 = cpml(a1, psi[0], np_, p.tab_f[0][x]);
                     p.psi[3][ix] = np_;
@@ -369,12 +379,12 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_shear3d(const 
                     u = fmaf(0.5f * Mxy, sa, u);
                     w = fmaf(0.5f * Mxz, sb, w);
                 }
-                p.s[3][i] = s_xy + u;
-                p.s[4][i] = s_xz + w;
+                p.s[3][i] = s_xy + u * p.dt;
+                p.s[4][i] = s_xz + w * p.dt;
             }
             // ---- sigma_yz ----
             if (in_yz) {
-                float a1 = deriv(c_vz, p.cd[1]), a2 = deriv(c_vy, p.cd[2]);
+                float a1 = deriv(c_vz, p, 1), a2 = deriv(c_vy, p, 2);
                 if (sy >= 0) {
                     a1 = cpml(a1, psi[4], np_, p.tab_h[1][y]);
                     p.psi[7][iy] = np_;
@@ -396,7 +406,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_shear3d(const 
                         }
                     u = fmaf(0.5f * Myz, sr, u);
                 }
-                p.s[5][i] = s_yz + u;
+                p.s[5][i] = s_yz + u * p.dt;
             }
         }
         if (t + 1 < kTX3S) {
@@ -494,7 +504,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
             float vxn = 0.f, vyn = 0.f, vzn = 0.f, np_;
             // vx: sxx[x+c]-sxx[x-c-1], sxy[y+c]-sxy[y-c-1], sxz[z+c]-sxz[z-c-1]
             if (in_vx) {
-                float a = wderiv<ORD>(wa, p.cd[0]), b = deriv(xb, p.cd[1]), e = deriv(xe, p.cd[2]);
+                float a = wderiv<ORD>(wa, p), b = deriv(xb, p, 1), e = deriv(xe, p, 2);
                 if (sx >= 0) {
                     a = cpml(a, psi[0], np_, p.tab_f[0][x]);
                     p.psi[9][ix] = np_;
@@ -507,11 +517,11 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
                     e = cpml(e, psi[2], np_, p.tab_f[2][z]);
                     p.psi[11][iz] = np_;
                 }
-                vxn = fmaf(a + b + e, dtx, v0[0]);
+                vxn = wgsl_velocity(v0[0], a + b + e, dtx, p.dt);
             }
             // vy: sxy[x+c+1]-sxy[x-c], syy[y+c+1]-syy[y-c], syz[z+c]-syz[z-c-1]
             if (in_vy) {
-                float a = wderiv<ORD>(wb, p.cd[0]), b = deriv(yb, p.cd[1]), e = deriv(ye, p.cd[2]);
+                float a = wderiv<ORD>(wb, p), b = deriv(yb, p, 1), e = deriv(ye, p, 2);
                 if (sx >= 0) {
                     a = cpml(a, psi[3], np_, p.tab_h[0][x]);
                     p.psi[12][ix] = np_;
@@ -524,11 +534,11 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
                     e = cpml(e, psi[5], np_, p.tab_f[2][z]);
                     p.psi[14][iz] = np_;
                 }
-                vyn = fmaf(a + b + e, dty, v0[1]);
+                vyn = wgsl_velocity(v0[1], a + b + e, dty, p.dt);
             }
             // vz: sxz[x+c+1]-sxz[x-c], syz[y+c]-syz[y-c-1], szz[z+c+1]-szz[z-c]
             if (in_vz) {
-                float a = wderiv<ORD>(wc, p.cd[0]), b = deriv(zb, p.cd[1]), e = deriv(ze, p.cd[2]);
+                float a = wderiv<ORD>(wc, p), b = deriv(zb, p, 1), e = deriv(ze, p, 2);
                 if (sx >= 0) {
                     a = cpml(a, psi[6], np_, p.tab_h[0][x]);
                     p.psi[15][ix] = np_;
@@ -541,13 +551,13 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
                     e = cpml(e, psi[8], np_, p.tab_h[2][z]);
                     p.psi[17][iz] = np_;
                 }
-                vzn = fmaf(a + b + e, dty, v0[2]);  // the vy-node density (wgsl3d:1748)
+                vzn = wgsl_velocity(v0[2], a + b + e, dty, p.dt);  // the vy-node density (wgsl3d:1748)
             }
             if constexpr (MODE == 0) {
                 for (int q = q0; q < q1; ++q) {
                     const Source s = p.src[q];
                     if (s.cell == i && k < p.src_rows)
-                        vzn = fmaf(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), s.scale, vzn);
+                        vzn += wgsl_source(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), s.scale, p.dt);
                 }
             }
             p.v[0][i] = vxn;

@@ -59,8 +59,10 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// CPML update of one derivative with its memory in shared memory, in the
-// arithmetic of the family's regular kernel
+// The arithmetic of the regular kernels (ts_kernels2d.cuh): FAM 0 is
+// kTaichi, FAM 1 is kWgsl (sums of weighted differences divided by the grid
+// step, updates times dt, velocities divided by rho).
+// CPML update of one derivative with its memory in shared memory
 template <int FAM>
 __device__ __forceinline__ float pcpml(float d, float &psi, const Cpml &t) {
     if (FAM == 0) {
@@ -70,13 +72,18 @@ __device__ __forceinline__ float pcpml(float d, float &psi, const Cpml &t) {
         return r;
     }
     psi = fmaf(t.b, psi, t.a * d);
-    return fmaf(d, t.ik, psi);
+    return qdiv(d, t.k, t.ik) + psi;
 }
 
-// one derivative term: family 0 in the reference's order, else fma with coef / d
+// one derivative term: family 0 in the reference's order, else fma with coef
 template <int FAM>
 __device__ __forceinline__ float pterm(float acc, const StepParams &p, int axis, int c, float hi, float lo) {
-    return FAM == 0 ? taichi_term(acc, p.coef[c], hi, lo, p.od[axis]) : fmaf(p.cd[axis][c], hi - lo, acc);
+    return FAM == 0 ? taichi_term(acc, p.coef[c], hi, lo, p.od[axis]) : fmaf(p.coef[c], hi - lo, acc);
+}
+// the derivative from its sum: family 1 divides by the grid step
+template <int FAM>
+__device__ __forceinline__ float pfin(float s, const StepParams &p, int axis) {
+    return FAM == 0 ? s : qdiv(s, p.dd[axis], p.od[axis]);
 }
 
 template <int FAM, int R>
@@ -219,6 +226,8 @@ __global__ void __launch_bounds__(kPMaxThreads, 1) k_persist2d(const __grid_cons
                         ddx = pterm<FAM>(ddx, p, 0, c, svx[(jv + c + 1) * W + y], svx[(jv - c) * W + y]);
                         ddy = pterm<FAM>(ddy, p, 1, c, svy[jv * W + y + c], svy[jv * W + y - c - 1]);
                     }
+                    ddx = pfin<FAM>(ddx, p, 0);
+                    ddy = pfin<FAM>(ddy, p, 1);
                     if (sx >= 0) ddx = pcpml<FAM>(ddx, spnx[(0 * NS + j) * W + y], p.tab_h[0][x]);
                     if (sy >= 0) ddy = pcpml<FAM>(ddy, spny[(0 * NS + j) * syw + sy], p.tab_f[1][y]);
                     const float L = cL[j], M = cM[j];
@@ -230,8 +239,8 @@ __global__ void __launch_bounds__(kPMaxThreads, 1) k_persist2d(const __grid_cons
                     } else {
                         const float L2M = fmaf(2.f, M, L);
                         const float ux = fmaf(L2M, ddx, L * ddy), uy = fmaf(L, ddx, L2M * ddy);
-                        sxx += ux;
-                        syy += uy;
+                        sxx += ux * p.dt;
+                        syy += uy * p.dt;
                     }
                     ssxx[j * W + y] = sxx;
                     ssyy[j * W + y] = syy;
@@ -243,6 +252,8 @@ __global__ void __launch_bounds__(kPMaxThreads, 1) k_persist2d(const __grid_cons
                         av = pterm<FAM>(av, p, 0, c, svy[(jv + c) * W + y], svy[(jv - c - 1) * W + y]);
                         bv = pterm<FAM>(bv, p, 1, c, svx[jv * W + y + c + 1], svx[jv * W + y - c]);
                     }
+                    av = pfin<FAM>(av, p, 0);
+                    bv = pfin<FAM>(bv, p, 1);
                     if (sx >= 0) av = pcpml<FAM>(av, spnx[(1 * NS + j) * W + y], p.tab_f[0][x]);
                     if (sy >= 0) bv = pcpml<FAM>(bv, spny[(1 * NS + j) * syw + sy], p.tab_h[1][y]);
                     if (FAM == 0) {
@@ -250,7 +261,7 @@ __global__ void __launch_bounds__(kPMaxThreads, 1) k_persist2d(const __grid_cons
                     } else {
                         const float e = av + bv;
                         const float u = cMs[j] * e;
-                        ssxy[j * W + y] = ssxy[j * W + y] + u;
+                        ssxy[j * W + y] = ssxy[j * W + y] + u * p.dt;
                     }
                 }
             }
@@ -283,13 +294,14 @@ __global__ void __launch_bounds__(kPMaxThreads, 1) k_persist2d(const __grid_cons
                         av = pterm<FAM>(av, p, 0, c, ssxx[(js + c) * W + y], ssxx[(js - c - 1) * W + y]);
                         bv = pterm<FAM>(bv, p, 1, c, ssxy[js * W + y + c], ssxy[js * W + y - c - 1]);
                     }
+                    av = pfin<FAM>(av, p, 0);
+                    bv = pfin<FAM>(bv, p, 1);
                     if (sx >= 0) av = pcpml<FAM>(av, spvx[(0 * R + j) * W + y], p.tab_f[0][x]);
                     if (sy >= 0) bv = pcpml<FAM>(bv, spvy[(0 * R + j) * syw + sy], p.tab_f[1][y]);
                     if (FAM == 0) {
                         vxn = taichi_velocity(svx[jv * W + y], __fadd_rn(av, bv), 0.f, cdx[j], p.dt);
                     } else {
-                        const float fax = av + bv;
-                        vxn = fmaf(fax, cdx[j], svx[jv * W + y]);
+                        vxn = wgsl_velocity(svx[jv * W + y], av + bv, cdx[j], p.dt);
                     }
                 }
                 if (in_vy) {
@@ -299,6 +311,8 @@ __global__ void __launch_bounds__(kPMaxThreads, 1) k_persist2d(const __grid_cons
                         av = pterm<FAM>(av, p, 0, c, ssxy[(js + c + 1) * W + y], ssxy[(js - c) * W + y]);
                         bv = pterm<FAM>(bv, p, 1, c, ssyy[js * W + y + c + 1], ssyy[js * W + y - c]);
                     }
+                    av = pfin<FAM>(av, p, 0);
+                    bv = pfin<FAM>(bv, p, 1);
                     if (sx >= 0) av = pcpml<FAM>(av, spvx[(1 * R + j) * W + y], p.tab_h[0][x]);
                     if (sy >= 0) bv = pcpml<FAM>(bv, spvy[(1 * R + j) * syw + sy], p.tab_h[1][y]);
                     if (FAM == 0) {
@@ -311,15 +325,14 @@ __global__ void __launch_bounds__(kPMaxThreads, 1) k_persist2d(const __grid_cons
                         }
                         vyn = taichi_velocity(svy[jv * W + y], __fadd_rn(av, bv), src, cdy[j], p.dt);
                     } else {
-                        const float fay = av + bv;
-                        vyn = fmaf(fay, cdy[j], svy[jv * W + y]);
+                        vyn = wgsl_velocity(svy[jv * W + y], av + bv, cdy[j], p.dt);
                     }
                 }
                 if (FAM != 0) {
                     for (int q = q0; q < q1; ++q) {
-                        const int4 s = a.srcs[q];   // (row in the slab, column, table column, dt / rho bits)
+                        const int4 s = a.srcs[q];   // (row in the slab, column, table column, rho bits)
                         if (s.x == j && s.y == y && k < p.src_rows)
-                            vyn = fmaf(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.z), __int_as_float(s.w), vyn);
+                            vyn += wgsl_source(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.z), __int_as_float(s.w), p.dt);
                     }
                 }
                 svx[jv * W + y] = vxn;

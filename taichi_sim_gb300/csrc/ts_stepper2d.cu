@@ -22,13 +22,13 @@ void launch_tx(const StepParams &p, int zen_mode, int j, cudaStream_t st, int pa
         return;
     }
     if (parts & 1) {
-        if (zen_mode == 0) launch_pdl(k_stress2d<ORD, 1, 0, 0, TX>, grid, block, st, p);
-        else if (zen_mode == 1 && three) launch_pdl(k_stress2d<ORD, 1, 1, 3, TX>, grid, block, st, p);
-        else if (zen_mode == 1) launch_pdl(k_stress2d<ORD, 1, 1, kMaxSls, TX>, grid, block, st, p);
-        else if (three) launch_pdl(k_stress2d<ORD, 1, 2, 3, TX, false, (ORD == 2 ? 4 : 0)>, grid, block, st, p);
-        else launch_pdl(k_stress2d<ORD, 1, 2, kMaxSls, TX>, grid, block, st, p);
+        if (zen_mode == 0) launch_pdl(k_stress2d<ORD, kWgsl, 0, 0, TX>, grid, block, st, p);
+        else if (zen_mode == 1 && three) launch_pdl(k_stress2d<ORD, kWgsl, 1, 3, TX>, grid, block, st, p);
+        else if (zen_mode == 1) launch_pdl(k_stress2d<ORD, kWgsl, 1, kMaxSls, TX>, grid, block, st, p);
+        else if (three) launch_pdl(k_stress2d<ORD, kWgsl, 2, 3, TX, false, (ORD == 2 ? 4 : 0)>, grid, block, st, p);
+        else launch_pdl(k_stress2d<ORD, kWgsl, 2, kMaxSls, TX>, grid, block, st, p);
     }
-    if (parts & 2) launch_pdl(k_velocity2d<ORD, 1, TX, false, (ORD == 2 ? 4 : 0)>, grid, block, st, p, j);
+    if (parts & 2) launch_pdl(k_velocity2d<ORD, kWgsl, TX, false, (ORD == 2 ? 4 : 0)>, grid, block, st, p, j);
 }
 
 template <int ORD>

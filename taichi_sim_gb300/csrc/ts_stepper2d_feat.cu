@@ -1,6 +1,8 @@
-// Instantiations of the 2D step kernels that record the adjoint's per-node
-// quantities (family TS_WGSL2D, two nodes per thread), in their own
-// translation unit so that they compile in parallel with the plain ones.
+// The 2D step kernels of the adjoint's forward pass (family TS_WGSL2D with
+// the coefficients folded with dt, kWgslFolded; two nodes per thread):
+// with and without the record of the per-node quantities the adjoint
+// multiplies by, in their own translation unit so that they compile in
+// parallel with the stepper's.
 #include <cuda_runtime.h>
 #include "ts_kernels2d.cuh"
 
@@ -12,12 +14,26 @@ void launch_feat_mb(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
     constexpr int TX = 2;
     const dim3 block(kBX2, kBY2), grid((p.ny + kBX2 - 1) / kBX2, (p.nx + kBY2 * TX - 1) / (kBY2 * TX));
     const bool three = p.zen.n == 3;
-    if (zen_mode == 0) launch_pdl(k_stress2d<ORD, 1, 0, 0, TX, true, MINB>, grid, block, st, p);
-    else if (zen_mode == 1 && three) launch_pdl(k_stress2d<ORD, 1, 1, 3, TX, true, MINB>, grid, block, st, p);
-    else if (zen_mode == 1) launch_pdl(k_stress2d<ORD, 1, 1, kMaxSls, TX, true, MINB_Q>, grid, block, st, p);
-    else if (three) launch_pdl(k_stress2d<ORD, 1, 2, 3, TX, true, MINB_Q>, grid, block, st, p);
-    else launch_pdl(k_stress2d<ORD, 1, 2, kMaxSls, TX, true, MINB_Q>, grid, block, st, p);
-    launch_pdl(k_velocity2d<ORD, 1, TX, true, MINB>, grid, block, st, p, j);
+    if (zen_mode == 0) launch_pdl(k_stress2d<ORD, kWgslFolded, 0, 0, TX, true, MINB>, grid, block, st, p);
+    else if (zen_mode == 1 && three) launch_pdl(k_stress2d<ORD, kWgslFolded, 1, 3, TX, true, MINB>, grid, block, st, p);
+    else if (zen_mode == 1) launch_pdl(k_stress2d<ORD, kWgslFolded, 1, kMaxSls, TX, true, MINB_Q>, grid, block, st, p);
+    else if (three) launch_pdl(k_stress2d<ORD, kWgslFolded, 2, 3, TX, true, MINB_Q>, grid, block, st, p);
+    else launch_pdl(k_stress2d<ORD, kWgslFolded, 2, kMaxSls, TX, true, MINB_Q>, grid, block, st, p);
+    launch_pdl(k_velocity2d<ORD, kWgslFolded, TX, true, MINB>, grid, block, st, p, j);
+}
+
+// the same step without the record (the forward's unrecorded segments)
+template <int ORD>
+void launch_folded(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
+    constexpr int TX = 2, MB = ORD == 2 ? 4 : 0;
+    const dim3 block(kBX2, kBY2), grid((p.ny + kBX2 - 1) / kBX2, (p.nx + kBY2 * TX - 1) / (kBY2 * TX));
+    const bool three = p.zen.n == 3;
+    if (zen_mode == 0) launch_pdl(k_stress2d<ORD, kWgslFolded, 0, 0, TX>, grid, block, st, p);
+    else if (zen_mode == 1 && three) launch_pdl(k_stress2d<ORD, kWgslFolded, 1, 3, TX>, grid, block, st, p);
+    else if (zen_mode == 1) launch_pdl(k_stress2d<ORD, kWgslFolded, 1, kMaxSls, TX>, grid, block, st, p);
+    else if (three) launch_pdl(k_stress2d<ORD, kWgslFolded, 2, 3, TX, false, MB>, grid, block, st, p);
+    else launch_pdl(k_stress2d<ORD, kWgslFolded, 2, kMaxSls, TX>, grid, block, st, p);
+    launch_pdl(k_velocity2d<ORD, kWgslFolded, TX, false, MB>, grid, block, st, p, j);
 }
 
 // Register budget: order 2 takes 4 resident blocks per SM (64 registers:
@@ -33,6 +49,14 @@ void launch_feat(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
 }
 
 }  // namespace
+
+void launch_step_2d_folded(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st) {
+    switch (ord) {   // the adjoint serves orders 2 and 4
+    case 2: launch_folded<2>(p, zen_mode, j, st); break;
+    case 4: launch_folded<4>(p, zen_mode, j, st); break;
+    default: break;
+    }
+}
 
 void launch_step_2d_feat(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st) {
     switch (ord) {
