@@ -146,6 +146,15 @@ def case_3d(w=30, d=26, h=34, steps=90, acc=2, visco=1, seed=0, q=None, matrix=F
     return cfg
 
 
+def gated_mask(sim, taichi, n_steps):
+    """Trace samples a receiver does not record: rows before its first
+    recorded step (WGSL semantics: row k from k = delay; Taichi: from
+    k = delay - 1)."""
+    n_rec = int(sim._n_rec)
+    first = np.asarray(sim._delay_recv, np.int64).reshape(-1)[:n_rec] - (1 if taichi else 0)
+    return np.arange(n_steps)[:, None] < first[None, :]
+
+
 def rel_l2(a, b):
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
