@@ -177,11 +177,11 @@ int ts_copy_field(ts_sim *sim, int32_t what, void *dst, size_t dst_pitch, void *
 int ts_launches_per_step(const ts_sim *sim, int32_t *launches);
 
 /* How ts_run advances this handle: TS_PATH_STEPPED, the step's kernels
- * launched once per time step (replayed from a CUDA graph), or
+ * launched once per time step (replayed from a CUDA graph; the default), or
  * TS_PATH_PERSISTENT, every step of the call in one cooperative launch that
- * keeps the wavefield on chip (2D elastic models of order 2 whose row slabs
- * fit shared memory; TS_2D_PERSISTENT=0 in the environment at ts_create
- * turns it off).  Both give the same bits. */
+ * keeps the wavefield on chip (opt-in with TS_2D_PERSISTENT=1 in the
+ * environment at ts_create, for 2D elastic models of order 2 whose row
+ * slabs fit shared memory).  Both give the same bits. */
 #define TS_PATH_STEPPED 0
 #define TS_PATH_PERSISTENT 1
 int ts_step_path(const ts_sim *sim, int32_t *path);

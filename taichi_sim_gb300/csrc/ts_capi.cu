@@ -395,6 +395,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     for (int c = 0; c < ts::kMaxOrd; ++c) p.coef[c] = c < ord ? d->coefs[c] : 0.f;
     for (int a = 0; a < 3; ++a) p.od[a] = steps[a] > 0.f ? 1.f / steps[a] : 0.f;
     for (int a = 0; a < 3; ++a) p.dd[a] = steps[a];
+    for (int a = 0; a < 3; ++a) p.odl[a] = steps[a] > 0.f ? (float)(1.0 / (double)steps[a] - (double)p.od[a]) : 0.f;
     p.dt = d->dt;
 
     // ---- CPML tables and strips ----
@@ -524,11 +525,27 @@ int ts_create(const ts_desc *d, ts_sim **out) {
             palette = true;
         }
     }
-    if ((rc = s->upload(&dev, dtr0))) return bail(rc);
-    p.dtr[0] = dev;
-    if ((rc = s->upload(&dev, dtr1))) return bail(rc);
-    p.dtr[1] = dev;
-    p.dtr[2] = dev;  // vz uses the vy-node density (wgsl3d:1748)
+    if (s->family == TS_TAICHI2D) {   // rho itself: the Taichi kernels divide
+        if ((rc = s->upload(&dev, dtr0))) return bail(rc);
+        p.dtr[0] = dev;
+        if ((rc = s->upload(&dev, dtr1))) return bail(rc);
+        p.dtr[1] = dev;
+    } else {   // dt / rho as (hi, lo) pairs, computed in double from the float dt and rho
+        for (int c = 0; c < 2; ++c) {
+            const std::vector<float> &rh = c == 0 ? dtr0 : dtr1;
+            std::vector<float2> w(rh.size(), make_float2(0.f, 0.f));
+            for (size_t i = 0; i < rh.size(); ++i)
+                if (rh[i] > 0.f) {
+                    const double q = (double)dt / (double)rh[i];
+                    const float hi = (float)q;
+                    w[i] = make_float2(hi, (float)(q - (double)hi));
+                }
+            float2 *dw = nullptr;
+            if ((rc = s->upload(&dw, w))) return bail(rc);
+            p.dtw[c] = dw;
+        }
+        p.dtw[2] = p.dtw[1];   // vz uses the vy-node density (wgsl3d:1748)
+    }
     if (!palette) {
         if ((rc = s->upload(&dev, lam))) return bail(rc);
         p.lam_dt = dev;
@@ -664,12 +681,15 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     p.first_bad = s->first_bad;
     p.step_base = s->step_base;
 
-    // ---- persistent path: 2D elastic order-2 models whose row slabs fit on chip ----
+    // ---- persistent path (opt-in, TS_2D_PERSISTENT=1): 2D elastic order-2
+    // models whose row slabs fit on chip.  Measured slower than the stepped
+    // path on GB300 (the per-step compute of a slab, half of it recomputed
+    // halo rows, runs at 16 warps per SM), so it is not the default. ----
     if (s->dims == 2) {
         const char *env = getenv("TS_2D_PERSISTENT");
         int rows = 0, blocks = 0, threads = 0;
         size_t smem = 0;
-        if (!(env && env[0] == '0') &&
+        if (env && env[0] == '1' &&
             ts::persist_2d_plan(s->family, ord, s->zen_mode, nx, ny, p.strip[1].width, prop.multiProcessorCount,
                                 &rows, &blocks, &threads, &smem)) {
             ts::PersistArgs &a = s->pa;

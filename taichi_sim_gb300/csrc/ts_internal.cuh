@@ -76,6 +76,7 @@ struct StepParams {
     // coef[c], 1 / d_axis (float), d_axis, dt
     float coef[kMaxOrd];
     float od[3];
+    float odl[3];          // 1 / d_axis - od as a float: od + odl is 1 / d to ~48 bits
     float dd[3];           // the grid steps themselves
     float dt;
 
@@ -96,6 +97,7 @@ struct StepParams {
     const float *lam_dt, *mu_dt;          // normal node
     const float *mus_dt[3];               // shear nodes xy, xz, yz (2D: xy)
     const float *dtr[3];                  // dt / rho at vx, vy, vz nodes (0: no update)
+    const float2 *dtw[3];                 // WGSL stepper: dt / rho as a pair (hi, lo), hi + lo exact to ~48 bits
     const float *g_p, *g_s;               // per-cell attenuation scale (or null)
     // 3D coefficient palette (or null): the stress kernels take node i's
     // coefficients from pal[pal_idx[i]] instead of the arrays above
@@ -208,11 +210,13 @@ __device__ __forceinline__ float qdiv(float x, float b, float r) {
     const float e = fmaf(-q, b, x);
     return fmaf(e, r, q);
 }
-// WGSL velocity update v + (f dt) / rho, none where rho <= 0
-// (shader_webgpu_viscoelastic.wgsl:1020-1024, 1049-1052)
-__device__ __forceinline__ float wgsl_velocity(float v, float f, float rho, float dt) {
-    return rho > 0.f ? v + qdiv(f * dt, rho, __frcp_rn(rho)) : v;
-}
+// WGSL velocity update v + (f dt) / rho (shader_webgpu_viscoelastic.wgsl:
+// 1020-1024, 1049-1052) with w = dt / rho given as a pair (hi, lo) whose sum
+// holds it to ~48 bits (0 where rho <= 0: no update): the only roundings are
+// those of the two fmas, none repeating at every node
+__device__ __forceinline__ float wgsl_velocity(float v, float f, float2 w) { return fmaf(f, w.x, fmaf(f, w.y, v)); }
+// s / d for a grid step d with 1 / d = od + odl (to ~48 bits): unbiased
+__device__ __forceinline__ float dscale(float s, float od, float odl) { return fmaf(s, od, s * odl); }
 // WGSL source force src dt / rho (wgsl:1059-1065)
 __device__ __forceinline__ float wgsl_source(float src, float rho, float dt) {
     return qdiv(src * dt, rho, __frcp_rn(rho));

@@ -60,7 +60,7 @@ __device__ __forceinline__ float dw(const StepParams &p, int a, int c) {
 // a derivative's sum of weighted differences, divided by the grid step (kWgsl)
 template <int FAM>
 __device__ __forceinline__ float dfin(float s, const StepParams &p, int a) {
-    return FAM == kWgsl ? qdiv(s, p.dd[a], p.od[a]) : s;
+    return FAM == kWgsl ? dscale(s, p.od[a], p.odl[a]) : s;
 }
 
 // Loads.  ldg: data no kernel writes (coefficients, tables), through the
@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
         constexpr int NR = TX + 2 * ORD - 1;
         float rxx[NR], rxy[NR];
         float bl[TX][ORD], bh[TX][ORD - 1 > 0 ? ORD - 1 : 1], by[TX][2 * ORD];
-        float vx0[TX], vy0[TX], dx0[TX], dy0[TX];
+        float vx0[TX], vy0[TX], dx0[TX], dy0[TX], dxl[TX], dyl[TX];
 #pragma unroll
         for (int r = 0; r < NR; ++r) {
             rxx[r] = ldf(sxx + (int64_t)(x0 - ORD + r) * P + y);
@@ -361,8 +361,16 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             for (int c = 0; c < 2 * ORD; ++c) by[t][c] = ldf(syy + i - ORD + 1 + c);   // syy[y-ORD+1 .. y+ORD]
             vx0[t] = p.v[0][i];
             vy0[t] = p.v[1][i];
-            dx0[t] = ldg(p.dtr[0] + i);
-            dy0[t] = ldg(p.dtr[1] + i);
+            if (FAM == kWgsl) {
+                const float2 wx = __ldg(p.dtw[0] + i), wy = __ldg(p.dtw[1] + i);
+                dx0[t] = wx.x;
+                dxl[t] = wx.y;
+                dy0[t] = wy.x;
+                dyl[t] = wy.y;
+            } else {
+                dx0[t] = ldg(p.dtr[0] + i);
+                dy0[t] = ldg(p.dtr[1] + i);
+            }
         }
 #pragma unroll
         for (int t = 0; t < TX; ++t) {
@@ -383,7 +391,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             a = dfin<FAM>(a, p, 0);
             b = dfin<FAM>(b, p, 1);
             const float fax = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
-            const float vxn = FAM == kTaichi ? taichi_velocity(vx0[t], fax, 0.f, dx0[t], p.dt) : FAM == kWgsl ? wgsl_velocity(vx0[t], fax, dx0[t], p.dt)
+            const float vxn = FAM == kTaichi ? taichi_velocity(vx0[t], fax, 0.f, dx0[t], p.dt) : FAM == kWgsl ? wgsl_velocity(vx0[t], fax, make_float2(dx0[t], dxl[t]))
                                                    : fmaf(fax, dx0[t], vx0[t]);
             a = 0.f;
             b = 0.f;
@@ -400,7 +408,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             a = dfin<FAM>(a, p, 0);
             b = dfin<FAM>(b, p, 1);
             const float fay = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
-            const float vyn = FAM == kTaichi ? taichi_velocity(vy0[t], fay, 0.f, dy0[t], p.dt) : FAM == kWgsl ? wgsl_velocity(vy0[t], fay, dy0[t], p.dt)
+            const float vyn = FAM == kTaichi ? taichi_velocity(vy0[t], fay, 0.f, dy0[t], p.dt) : FAM == kWgsl ? wgsl_velocity(vy0[t], fay, make_float2(dy0[t], dyl[t]))
                                                    : fmaf(fay, dy0[t], vy0[t]);
             p.v[0][i] = vxn;
             p.v[1][i] = vyn;
@@ -434,14 +442,20 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             const int64_t ix = (int64_t)sx * P + y, iy = (int64_t)x * p.strip[1].width + syl;
             // ---- loads ----
             float bx_lo[ORD], bx_hi[ORD - 1 > 0 ? ORD - 1 : 1], by[2 * ORD];
-            float vx0 = 0.f, vy0 = 0.f, dx0 = 0.f, dy0 = 0.f, pxa = 0.f, pxb = 0.f, pya = 0.f, pyb = 0.f;
+            float vx0 = 0.f, vy0 = 0.f, dx0 = 0.f, dy0 = 0.f, dxl = 0.f, dyl = 0.f, pxa = 0.f, pxb = 0.f, pya = 0.f, pyb = 0.f;
             if (in_vx) {
 #pragma unroll
                 for (int c = 0; c < ORD; ++c) bx_lo[c] = ldf(sxy + i - c - 1);   // sxy[y-c-1]
 #pragma unroll
                 for (int c = 1; c < ORD; ++c) bx_hi[c - 1] = ldf(sxy + i + c);   // sxy[y+c], c >= 1
                 vx0 = p.v[0][i];
-                dx0 = ldg(p.dtr[0] + i);
+                if (FAM == kWgsl) {
+                    const float2 w = __ldg(p.dtw[0] + i);
+                    dx0 = w.x;
+                    dxl = w.y;
+                } else {
+                    dx0 = ldg(p.dtr[0] + i);
+                }
                 if (sx >= 0) pxa = p.psi[4][ix];
                 if (syl >= 0) pxb = p.psi[6][iy];
             }
@@ -449,7 +463,13 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
 #pragma unroll
                 for (int c = 0; c < 2 * ORD; ++c) by[c] = ldf(syy + i - ORD + 1 + c);   // syy[y-ORD+1 .. y+ORD]
                 vy0 = p.v[1][i];
-                dy0 = ldg(p.dtr[1] + i);
+                if (FAM == kWgsl) {
+                    const float2 w = __ldg(p.dtw[1] + i);
+                    dy0 = w.x;
+                    dyl = w.y;
+                } else {
+                    dy0 = ldg(p.dtr[1] + i);
+                }
                 if (sx >= 0) pya = p.psi[5][ix];
                 if (syl >= 0) pyb = p.psi[7][iy];
             }
@@ -480,7 +500,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                 }
                 fax = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
                 vxn = FAM == kTaichi ? taichi_velocity(vx0, fax, 0.f, dx0, p.dt)
-                      : FAM == kWgsl   ? wgsl_velocity(vx0, fax, dx0, p.dt)
+                      : FAM == kWgsl   ? wgsl_velocity(vx0, fax, make_float2(dx0, dxl))
                                        : fmaf(fax, dx0, vx0);
             }
             if (in_vy) {
@@ -518,7 +538,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                     }
                     vyn = taichi_velocity(vy0, fay, src, dy0, p.dt);
                 } else {
-                    vyn = FAM == kWgsl ? wgsl_velocity(vy0, fay, dy0, p.dt) : fmaf(fay, dy0, vy0);
+                    vyn = FAM == kWgsl ? wgsl_velocity(vy0, fay, make_float2(dy0, dyl)) : fmaf(fay, dy0, vy0);
                 }
             }
             if constexpr (!FAST && FAM != kTaichi) {

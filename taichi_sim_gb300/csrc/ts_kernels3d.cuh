@@ -21,10 +21,10 @@
 // outside the vz region, the source drives vz).
 //
 // Arithmetic: as the shaders, every derivative divided by its grid step,
-// every update multiplied by dt and every velocity update divided by rho,
-// each division done once per derivative or update and rounded as a division
-// (qdiv), so that no folded constant (coef / d, lambda dt, dt / rho) biases
-// every node and step alike; sums contract to fma.
+// every update multiplied by dt and every velocity update divided by rho;
+// the constants 1 / d and dt / rho enter as pairs (hi, lo) exact to ~48 bits,
+// so that no rounded constant (coef / d, lambda dt, dt / rho) biases every
+// node and step alike; sums contract to fma.
 //
 // Coefficients: with PAL the stress kernels take the per-node coefficients
 // from a palette (one 16-bit index per node into a table of the model's
@@ -79,7 +79,7 @@ __device__ __forceinline__ float deriv(const Pairs<ORD> &q, const StepParams &p,
     float a = 0.f;
 #pragma unroll
     for (int c = 0; c < ORD; ++c) a = fmaf(p.coef[c], q.hi[c] - q.lo[c], a);
-    return qdiv(a, p.dd[axis], p.od[axis]);
+    return dscale(a, p.od[axis], p.odl[axis]);
 }
 
 // Resident blocks per SM the kernels are compiled for (register budgets 64
@@ -133,7 +133,7 @@ __device__ __forceinline__ float wderiv(const float (&w)[2 * ORD], const StepPar
     float a = 0.f;
 #pragma unroll
     for (int c = 0; c < ORD; ++c) a = fmaf(p.coef[c], w[ORD + c] - w[ORD - 1 - c], a);
-    return qdiv(a, p.dd[0], p.od[0]);
+    return dscale(a, p.od[0], p.odl[0]);
 }
 
 // Normal stresses (sxx, syy, szz, their Zener memory variables and CPML
@@ -472,13 +472,14 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
             const I iz = ((I)x * p.ny + y) * p.strip[2].width + szl;
             // ---- loads ----
             Pairs<ORD> xb, xe, yb, ye, zb, ze;
-            float v0[3] = {0.f, 0.f, 0.f}, dtx = 0.f, dty = 0.f;
+            float v0[3] = {0.f, 0.f, 0.f};
+            float2 dtx = make_float2(0.f, 0.f), dty = make_float2(0.f, 0.f);
             float psi[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             if (in_vx) {
                 xb = load_pairs<ORD, false>(sxy, i, Y);
                 xe = load_pairs<ORD, false>(sxz, i, (I)1);
                 v0[0] = p.v[0][i];
-                dtx = __ldg(p.dtr[0] + i);
+                dtx = __ldg(p.dtw[0] + i);
                 if (sx >= 0) psi[0] = p.psi[9][ix];
                 if (syl >= 0) psi[1] = p.psi[10][iy];
                 if (szl >= 0) psi[2] = p.psi[11][iz];
@@ -495,7 +496,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
                 zb = load_pairs<ORD, false>(syz, i, Y);
                 ze = load_pairs<ORD, true>(szz, i, (I)1);
                 v0[2] = p.v[2][i];
-                dty = __ldg(p.dtr[1] + i);
+                dty = __ldg(p.dtw[1] + i);
                 if (sx >= 0) psi[6] = p.psi[15][ix];
                 if (syl >= 0) psi[7] = p.psi[16][iy];
                 if (szl >= 0) psi[8] = p.psi[17][iz];
@@ -517,7 +518,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
                     e = cpml(e, psi[2], np_, p.tab_f[2][z]);
                     p.psi[11][iz] = np_;
                 }
-                vxn = wgsl_velocity(v0[0], a + b + e, dtx, p.dt);
+                vxn = wgsl_velocity(v0[0], a + b + e, dtx);
             }
             // vy: sxy[x+c+1]-sxy[x-c], syy[y+c+1]-syy[y-c], syz[z+c]-syz[z-c-1]
             if (in_vy) {
@@ -534,7 +535,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
                     e = cpml(e, psi[5], np_, p.tab_f[2][z]);
                     p.psi[14][iz] = np_;
                 }
-                vyn = wgsl_velocity(v0[1], a + b + e, dty, p.dt);
+                vyn = wgsl_velocity(v0[1], a + b + e, dty);
             }
             // vz: sxz[x+c+1]-sxz[x-c], syz[y+c]-syz[y-c-1], szz[z+c+1]-szz[z-c]
             if (in_vz) {
@@ -551,7 +552,7 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
                     e = cpml(e, psi[8], np_, p.tab_h[2][z]);
                     p.psi[17][iz] = np_;
                 }
-                vzn = wgsl_velocity(v0[2], a + b + e, dty, p.dt);  // the vy-node density (wgsl3d:1748)
+                vzn = wgsl_velocity(v0[2], a + b + e, dty);  // the vy-node density (wgsl3d:1748)
             }
             if constexpr (MODE == 0) {
                 for (int q = q0; q < q1; ++q) {

@@ -80,7 +80,7 @@ def _check_stepper(sim, family, names, n_steps, exact=False):
 
 
 def test_full_elastic2d_512_2000_steps():
-    """Taichi semantics: the persistent path, bit for bit the float oracle."""
+    """Taichi semantics, bit for bit the float oracle."""
     sim = Simulator(workloads.elastic2d_512())
     assert sim.grid_shape() == (512, 512)
     _check_stepper(sim, engine.TAICHI2D, F2, 2000, exact=True)

@@ -111,9 +111,8 @@ TAICHI_CASES = sorted(n for n, (_, f) in CASES_2D.items() if f == engine.TAICHI2
 def test_taichi_family_is_bit_exact(name, persistent, monkeypatch):
     """The Taichi family keeps the reference's operation order with every
     operation rounded on its own, so every field and trace equals the
-    strict-IEEE float oracle bit for bit, on both 2D paths (order 2 models
-    take the persistent path unless it is switched off; other orders always
-    take the regular one)."""
+    strict-IEEE float oracle bit for bit, on both 2D paths (the persistent
+    one serves order 2 only; other orders take the regular one)."""
     monkeypatch.setenv("TS_2D_PERSISTENT", persistent)
     build, family = CASES_2D[name]
     sim = Simulator(build())

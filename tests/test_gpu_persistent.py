@@ -1,10 +1,11 @@
 """The persistent 2D elastic path (one cooperative launch per ts_run, the
-wavefield held on chip) against the regular two-kernel step.
+wavefield held on chip; opt-in with TS_2D_PERSISTENT=1) against the regular
+two-kernel step.
 
 Both run the same arithmetic, expression for expression, so fields and
 traces must agree bit for bit; the regular path is itself checked against
 the oracle (test_gpu_parity.py, test_gpu_full_size.py).  A handle created
-with TS_2D_PERSISTENT=0 takes the regular path.  The bounded wait between
+without TS_2D_PERSISTENT=1 takes the regular path.  The bounded wait between
 thread blocks is tested by a block that never releases its step counter (a
 test hook): its neighbours give up after the wait bound, the handle reports
 TS_E_TIMEOUT from ts_status, and the device stays usable.
