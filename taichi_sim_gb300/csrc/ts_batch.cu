@@ -6,8 +6,8 @@
 // covers the W shots of one grid node (one or two per lane), so every load
 // and store is one contiguous 128- or 256-byte row, neighbouring nodes along
 // y are W floats apart (immediate offsets), the per-node coefficients
-// (lambda*dt, mu*dt, dt/rho, Q scale) are one broadcast load shared by all
-// shots, and the region and CPML-strip tests are uniform across the warp.
+// (lambda, mu, dt/rho, Q scale) are one broadcast load shared by all shots,
+// and the region and CPML-strip tests are uniform across the warp.
 // Blocks are 32 lanes x CY nodes along y; each thread updates TX consecutive
 // nodes along x, keeping the x-stencil rows in a register window (one new
 // row per node), for SPT shots.  The flat block index runs over (phantom,
@@ -24,7 +24,10 @@
 // and :1118-1134) per shot, except for the source columns: shot s injects
 // column idx of its own source table (the column the reference's source map
 // names), so one-element shots of a full-matrix capture fire the element
-// they name.
+// they name.  The arithmetic is the single-shot stepper's (ts_kernels2d.cuh,
+// kWgsl): derivative sums times 1 / d as a (hi, lo) pair, updates times dt,
+// velocity updates times dt / rho as a pair, so that no rounded constant
+// biases every node and step alike.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -46,7 +49,7 @@ constexpr int kMaxPhantoms = 8;
 struct BSrc {
     int cell;     // x * ny + y
     int col;      // source column
-    float scale;  // dt / rho at the vy node
+    float scale;  // rho at the vy node (the source force is divided by it)
 };
 
 // Flat block range of one phantom in one kernel's launch: blocks of 32 lanes
@@ -60,11 +63,12 @@ struct BPh {
     int G;      // nx * ny * S (checked < 2^31 with the memory variables)
     int sblocks;
     Decomp dc[2];  // block decomposition of the stress (0) and velocity (1) launches
-    float cd[2][kMaxOrd];
+    float od[2], odl[2];   // 1 / dx, 1 / dy as (hi, lo): a derivative is its sum times them
     float *v[2], *s[3], *r[3], *psi[8];
     const Cpml *tab_f[2], *tab_h[2];
     Strip strip[2];
-    const float *lam, *mu, *mus, *dtr0, *dtr1, *gp, *gs;
+    const float *lam, *mu, *mus, *gp, *gs;   // lambda, mu, mu at the shear node (not folded with dt)
+    const float2 *dtw0, *dtw1;                // dt / rho at the vx, vy nodes as (hi, lo) pairs
     const BSrc *src;
     const int *src_start;  // [xchunks * yblocks + 1] of the velocity launch
     const float *shot_tab;  // [n_shots][rows][ncol]
@@ -82,6 +86,8 @@ struct BParams {
     BPh ph[kMaxPhantoms];
     int block_end[2][kMaxPhantoms];  // exclusive flat block end per kernel and phantom
     Zener zen;
+    float coef[kMaxOrd];   // staggered FD coefficients
+    float dt;
     int rows;
     float v2_threshold;
     float *block_max;
@@ -90,9 +96,10 @@ struct BParams {
     int rec_work;
 };
 
+// b psi + a d, then d / k + psi (the shader's division, rounded as one)
 __device__ __forceinline__ float cpml(float d, float psi_old, float &psi_new, const Cpml &t) {
     psi_new = fmaf(t.b, psi_old, t.a * d);
-    return fmaf(d, t.ik, psi_new);
+    return qdiv(d, t.k, t.ik) + psi_new;
 }
 
 struct Loc {
@@ -215,8 +222,8 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bstress(co
     float cdx[ORD], cdy[ORD];
 #pragma unroll
     for (int c = 0; c < ORD; ++c) {
-        cdx[c] = h.cd[0][c];
-        cdy[c] = h.cd[1][c];
+        cdx[c] = p.coef[c];   // the sums are scaled by 1 / d after (dscale)
+        cdy[c] = p.coef[c];
     }
     const float *__restrict__ vx = h.v[0];   // read with ldf only
     const float *__restrict__ vy = h.v[1];
@@ -307,6 +314,8 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bstress(co
                             ddx = fmaf(cdx[c], wvx[c + ORD][q] - wvx[ORD - 1 - c][q], ddx);
                             ddy = fmaf(cdy[c], ny_hi[c][q] - ny_lo[c][q], ddy);
                         }
+                        ddx = dscale(ddx, h.od[0], h.odl[0]);
+                        ddy = dscale(ddy, h.od[1], h.odl[1]);
                         if (sx >= 0) ddx = cpml(ddx, pn0[q], pn0n[q], h.tab_h[0][x]);
                         if (syl >= 0) ddy = cpml(ddy, pn1[q], pn1n[q], h.tab_f[1][y]);
                         const float L2M = fmaf(2.f, M, L);
@@ -327,8 +336,8 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bstress(co
                             ux[q] = fmaf(hl, srxx, fmaf(M, sryy, ux[q]));
                             uy[q] = fmaf(hl, srxx, fmaf(-M, sryy, uy[q]));
                         }
-                        ux[q] += sxx[q];
-                        uy[q] += syy[q];
+                        ux[q] = sxx[q] + ux[q] * p.dt;   // (...) dt, wgsl:915-916
+                        uy[q] = syy[q] + uy[q] * p.dt;
                     }
                     if (sx >= 0) sto<SPT>(h.psi[0] + ix, pn0n);
                     if (syl >= 0) sto<SPT>(h.psi[2] + iy, pn1n);
@@ -354,6 +363,8 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bstress(co
                             a = fmaf(cdx[c], wvy[c + ORD][q] - wvy[ORD - 1 - c][q], a);
                             b = fmaf(cdy[c], sx_hi[c][q] - sx_lo[c][q], b);
                         }
+                        a = dscale(a, h.od[0], h.odl[0]);
+                        b = dscale(b, h.od[1], h.odl[1]);
                         if (sx >= 0) a = cpml(a, ps0[q], ps0n[q], h.tab_f[0][x]);
                         if (syl >= 0) b = cpml(b, ps1[q], ps1n[q], h.tab_h[1][y]);
                         const float e = a + b;
@@ -368,7 +379,7 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bstress(co
                                 }
                             u[q] = fmaf(0.5f * Ms, sr, u[q]);
                         }
-                        u[q] += sxy[q];
+                        u[q] = sxy[q] + u[q] * p.dt;
                     }
                     if (sx >= 0) sto<SPT>(h.psi[1] + ix, ps0n);
                     if (syl >= 0) sto<SPT>(h.psi[3] + iy, ps1n);
@@ -407,14 +418,14 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocksV<CY>::v)) k_bvelocity(cons
     float cdx[ORD], cdy[ORD];
 #pragma unroll
     for (int c = 0; c < ORD; ++c) {
-        cdx[c] = h.cd[0][c];
-        cdy[c] = h.cd[1][c];
+        cdx[c] = p.coef[c];   // the sums are scaled by 1 / d after (dscale)
+        cdy[c] = p.coef[c];
     }
     const float *__restrict__ sxx = h.s[0];  // read with ldf only
     const float *__restrict__ syy = h.s[1];
     const float *__restrict__ sxy = h.s[2];
-    const float *__restrict__ dtr0 = h.dtr0;
-    const float *__restrict__ dtr1 = h.dtr1;
+    const float2 *__restrict__ dtw0 = h.dtw0;
+    const float2 *__restrict__ dtw1 = h.dtw1;
     float *__restrict__ v0 = h.v[0];
     float *__restrict__ v1 = h.v[1];
     pdl_wait();
@@ -441,7 +452,8 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocksV<CY>::v)) k_bvelocity(cons
         constexpr int NR = TX + 2 * ORD - 1;
         float rxx[NR][SPT], rxy[NR][SPT];
         float bxh[TX][ORD][SPT], bxl[TX][ORD][SPT], byh[TX][ORD][SPT], byl[TX][ORD][SPT];
-        float vx0[TX][SPT], vy0[TX][SPT], dx0[TX], dy0[TX];
+        float vx0[TX][SPT], vy0[TX][SPT];
+        float2 dx0[TX], dy0[TX];
 #pragma unroll
         for (int r = 0; r < NR; ++r) {
             ldf<SPT>(rxx[r], sxx + (at.x0 - ORD + r) * X + col);
@@ -459,8 +471,8 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocksV<CY>::v)) k_bvelocity(cons
             }
             ldo<SPT>(vx0[t], v0 + i);
             ldo<SPT>(vy0[t], v1 + i);
-            dx0[t] = __ldg(dtr0 + cell);
-            dy0[t] = __ldg(dtr1 + cell);
+            dx0[t] = __ldg(dtw0 + cell);
+            dy0[t] = __ldg(dtw1 + cell);
         }
 #pragma unroll
         for (int t = 0; t < TX; ++t) {
@@ -477,8 +489,12 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocksV<CY>::v)) k_bvelocity(cons
                     ay = fmaf(cdx[c], rxy[t + ORD + c][q] - rxy[t + ORD - 1 - c][q], ay);
                     by = fmaf(cdy[c], byh[t][c][q] - byl[t][c][q], by);
                 }
-                vxn[q] = fmaf(ax + bx, dx0[t], vx0[t][q]);
-                vyn[q] = fmaf(ay + by, dy0[t], vy0[t][q]);
+                ax = dscale(ax, h.od[0], h.odl[0]);
+                bx = dscale(bx, h.od[1], h.odl[1]);
+                ay = dscale(ay, h.od[0], h.odl[0]);
+                by = dscale(by, h.od[1], h.odl[1]);
+                vxn[q] = wgsl_velocity(vx0[t][q], ax + bx, dx0[t]);
+                vyn[q] = wgsl_velocity(vy0[t][q], ay + by, dy0[t]);
                 const float v2 = fmaf(vxn[q], vxn[q], vyn[q] * vyn[q]);
                 bad |= !(v2 <= p.v2_threshold);
                 vmax = max(vmax, __float_as_uint(v2));
@@ -510,7 +526,7 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocksV<CY>::v)) k_bvelocity(cons
             // ---- loads ----
             float bx_hi[ORD][SPT], bx_lo[ORD][SPT], by_hi[ORD][SPT], by_lo[ORD][SPT];
             float vx0[SPT], vy0[SPT], pxa[SPT], pxb[SPT], pya[SPT], pyb[SPT];
-            float dx0 = 0.f, dy0 = 0.f;
+            float2 dx0 = make_float2(0.f, 0.f), dy0 = make_float2(0.f, 0.f);
             if (in_vx) {
 #pragma unroll
                 for (int c = 0; c < ORD; ++c) {
@@ -518,7 +534,7 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocksV<CY>::v)) k_bvelocity(cons
                     ldf<SPT>(bx_lo[c], sxy + i - (c + 1) * Y);   // sxy[y-c-1]
                 }
                 ldo<SPT>(vx0, v0 + i);
-                dx0 = __ldg(dtr0 + cell);
+                dx0 = __ldg(dtw0 + cell);
                 if (sx >= 0) ldo<SPT>(pxa, h.psi[4] + ix);
                 if (syl >= 0) ldo<SPT>(pxb, h.psi[6] + iy);
             }
@@ -529,7 +545,7 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocksV<CY>::v)) k_bvelocity(cons
                     ldf<SPT>(by_lo[c], syy + i - c * Y);         // syy[y-c]
                 }
                 ldo<SPT>(vy0, v1 + i);
-                dy0 = __ldg(dtr1 + cell);
+                dy0 = __ldg(dtw1 + cell);
                 if (sx >= 0) ldo<SPT>(pya, h.psi[5] + ix);
                 if (syl >= 0) ldo<SPT>(pyb, h.psi[7] + iy);
             }
@@ -546,9 +562,11 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocksV<CY>::v)) k_bvelocity(cons
                         a = fmaf(cdx[c], wxx[c + ORD][q] - wxx[ORD - 1 - c][q], a);
                         b = fmaf(cdy[c], bx_hi[c][q] - bx_lo[c][q], b);
                     }
+                    a = dscale(a, h.od[0], h.odl[0]);
+                    b = dscale(b, h.od[1], h.odl[1]);
                     if (sx >= 0) a = cpml(a, pxa[q], pxan[q], h.tab_f[0][x]);
                     if (syl >= 0) b = cpml(b, pxb[q], pxbn[q], h.tab_f[1][y]);
-                    vxn[q] = fmaf(a + b, dx0, vx0[q]);
+                    vxn[q] = wgsl_velocity(vx0[q], a + b, dx0);
                 }
                 if (in_vy) {
                     float a = 0.f, b = 0.f;
@@ -557,17 +575,19 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocksV<CY>::v)) k_bvelocity(cons
                         a = fmaf(cdx[c], wxy[c + ORD][q] - wxy[ORD - 1 - c][q], a);
                         b = fmaf(cdy[c], by_hi[c][q] - by_lo[c][q], b);
                     }
+                    a = dscale(a, h.od[0], h.odl[0]);
+                    b = dscale(b, h.od[1], h.odl[1]);
                     if (sx >= 0) a = cpml(a, pya[q], pyan[q], h.tab_h[0][x]);
                     if (syl >= 0) b = cpml(b, pyb[q], pybn[q], h.tab_h[1][y]);
-                    vyn[q] = fmaf(a + b, dy0, vy0[q]);
+                    vyn[q] = wgsl_velocity(vy0[q], a + b, dy0);
                 }
                 const int shot = at.s0 + q;
                 if (!FAST && q0 < q1 && shot < h.n_shots)
                     for (int qq = q0; qq < q1; ++qq) {
                         const BSrc s = h.src[qq];
                         if (s.cell == cell)
-                            vyn[q] = fmaf(__ldg(h.shot_tab + ((int64_t)shot * p.rows + k) * h.ncol + s.col), s.scale,
-                                          vyn[q]);
+                            vyn[q] += wgsl_source(__ldg(h.shot_tab + ((int64_t)shot * p.rows + k) * h.ncol + s.col),
+                                                  s.scale, p.dt);
                     }
                 const float v2 = fmaf(vxn[q], vxn[q], vyn[q] * vyn[q]);
                 bad |= !(v2 <= p.v2_threshold);
@@ -821,8 +841,10 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
             block0[k] += dc.xchunks * dc.yblocks * h.sblocks;
         }
         const float steps[2] = {d->dx, d->dy};
-        for (int a = 0; a < 2; ++a)
-            for (int c = 0; c < kMaxOrd; ++c) h.cd[a][c] = c < d->ord ? d->coefs[c] / steps[a] : 0.f;
+        for (int a = 0; a < 2; ++a) {
+            h.od[a] = 1.f / steps[a];
+            h.odl[a] = (float)(1.0 / (double)steps[a] - (double)h.od[a]);
+        }
         Axis ax[2] = {make_axis(h.nx, d->ord, d->a_x, d->b_x, d->k_x, d->a_xh, d->b_xh, d->k_xh),
                       make_axis(h.ny, d->ord, d->a_y, d->b_y, d->k_y, d->a_yh, d->b_yh, d->k_yh)};
         for (int a = 0; a < 2; ++a) {
@@ -850,11 +872,11 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
             for (int y = 0; y < h.ny; ++y) {
                 const Coef2D c = coef_2d(d, x, y);
                 const int64_t i = (int64_t)x * h.ny + y;
-                lam[i] = c.lam;
-                mu[i] = c.mu;
-                mus[i] = c.mus;
-                dtr0[i] = c.dtr_vx;
-                dtr1[i] = c.dtr_vy;
+                lam[i] = c.lam_raw;
+                mu[i] = c.mu_raw;
+                mus[i] = c.mus_raw;
+                dtr0[i] = c.rho_vx;
+                dtr1[i] = c.rho_vy;
                 rho_vy[i] = c.rho_vy;
             }
         float *dev = nullptr;
@@ -864,10 +886,19 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
         h.mu = dev;
         if ((rc = b->upload(&dev, mus))) return bail(rc);
         h.mus = dev;
-        if ((rc = b->upload(&dev, dtr0))) return bail(rc);
-        h.dtr0 = dev;
-        if ((rc = b->upload(&dev, dtr1))) return bail(rc);
-        h.dtr1 = dev;
+        for (int c = 0; c < 2; ++c) {   // dt / rho as (hi, lo), computed in double
+            const std::vector<float> &rh = c == 0 ? dtr0 : dtr1;
+            std::vector<float2> w(rh.size(), make_float2(0.f, 0.f));
+            for (size_t i = 0; i < rh.size(); ++i)
+                if (rh[i] > 0.f) {
+                    const double q = (double)d->dt / (double)rh[i];
+                    const float hi = (float)q;
+                    w[i] = make_float2(hi, (float)(q - (double)hi));
+                }
+            float2 *dw = nullptr;
+            if ((rc = b->upload(&dw, w))) return bail(rc);
+            (c == 0 ? h.dtw0 : h.dtw1) = dw;
+        }
         if (b->zen_mode == 2) {
             std::vector<float> gp(d->g_p, d->g_p + cells), gs(d->g_s, d->g_s + cells);
             if ((rc = b->upload(&dev, gp))) return bail(rc);
@@ -883,7 +914,7 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
                 const int idx = d->pos_sources[(int64_t)x * h.ny + y];
                 const float r4 = rho_vy[(int64_t)x * h.ny + y];
                 if (idx < 0 || idx >= d->src_cols || !(r4 > 0.f)) continue;
-                bins[(size_t)(x / b->tx[1]) * h.dc[1].yblocks + y / b->cy[1]].push_back(BSrc{x * h.ny + y, idx, d->dt / r4});
+                bins[(size_t)(x / b->tx[1]) * h.dc[1].yblocks + y / b->cy[1]].push_back(BSrc{x * h.ny + y, idx, r4});
                 maxcol = std::max(maxcol, idx + 1);
             }
         std::vector<BSrc> list;
@@ -939,6 +970,8 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
     if ((int64_t)rec0 > (int64_t)block0[1] * 32 * b->cy[1])
         return bail(bfail(TS_E_ARG, "more (shot, receiver) pairs than threads of a step launch"));
     p.zen = zener_constants(d0);
+    for (int c = 0; c < kMaxOrd; ++c) p.coef[c] = c < d0->ord ? d0->coefs[c] : 0.f;
+    p.dt = d0->dt;
     p.rows = b->rows;
     p.v2_threshold = FLT_MAX;
     p.rec_work = rec0;

@@ -509,11 +509,17 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     float *dev = nullptr;
     bool palette = false;
     const char *pal_env = getenv("TS_3D_COEF_PALETTE");   // "0": arrays (tests cover both paths)
-    if (s->dims == 3 && s->grid_elems * (int64_t)std::max(1, p.zen.n) < ((int64_t)1 << 31) &&
-        !(pal_env && pal_env[0] == '0')) {
+    const char *pal2_env = getenv("TS_2D_COEF_PALETTE");  // "0": arrays
+    const bool pal3 = s->dims == 3 && s->grid_elems * (int64_t)std::max(1, p.zen.n) < ((int64_t)1 << 31) &&
+                      !(pal_env && pal_env[0] == '0');
+    const char *pers_env = getenv("TS_2D_PERSISTENT");     // the persistent kernel reads the arrays
+    const bool pal2 = s->dims == 2 && s->family == TS_WGSL2D && ord == 2 && !(pal2_env && pal2_env[0] == '0') &&
+                      !(pers_env && pers_env[0] == '1');
+    if (pal3 || pal2) {
         const std::vector<float> ones(gp.empty() ? s->grid_elems : 0, 1.f);
+        const std::vector<float> zeros(pal2 ? s->grid_elems : 0, 0.f);
         const std::vector<float> *cols[7] = {&lam, &mu, gp.empty() ? &ones : &gp, gs.empty() ? &ones : &gs,
-                                             &mus[0], &mus[1], &mus[2]};
+                                             &mus[0], pal2 ? &zeros : &mus[1], pal2 ? &zeros : &mus[2]};
         std::vector<uint16_t> idx;
         std::vector<ts::Pal3> table;
         if (build_palette_3d(cols, idx, table)) {
@@ -525,7 +531,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
             palette = true;
         }
     }
-    if (s->family == TS_TAICHI2D) {   // rho itself: the Taichi kernels divide
+    if (s->dims == 2) {   // rho itself: the 2D kernels divide by it
         if ((rc = s->upload(&dev, dtr0))) return bail(rc);
         p.dtr[0] = dev;
         if ((rc = s->upload(&dev, dtr1))) return bail(rc);

@@ -119,7 +119,11 @@ __device__ __forceinline__ bool interior_warp(const Params &p, int y, int x0, in
     return __all_sync(0xffffffffu, lane);
 }
 
-template <int ORD, int FAM, int ZM, int NS, int TX, bool FEAT = false, int MINB = 0>
+// PAL: the node's coefficients (lambda, mu, its Q scales; mu at the shear
+// node) come from p.pal[p.pal_idx[node]] (one 16-bit index per node into the
+// model's distinct coefficient tuples, loaded first; its table entry after
+// every other load) instead of five arrays.
+template <int ORD, int FAM, int ZM, int NS, int TX, bool FEAT = false, int MINB = 0, bool PAL = false>
 __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams p) {
     const int y = blockIdx.x * kBX2 + threadIdx.x;
     const int x0 = (blockIdx.y * kBY2 + threadIdx.y) * TX;
@@ -157,10 +161,13 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
                 float ny_lo[ORD], ny_hi[ORD - 1 > 0 ? ORD - 1 : 1], sx_lo[ORD - 1 > 0 ? ORD - 1 : 1], sx_hi[ORD];
                 float rxx[R], ryy[R], rxy[R];
                 float pn0 = 0.f, pn1 = 0.f, ps0 = 0.f, ps1 = 0.f;
+                const uint16_t pidx = PAL ? __ldg(p.pal_idx + i) : 0;
                 if (in_n) {
-                    L = ldg(p.lam_dt + i);
-                    M = ldg(p.mu_dt + i);
-                    if (ZM == 2) gp = ldg(p.g_p + i);
+                    if (!PAL) {
+                        L = ldg(p.lam_dt + i);
+                        M = ldg(p.mu_dt + i);
+                        if (ZM == 2) gp = ldg(p.g_p + i);
+                    }
 #pragma unroll
                     for (int c = 0; c < ORD; ++c) ny_lo[c] = ldf(vy + i - c - 1);   // vy[y-c-1]
 #pragma unroll
@@ -179,7 +186,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
                     }
                 }
                 if (in_s) {
-                    Ms = ldg(p.mus_dt[0] + i);
+                    if (!PAL) Ms = ldg(p.mus_dt[0] + i);
 #pragma unroll
                     for (int c = 0; c < ORD; ++c) sx_hi[c] = ldf(vx + i + c + 1);   // vx[y+c+1]
 #pragma unroll
@@ -193,7 +200,15 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
                             if (l < n_mech) rxy[l] = p.r[2][l * p.grid_elems + i];
                     }
                 }
-                if (ZM == 2) gs = ldg(p.g_s + i);
+                if (ZM == 2 && !PAL) gs = ldg(p.g_s + i);
+                if (PAL) {
+                    const float4 cn = __ldg(&p.pal[pidx].normal), cs = __ldg(&p.pal[pidx].shear);
+                    L = cn.x;
+                    M = cn.y;
+                    gp = cn.z;
+                    gs = cn.w;
+                    Ms = cs.x;
+                }
                 // ---- normal stresses ----
                 if (in_n) {
                     float ddx = 0.f, ddy = 0.f, np_;
@@ -344,7 +359,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
         constexpr int NR = TX + 2 * ORD - 1;
         float rxx[NR], rxy[NR];
         float bl[TX][ORD], bh[TX][ORD - 1 > 0 ? ORD - 1 : 1], by[TX][2 * ORD];
-        float vx0[TX], vy0[TX], dx0[TX], dy0[TX], dxl[TX], dyl[TX];
+        float vx0[TX], vy0[TX], dx0[TX], dy0[TX];
 #pragma unroll
         for (int r = 0; r < NR; ++r) {
             rxx[r] = ldf(sxx + (int64_t)(x0 - ORD + r) * P + y);
@@ -361,16 +376,8 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             for (int c = 0; c < 2 * ORD; ++c) by[t][c] = ldf(syy + i - ORD + 1 + c);   // syy[y-ORD+1 .. y+ORD]
             vx0[t] = p.v[0][i];
             vy0[t] = p.v[1][i];
-            if (FAM == kWgsl) {
-                const float2 wx = __ldg(p.dtw[0] + i), wy = __ldg(p.dtw[1] + i);
-                dx0[t] = wx.x;
-                dxl[t] = wx.y;
-                dy0[t] = wy.x;
-                dyl[t] = wy.y;
-            } else {
-                dx0[t] = ldg(p.dtr[0] + i);
-                dy0[t] = ldg(p.dtr[1] + i);
-            }
+            dx0[t] = ldg(p.dtr[0] + i);
+            dy0[t] = ldg(p.dtr[1] + i);
         }
 #pragma unroll
         for (int t = 0; t < TX; ++t) {
@@ -391,7 +398,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             a = dfin<FAM>(a, p, 0);
             b = dfin<FAM>(b, p, 1);
             const float fax = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
-            const float vxn = FAM == kTaichi ? taichi_velocity(vx0[t], fax, 0.f, dx0[t], p.dt) : FAM == kWgsl ? wgsl_velocity(vx0[t], fax, make_float2(dx0[t], dxl[t]))
+            const float vxn = FAM == kTaichi ? taichi_velocity(vx0[t], fax, 0.f, dx0[t], p.dt) : FAM == kWgsl ? wgsl_velocity_rho(vx0[t], fax, dx0[t], p.dt)
                                                    : fmaf(fax, dx0[t], vx0[t]);
             a = 0.f;
             b = 0.f;
@@ -408,7 +415,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             a = dfin<FAM>(a, p, 0);
             b = dfin<FAM>(b, p, 1);
             const float fay = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
-            const float vyn = FAM == kTaichi ? taichi_velocity(vy0[t], fay, 0.f, dy0[t], p.dt) : FAM == kWgsl ? wgsl_velocity(vy0[t], fay, make_float2(dy0[t], dyl[t]))
+            const float vyn = FAM == kTaichi ? taichi_velocity(vy0[t], fay, 0.f, dy0[t], p.dt) : FAM == kWgsl ? wgsl_velocity_rho(vy0[t], fay, dy0[t], p.dt)
                                                    : fmaf(fay, dy0[t], vy0[t]);
             p.v[0][i] = vxn;
             p.v[1][i] = vyn;
@@ -442,20 +449,14 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             const int64_t ix = (int64_t)sx * P + y, iy = (int64_t)x * p.strip[1].width + syl;
             // ---- loads ----
             float bx_lo[ORD], bx_hi[ORD - 1 > 0 ? ORD - 1 : 1], by[2 * ORD];
-            float vx0 = 0.f, vy0 = 0.f, dx0 = 0.f, dy0 = 0.f, dxl = 0.f, dyl = 0.f, pxa = 0.f, pxb = 0.f, pya = 0.f, pyb = 0.f;
+            float vx0 = 0.f, vy0 = 0.f, dx0 = 0.f, dy0 = 0.f, pxa = 0.f, pxb = 0.f, pya = 0.f, pyb = 0.f;
             if (in_vx) {
 #pragma unroll
                 for (int c = 0; c < ORD; ++c) bx_lo[c] = ldf(sxy + i - c - 1);   // sxy[y-c-1]
 #pragma unroll
                 for (int c = 1; c < ORD; ++c) bx_hi[c - 1] = ldf(sxy + i + c);   // sxy[y+c], c >= 1
                 vx0 = p.v[0][i];
-                if (FAM == kWgsl) {
-                    const float2 w = __ldg(p.dtw[0] + i);
-                    dx0 = w.x;
-                    dxl = w.y;
-                } else {
-                    dx0 = ldg(p.dtr[0] + i);
-                }
+                dx0 = ldg(p.dtr[0] + i);
                 if (sx >= 0) pxa = p.psi[4][ix];
                 if (syl >= 0) pxb = p.psi[6][iy];
             }
@@ -463,13 +464,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
 #pragma unroll
                 for (int c = 0; c < 2 * ORD; ++c) by[c] = ldf(syy + i - ORD + 1 + c);   // syy[y-ORD+1 .. y+ORD]
                 vy0 = p.v[1][i];
-                if (FAM == kWgsl) {
-                    const float2 w = __ldg(p.dtw[1] + i);
-                    dy0 = w.x;
-                    dyl = w.y;
-                } else {
-                    dy0 = ldg(p.dtr[1] + i);
-                }
+                dy0 = ldg(p.dtr[1] + i);
                 if (sx >= 0) pya = p.psi[5][ix];
                 if (syl >= 0) pyb = p.psi[7][iy];
             }
@@ -500,7 +495,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                 }
                 fax = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
                 vxn = FAM == kTaichi ? taichi_velocity(vx0, fax, 0.f, dx0, p.dt)
-                      : FAM == kWgsl   ? wgsl_velocity(vx0, fax, make_float2(dx0, dxl))
+                      : FAM == kWgsl   ? wgsl_velocity_rho(vx0, fax, dx0, p.dt)
                                        : fmaf(fax, dx0, vx0);
             }
             if (in_vy) {
@@ -538,7 +533,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                     }
                     vyn = taichi_velocity(vy0, fay, src, dy0, p.dt);
                 } else {
-                    vyn = FAM == kWgsl ? wgsl_velocity(vy0, fay, make_float2(dy0, dyl)) : fmaf(fay, dy0, vy0);
+                    vyn = FAM == kWgsl ? wgsl_velocity_rho(vy0, fay, dy0, p.dt) : fmaf(fay, dy0, vy0);
                 }
             }
             if constexpr (!FAST && FAM != kTaichi) {

@@ -120,8 +120,7 @@ __global__ void __launch_bounds__(kPMaxThreads, 1) k_persist2d(const __grid_cons
         svx[r * W + y] = in ? p.v[0][(int64_t)x * P + y] : 0.f;
         svy[r * W + y] = in ? p.v[1][(int64_t)x * P + y] : 0.f;
     }
-    // velocity-node coefficients: rho (family 0) or dt / rho as (hi, lo) (family 1)
-    float cL[NS], cM[NS], cMs[NS], cdx[R], cdy[R], cdxl[R], cdyl[R];
+    float cL[NS], cM[NS], cMs[NS], cdx[R], cdy[R];   // cdx, cdy: rho at the velocity nodes
 #pragma unroll
     for (int j = 0; j < NS; ++j) {
         const int x = slo + j;
@@ -146,17 +145,8 @@ __global__ void __launch_bounds__(kPMaxThreads, 1) k_persist2d(const __grid_cons
         const int x = x0 + j;
         const bool in = col && x < nx;
         const int64_t i = (int64_t)x * P + y;
-        if (FAM == 0) {
-            cdx[j] = in ? p.dtr[0][i] : 0.f;
-            cdy[j] = in ? p.dtr[1][i] : 0.f;
-            cdxl[j] = cdyl[j] = 0.f;
-        } else {
-            const float2 wx = in ? p.dtw[0][i] : make_float2(0.f, 0.f), wy = in ? p.dtw[1][i] : make_float2(0.f, 0.f);
-            cdx[j] = wx.x;
-            cdxl[j] = wx.y;
-            cdy[j] = wy.x;
-            cdyl[j] = wy.y;
-        }
+        cdx[j] = in ? p.dtr[0][i] : 0.f;
+        cdy[j] = in ? p.dtr[1][i] : 0.f;
         const int sx = in ? strip_index(p.strip[0], x) : -1;
         spvx[(0 * R + j) * W + y] = sx >= 0 ? p.psi[4][(int64_t)sx * P + y] : 0.f;
         spvx[(1 * R + j) * W + y] = sx >= 0 ? p.psi[5][(int64_t)sx * P + y] : 0.f;
@@ -311,7 +301,7 @@ __global__ void __launch_bounds__(kPMaxThreads, 1) k_persist2d(const __grid_cons
                     if (FAM == 0) {
                         vxn = taichi_velocity(svx[jv * W + y], __fadd_rn(av, bv), 0.f, cdx[j], p.dt);
                     } else {
-                        vxn = wgsl_velocity(svx[jv * W + y], av + bv, make_float2(cdx[j], cdxl[j]));
+                        vxn = wgsl_velocity_rho(svx[jv * W + y], av + bv, cdx[j], p.dt);
                     }
                 }
                 if (in_vy) {
@@ -335,7 +325,7 @@ __global__ void __launch_bounds__(kPMaxThreads, 1) k_persist2d(const __grid_cons
                         }
                         vyn = taichi_velocity(svy[jv * W + y], __fadd_rn(av, bv), src, cdy[j], p.dt);
                     } else {
-                        vyn = wgsl_velocity(svy[jv * W + y], av + bv, make_float2(cdy[j], cdyl[j]));
+                        vyn = wgsl_velocity_rho(svy[jv * W + y], av + bv, cdy[j], p.dt);
                     }
                 }
                 if (FAM != 0) {

@@ -21,6 +21,16 @@ void launch_tx(const StepParams &p, int zen_mode, int j, cudaStream_t st, int pa
         if (parts & 2) launch_pdl(k_velocity2d<ORD, 0, TX>, grid, block, st, p, j);
         return;
     }
+    if constexpr (ORD == 2) {   // coefficient palette (order 2 only, the benchmark's)
+        if ((parts & 1) && p.pal) {
+            if (zen_mode == 0) launch_pdl(k_stress2d<ORD, kWgsl, 0, 0, TX, false, 0, true>, grid, block, st, p);
+            else if (zen_mode == 1 && three) launch_pdl(k_stress2d<ORD, kWgsl, 1, 3, TX, false, 0, true>, grid, block, st, p);
+            else if (zen_mode == 1) launch_pdl(k_stress2d<ORD, kWgsl, 1, kMaxSls, TX, false, 0, true>, grid, block, st, p);
+            else if (three) launch_pdl(k_stress2d<ORD, kWgsl, 2, 3, TX, false, 4, true>, grid, block, st, p);
+            else launch_pdl(k_stress2d<ORD, kWgsl, 2, kMaxSls, TX, false, 0, true>, grid, block, st, p);
+            parts &= ~1;
+        }
+    }
     if (parts & 1) {
         if (zen_mode == 0) launch_pdl(k_stress2d<ORD, kWgsl, 0, 0, TX>, grid, block, st, p);
         else if (zen_mode == 1 && three) launch_pdl(k_stress2d<ORD, kWgsl, 1, 3, TX>, grid, block, st, p);

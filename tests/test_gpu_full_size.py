@@ -133,6 +133,32 @@ def test_full_fmc2d_three_phantoms_300_steps():
             assert e_tr <= TOL and e_f <= TOL, (q, s, e_tr, e_f)
 
 
+def test_fmc2d_all_3000_steps_512x768():
+    """Long-run accuracy of the batched kernels: all 3000 steps of the
+    smallest phantom's 64-shot batch (about 90 wavelengths travelled), shots
+    0 and 63 against the oracle."""
+    from taichi_sim_gb300.batch import BatchStepper, fmc_shot_sources
+    sim = Simulator(workloads.fmc2d_phantoms(shapes=((512, 768),))[0])
+    assert sim._n_steps == 3000
+    shots = fmc_shot_sources(sim)
+    with BatchStepper([sim], [shots]) as b:
+        b.run(sim._n_steps)
+        assert b.status()[2] == -1
+        tr, f = b.traces(0), b.field(0, "syy")
+    for s in (0, 63):
+        ref = _with_shot(sim, shots[s], lambda: oracle.run(sim, oracle.WGSL2D))
+        e_tr, e_f = rel_l2(tr[s], ref["sens"]), rel_l2(f[s], ref["syy"])
+        assert e_tr <= TOL and e_f <= TOL, (s, e_tr, e_f)
+
+
+def test_visco3d_all_1000_steps_96():
+    """Long-run accuracy in 3D: the visco3d workload's model (layers, per-cell
+    Q, Ricker source, receiver plane) on a 96^3 grid for all 1000 steps."""
+    sim = Simulator3D(workloads.visco3d_256(n_grid=96))
+    assert sim._n_steps == 1000
+    _check_stepper(sim, engine.WGSL3D, F3, 1000)
+
+
 def test_full_adjoint2d_512x1024_forward_300_steps():
     """The adjoint's forward (checkpointed, through ts_adj_forward) on the
     full 512 x 1024 model, one shot, against the oracle."""

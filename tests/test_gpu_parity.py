@@ -103,6 +103,24 @@ def test_parity_2d_nodes_per_thread(name, tx, monkeypatch):
     _compare(sim, family, ["vx", "vy", "sxx", "syy", "sxy"])
 
 
+@pytest.mark.parametrize("name", ["wgsl_elastic", "wgsl_visco", "wgsl_visco_q", "wgsl_delayed_rx"])
+def test_parity_2d_coefficient_arrays(name, monkeypatch):
+    """The WGSL stepper's other coefficient path: one array per coefficient
+    instead of the order-2 palette of distinct coefficient tuples."""
+    monkeypatch.setenv("TS_2D_COEF_PALETTE", "0")
+    build, family = CASES_2D[name]
+    _compare(Simulator(build()), family, ["vx", "vy", "sxx", "syy", "sxy"])
+
+
+@pytest.mark.parametrize("name", ["wgsl_elastic", "wgsl_visco", "wgsl_visco_q", "wgsl_delayed_rx"])
+def test_parity_2d_coefficient_arrays(name, monkeypatch):
+    """The WGSL stepper's other coefficient path: one array per coefficient
+    instead of the order-2 palette of distinct coefficient tuples."""
+    monkeypatch.setenv("TS_2D_COEF_PALETTE", "0")
+    build, family = CASES_2D[name]
+    _compare(Simulator(build()), family, ["vx", "vy", "sxx", "syy", "sxy"])
+
+
 TAICHI_CASES = sorted(n for n, (_, f) in CASES_2D.items() if f == engine.TAICHI2D)
 
 
