@@ -46,14 +46,17 @@ sys.path.insert(0, ROOT)
 
 from taichi_sim_gb300 import workloads  # noqa: E402
 
-# Per-cell bytes each kernel must move at least once per step (float32):
-# stress: v read (2D 8, 3D 12), stresses r/w, memory variables r/w, moduli,
-# per-cell Q scale; velocity: stresses read, v r/w, dt/rho.  CPML strip
-# memories are added per strip cell.
+# Per-cell bytes each kernel must move at least once per step (float32),
+# counting each array of its data layout once: stress: v read (2D 8, 3D 12),
+# stresses r/w, memory variables r/w, and the coefficients as stored: a
+# 2-byte palette index (2D order-2 WGSL stepper, 3D) or lambda, mu, mu_s
+# (Taichi 2D); velocity: stresses read, v r/w, rho (2D, 4 B per node and
+# component) or dt / rho as a (hi, lo) pair (3D, 8 B).  CPML strip memories
+# are added per strip cell.
 KERNEL_BYTES = {
-    "visco2d": {"stress": 8 + 24 + 72 + 12 + 8, "velocity": 12 + 16 + 8, "psi_stress": 8 * 2, "psi_vel": 8 * 2},
+    "visco2d": {"stress": 8 + 24 + 72 + 2, "velocity": 12 + 16 + 8, "psi_stress": 8 * 2, "psi_vel": 8 * 2},
     "elastic2d": {"stress": 8 + 24 + 12, "velocity": 12 + 16 + 8, "psi_stress": 8 * 2, "psi_vel": 8 * 2},
-    "visco3d": {"stress": 12 + 48 + 144 + 20 + 8, "velocity": 24 + 24 + 8, "psi_stress": 8 * 3, "psi_vel": 8 * 3},
+    "visco3d": {"stress": 12 + 48 + 144 + 2, "velocity": 24 + 24 + 16, "psi_stress": 8 * 3, "psi_vel": 8 * 3},
 }
 FAMILY = {"elastic2d": "TAICHI2D", "visco2d": "WGSL2D", "visco3d": "WGSL3D"}
 
