@@ -207,7 +207,9 @@ using ts::round_up;
 
 // Kernel launches of one time step: 2D stress + velocity; 3D normal stress,
 // shear stress, velocity.
-static int kernels_per_step(const ts_sim *s) { return (s->dims == 3 ? 3 : 2) + (s->rc.n_chunks > 0 ? 1 : 0); }
+static int kernels_per_step(const ts_sim *s) {
+    return (s->dims == 3 ? (s->p.stress_pair_3d ? 2 : 3) : 2) + (s->rc.n_chunks > 0 ? 1 : 0);
+}
 
 extern "C" {
 
@@ -382,6 +384,8 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         }
         const char *xy = getenv("TS_3D_XY_SWEEP");
         p.xy_sweep_3d = !(xy && xy[0] == '0');
+        const char *pair = getenv("TS_3D_STRESS_PAIR");
+        p.stress_pair_3d = !(pair && pair[0] == '0');
     }
     p.nx = nx;
     p.ny = ny;

@@ -67,6 +67,7 @@ struct StepParams {
     int family;
     int tx;                // 2D: nodes each thread updates along x (1, 2 or 4)
     int xy_sweep_3d;       // 3D velocity kernel: warps interior in x and y take the x-y sweep
+    int stress_pair_3d;    // 3D: normal and shear stress updates in one launch (k_stress3d)
     int nx, ny, nz;        // nz = 1 in 2D
     int pitch;             // padded last-axis length (floats)
     int64_t plane;         // ny * pitch (3D x stride); 2D: pitch

@@ -141,10 +141,10 @@ __device__ __forceinline__ float wderiv(const float (&w)[2 * ORD], const StepPar
 // the x-derivative of vx from a register window, the y- and z-derivatives
 // from loads.
 template <int ORD, int ZM, int NS, typename I, bool PAL>
-__global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_normal3d(const StepParams p) {
+__device__ __forceinline__ void normal3d_body(const StepParams &p, int bz) {
     const int z = blockIdx.x * kZB3 + (threadIdx.y % kZW3) * kBX3 + threadIdx.x;
     const int y = blockIdx.y * kYB3 + threadIdx.y / kZW3;
-    const int x0 = blockIdx.z * kTX3S;
+    const int x0 = bz * kTX3S;
     if (y >= p.ny || z >= p.nz || x0 >= p.nx) return;
     const I X = (I)p.plane, Y = (I)p.pitch, yz = (I)y * Y + z, G = (I)p.grid_elems;
     const float *__restrict__ vx = p.v[0];
@@ -261,10 +261,10 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_normal3d(const
 // strips), x-marching as k_normal3d: the x-derivatives of vy and vz from
 // register windows.
 template <int ORD, int ZM, int NS, typename I, bool PAL>
-__global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_shear3d(const StepParams p) {
+__device__ __forceinline__ void shear3d_body(const StepParams &p, int bz) {
     const int z = blockIdx.x * kZB3 + (threadIdx.y % kZW3) * kBX3 + threadIdx.x;
     const int y = blockIdx.y * kYB3 + threadIdx.y / kZW3;
-    const int x0 = blockIdx.z * kTX3S;
+    const int x0 = bz * kTX3S;
     if (y >= p.ny || z >= p.nz || x0 >= p.nx) return;
     const I X = (I)p.plane, Y = (I)p.pitch, yz = (I)y * Y + z, G = (I)p.grid_elems;
     const float *__restrict__ vx = p.v[0];
@@ -415,6 +415,26 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_shear3d(const 
         }
     }
     pdl_trigger();
+}
+
+template <int ORD, int ZM, int NS, typename I, bool PAL>
+__global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_normal3d(const StepParams p) {
+    normal3d_body<ORD, ZM, NS, I, PAL>(p, blockIdx.z);
+}
+
+template <int ORD, int ZM, int NS, typename I, bool PAL>
+__global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_shear3d(const StepParams p) {
+    shear3d_body<ORD, ZM, NS, I, PAL>(p, blockIdx.z);
+}
+
+// Both stress updates in one launch: block z-index 2c updates the normal
+// stresses of x-chunk c, 2c + 1 its shear stresses.  Both read the same
+// velocities at about the same time, so the second read of a chunk mostly
+// hits L2, and a step has one launch boundary fewer.
+template <int ORD, int ZM, int NS, typename I, bool PAL>
+__global__ void __launch_bounds__(kBX3 *kBY3, kStressMinBlocks) k_stress3d(const StepParams p) {
+    if (blockIdx.z & 1) shear3d_body<ORD, ZM, NS, I, PAL>(p, blockIdx.z >> 1);
+    else normal3d_body<ORD, ZM, NS, I, PAL>(p, blockIdx.z >> 1);
 }
 
 // Velocity update, x-marching: thread (z, y) updates TX consecutive nodes
@@ -596,7 +616,14 @@ void launch_idx(const StepParams &p, int zen_mode, int j, cudaStream_t st, int p
     const bool three = p.zen.n == 3;
     if (parts & 1) {
         const dim3 grid((p.nz + kZB3 - 1) / kZB3, (p.ny + kYB3 - 1) / kYB3, (p.nx + kTX3S - 1) / kTX3S);
-        if (zen_mode == 0) {
+        if (p.stress_pair_3d) {
+            const dim3 g2(grid.x, grid.y, 2 * grid.z);
+            if (zen_mode == 0) launch_pdl(k_stress3d<ORD, 0, 0, I, PAL>, g2, block, st, p);
+            else if (zen_mode == 1 && three) launch_pdl(k_stress3d<ORD, 1, 3, I, PAL>, g2, block, st, p);
+            else if (zen_mode == 1) launch_pdl(k_stress3d<ORD, 1, kMaxSls, I, PAL>, g2, block, st, p);
+            else if (three) launch_pdl(k_stress3d<ORD, 2, 3, I, PAL>, g2, block, st, p);
+            else launch_pdl(k_stress3d<ORD, 2, kMaxSls, I, PAL>, g2, block, st, p);
+        } else if (zen_mode == 0) {
             launch_pdl(k_normal3d<ORD, 0, 0, I, PAL>, grid, block, st, p);
             launch_pdl(k_shear3d<ORD, 0, 0, I, PAL>, grid, block, st, p);
         } else if (zen_mode == 1 && three) {
