@@ -71,10 +71,15 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def build_model(name, time_steps=None):
+def build_model(name, time_steps=None, grid=None):
     from taichi_sim_gb300.sim_support.simulator import Simulator
     from taichi_sim_gb300.sim_support.Simulator3D import Simulator3D
-    cfg = workloads.WORKLOADS[name]() if time_steps is None else workloads.WORKLOADS[name](n_steps=time_steps)
+    kw = {}
+    if time_steps is not None:
+        kw["n_steps"] = time_steps
+    if grid is not None:
+        kw["n_grid"] = grid
+    cfg = workloads.WORKLOADS[name](**kw)
     return (Simulator3D if name == "visco3d" else Simulator)(cfg)
 
 
@@ -224,7 +229,7 @@ def stepper_record(name, args, steps, warmup, world=1, rank=0, local=0, dist=Non
     import torch
     from taichi_sim_gb300 import engine, shards
 
-    sim = build_model(name, args.time_steps)
+    sim = build_model(name, args.time_steps, args.grid)
     n_t = int(sim._n_steps)
     cells = int(np.prod(sim.grid_shape()))
     fam = getattr(engine, FAMILY[name])
@@ -656,6 +661,8 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=200)
     ap.add_argument("--time-steps", type=int, default=None,
                     help="override the workload's time steps (small runs for profiler captures)")
+    ap.add_argument("--grid", type=int, default=None,
+                    help="elastic2d/visco2d/visco3d: nodes per side instead of the workload's (profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("bench: at least 3 warm-up steps are required; using 3", file=sys.stderr)
