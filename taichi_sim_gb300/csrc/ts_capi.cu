@@ -155,10 +155,11 @@ struct ts_sim {
 
 using ts::Axis;
 
-// Coefficient palette of a 3D model: the distinct tuples of the stress
-// kernels' per-node coefficients (compared bit for bit) and each node's
-// 16-bit index into them.  Models built from a few materials (layers, inclusions) have a few
-// dozen tuples; false when there are more than 65536 (the arrays are used).
+// Coefficient palette of a 3D model (and of the 2D order-2 WGSL stepper):
+// the distinct tuples of the stress kernels' per-node coefficients (compared
+// bit for bit) and each node's 16-bit index into them.  Models built from a
+// few materials (layers, inclusions) have a few dozen tuples; false when
+// there are more than 65536 (the arrays are used).
 bool build_palette_3d(const std::vector<float> *const (&c)[7], std::vector<uint16_t> &idx,
                       std::vector<ts::Pal3> &table) {
     struct Key {
@@ -201,6 +202,15 @@ bool build_palette_3d(const std::vector<float> *const (&c)[7], std::vector<uint1
         last_id = id;
     }
     return true;
+}
+
+// dt / rho as a pair (hi, lo), computed in double from the float dt and rho
+// (0 where rho <= 0: no update)
+static float2 dt_over_rho(float dt, float rho) {
+    if (!(rho > 0.f)) return make_float2(0.f, 0.f);
+    const double q = (double)dt / (double)rho;
+    const float hi = (float)q;
+    return make_float2(hi, (float)(q - (double)hi));
 }
 using ts::make_axis;
 using ts::round_up;
@@ -540,16 +550,11 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         p.dtr[0] = dev;
         if ((rc = s->upload(&dev, dtr1))) return bail(rc);
         p.dtr[1] = dev;
-    } else {   // dt / rho as (hi, lo) pairs, computed in double from the float dt and rho
+    } else {   // dt / rho as (hi, lo) pairs
         for (int c = 0; c < 2; ++c) {
             const std::vector<float> &rh = c == 0 ? dtr0 : dtr1;
-            std::vector<float2> w(rh.size(), make_float2(0.f, 0.f));
-            for (size_t i = 0; i < rh.size(); ++i)
-                if (rh[i] > 0.f) {
-                    const double q = (double)dt / (double)rh[i];
-                    const float hi = (float)q;
-                    w[i] = make_float2(hi, (float)(q - (double)hi));
-                }
+            std::vector<float2> w(rh.size());
+            for (size_t i = 0; i < rh.size(); ++i) w[i] = dt_over_rho(d->dt, rh[i]);
             float2 *dw = nullptr;
             if ((rc = s->upload(&dw, w))) return bail(rc);
             p.dtw[c] = dw;

@@ -56,8 +56,9 @@ struct Source {
 // Everything a 2D or 3D kernel reads, passed by value.
 // One entry of the 3D coefficient palette: the coefficients each stress
 // kernel reads at a node, grouped so that a kernel fetches its own with one
-// load.  (The velocity kernel reads dt / rho from its arrays: its palette
-// variant measured slower.)
+// load.  (The velocity kernel reads its dt / rho pairs from arrays: a
+// variant reading them from a second table under the same index measured
+// slower, the dependent index load sitting on its critical path.)
 struct alignas(16) Pal3 {
     float4 normal;    // lambda dt, mu dt, Q scale p, Q scale s
     float4 shear;     // mu dt at the xy, xz, yz nodes, Q scale s
@@ -97,7 +98,7 @@ struct StepParams {
     // adjoint's forward and the batched kernels: lambda dt, mu dt, dt / rho)
     const float *lam_dt, *mu_dt;          // normal node
     const float *mus_dt[3];               // shear nodes xy, xz, yz (2D: xy)
-    const float *dtr[3];                  // dt / rho at vx, vy, vz nodes (0: no update)
+    const float *dtr[3];                  // rho at the vx, vy nodes (the folded forward: dt / rho; 0: no update)
     const float2 *dtw[3];                 // 3D stepper: dt / rho as a pair (hi, lo), hi + lo exact to ~48 bits
     const float *g_p, *g_s;               // per-cell attenuation scale (or null)
     // 3D coefficient palette (or null): the stress kernels take node i's
@@ -305,7 +306,10 @@ constexpr int kBX3 = 32, kBY3 = 8, kTX3S = 4;
 // 8 on the 256^3 case: longer contiguous runs per block, y-neighbours still
 // shared in L1).
 constexpr int kZW3 = 2, kZB3 = kBX3 * kZW3, kYB3 = kBY3 / kZW3;
-constexpr int velocity_tx_3d(int ord) { return ord == 2 ? 4 : 2; }
+#ifndef TS_VELOCITY3D_TX
+#define TS_VELOCITY3D_TX 4
+#endif
+constexpr int velocity_tx_3d(int ord) { return ord == 2 ? TS_VELOCITY3D_TX : 2; }
 
 // Flat index of the 3D velocity block that updates node (x, y, z).
 inline int block_of_3d(const StepParams &p, int x, int y, int z) {

@@ -29,7 +29,8 @@
 // Coefficients: with PAL the stress kernels take the per-node coefficients
 // from a palette (one 16-bit index per node into a table of the model's
 // distinct coefficient tuples, ts_internal.cuh: Pal3), otherwise from one
-// array per coefficient; the velocity kernel reads dt / rho arrays.
+// array per coefficient; the velocity kernel reads its dt / rho pairs from
+// arrays (a variant reading them from a palette table measured slower).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -84,7 +85,10 @@ __device__ __forceinline__ float deriv(const Pairs<ORD> &q, const StepParams &p,
 
 // Resident blocks per SM the kernels are compiled for (register budgets 64
 // and 85 per thread; measured against 1 to 4 on the 256^3 case).
-constexpr int kStressMinBlocks = 4, kVelocityMinBlocks = 3;
+#ifndef TS_VELOCITY3D_MIN_BLOCKS
+#define TS_VELOCITY3D_MIN_BLOCKS 3
+#endif
+constexpr int kStressMinBlocks = 4, kVelocityMinBlocks = TS_VELOCITY3D_MIN_BLOCKS;
 // x window of 2*ORD planes of one field at (y, z), first plane r0; planes
 // outside the grid read 0
 // (CHECK = false: every plane is known to lie inside the grid)
