@@ -396,6 +396,8 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         p.xy_sweep_3d = !(xy && xy[0] == '0');
         const char *pair = getenv("TS_3D_STRESS_PAIR");
         p.stress_pair_3d = !(pair && pair[0] == '0');
+        const char *pf = getenv("TS_3D_PREFETCH");   // "0": no L2 prefetch of a thread's later x nodes
+        p.prefetch_3d = !(pf && pf[0] == '0');
     }
     p.nx = nx;
     p.ny = ny;

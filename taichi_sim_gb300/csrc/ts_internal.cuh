@@ -69,6 +69,7 @@ struct StepParams {
     int tx;                // 2D: nodes each thread updates along x (1, 2 or 4)
     int xy_sweep_3d;       // 3D velocity kernel: warps interior in x and y take the x-y sweep
     int stress_pair_3d;    // 3D: normal and shear stress updates in one launch (k_stress3d)
+    int prefetch_3d;       // 3D: the kernels prefetch the state of a thread's later x nodes into L2 first
     int nx, ny, nz;        // nz = 1 in 2D
     int pitch;             // padded last-axis length (floats)
     int64_t plane;         // ny * pitch (3D x stride); 2D: pitch
@@ -244,6 +245,9 @@ enum { kFeatLam = 0, kFeatMuX, kFeatMuY, kFeatShear, kFeatVx, kFeatVy, kFeat };
 // path: that kernel's lifetime overlaps this one's, and such reads returned
 // stale values in a few percent of runs.  The trigger lets the next
 // kernel's launch start once every block of this one has issued it.
+// Hint: bring the 128-byte line holding `a` into L2 (no register, no wait).
+__device__ __forceinline__ void prefetch_l2(const void *a) { asm volatile("prefetch.global.L2 [%0];" ::"l"(a)); }
+
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 

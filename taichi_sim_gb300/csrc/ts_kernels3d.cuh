@@ -159,6 +159,24 @@ __device__ __forceinline__ void normal3d_body(const StepParams &p, int bz) {
     const int n_mech = NS == 3 ? 3 : p.zen.n;
     constexpr int R = NS > 0 ? NS : 1;
     pdl_wait();
+    if (p.prefetch_3d && yz_n) {   // the later nodes' stresses and memory variables
+#pragma unroll
+        for (int t = 1; t < kTX3S; ++t) {
+            const int x = x0 + t;
+            if (x >= ORD - 1 && x < p.nx - ORD) {
+                const I i = (I)x * X + yz;
+                prefetch_l2(p.s[0] + i);
+                prefetch_l2(p.s[1] + i);
+                prefetch_l2(p.s[2] + i);
+                if (ZM != 0)
+                    for (int l = 0; l < n_mech; ++l) {
+                        prefetch_l2(p.r[0] + l * G + i);
+                        prefetch_l2(p.r[1] + l * G + i);
+                        prefetch_l2(p.r[2] + l * G + i);
+                    }
+            }
+        }
+    }
     float wx[2 * ORD];   // vx planes [x-ORD+1, x+ORD]
     xwindow<ORD>(wx, vx, x0 - ORD + 1, p.nx, X, yz);
 #pragma unroll
@@ -279,6 +297,24 @@ __device__ __forceinline__ void shear3d_body(const StepParams &p, int bz) {
     const int n_mech = NS == 3 ? 3 : p.zen.n;
     constexpr int R = NS > 0 ? NS : 1;
     pdl_wait();
+    if (p.prefetch_3d && yz_s) {   // the later nodes' stresses and memory variables
+#pragma unroll
+        for (int t = 1; t < kTX3S; ++t) {
+            const int x = x0 + t;
+            if (x >= ORD - 1 && x < p.nx - ORD + 1) {
+                const I i = (I)x * X + yz;
+                prefetch_l2(p.s[3] + i);
+                prefetch_l2(p.s[4] + i);
+                prefetch_l2(p.s[5] + i);
+                if (ZM != 0)
+                    for (int l = 0; l < n_mech; ++l) {
+                        prefetch_l2(p.r[3] + l * G + i);
+                        prefetch_l2(p.r[4] + l * G + i);
+                        prefetch_l2(p.r[5] + l * G + i);
+                    }
+            }
+        }
+    }
     float wy[2 * ORD], wz[2 * ORD];   // vy and vz planes [x-ORD, x+ORD-1]
     xwindow<ORD>(wy, vy, x0 - ORD, p.nx, X, yz);
     xwindow<ORD>(wz, vz, x0 - ORD, p.nx, X, yz);
@@ -469,6 +505,22 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
     const bool fast = interior_warp<ORD, TX>(p, y, z, x0, sy, sz) && q0 == q1;
     const bool fast_xy = !fast && q0 == q1 && p.xy_sweep_3d && xy_interior_warp<ORD, TX>(p, y, z, x0, sy);
     pdl_wait();
+    if (p.prefetch_3d && col) {   // the later nodes' velocities, dt / rho and stresses
+#pragma unroll
+        for (int t = 1; t < TX; ++t) {
+            const int x = x0 + t;
+            if (x < p.nx) {
+                const I i = (I)x * X + yz;
+                prefetch_l2(p.v[0] + i);
+                prefetch_l2(p.v[1] + i);
+                prefetch_l2(p.v[2] + i);
+                prefetch_l2(p.dtw[0] + i);
+                prefetch_l2(p.dtw[1] + i);
+#pragma unroll
+                for (int f = 0; f < 6; ++f) prefetch_l2(p.s[f] + i);
+            }
+        }
+    }
     const int k = *p.step_base + j;
     unsigned vmax = 0u;  // max |v|^2 as float bits (v2 >= 0 or NaN: NaN ranks highest)
     bool bad = false;
