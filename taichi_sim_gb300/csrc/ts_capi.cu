@@ -25,6 +25,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -32,6 +34,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -86,6 +89,42 @@ int cuda_fail(cudaError_t e, const char *what) {
     } while (0)
 
 constexpr int kGraphSteps = 32;
+
+// f(x) for x in [0, n) on up to 16 host threads (rows of the host-side
+// preparation; every x writes its own nodes).
+template <typename F>
+void parallel_rows(int n, const F &f) {
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const int nt = (int)std::min<int64_t>(hw, std::max(1, n / 4));
+    if (nt <= 1) {
+        for (int x = 0; x < n; ++x) f(x);
+        return;
+    }
+    std::atomic<int> next{0};
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t)
+        pool.emplace_back([&] {
+            for (int x; (x = next.fetch_add(1)) < n;) f(x);
+        });
+    for (auto &t : pool) t.join();
+}
+
+// Phase times of ts_create on stderr when TS_CREATE_TIMING=1 (diagnostic).
+struct PhaseClock {
+    bool on = false;
+    std::chrono::steady_clock::time_point t0;
+    PhaseClock() {
+        const char *e = getenv("TS_CREATE_TIMING");
+        on = e && e[0] == '1';
+        t0 = std::chrono::steady_clock::now();
+    }
+    void mark(const char *what) {
+        if (!on) return;
+        const auto t = std::chrono::steady_clock::now();
+        fprintf(stderr, "ts_create %-14s %8.3f ms\n", what, std::chrono::duration<double, std::milli>(t - t0).count());
+        t0 = t;
+    }
+};
 
 }  // namespace
 
@@ -157,50 +196,79 @@ using ts::Axis;
 
 // Coefficient palette of a 3D model (and of the 2D order-2 WGSL stepper):
 // the distinct tuples of the stress kernels' per-node coefficients (compared
-// bit for bit) and each node's 16-bit index into them.  Models built from a
-// few materials (layers, inclusions) have a few dozen tuples; false when
-// there are more than 65536 (the arrays are used).
-bool build_palette_3d(const std::vector<float> *const (&c)[7], std::vector<uint16_t> &idx,
+// bit for bit) and each node's 16-bit index into them, numbered in the order
+// of first occurrence.  Models built from a few materials (layers,
+// inclusions) have a few dozen tuples; false when there are more than 65536
+// (the arrays are used).  The grid is scanned in `rows` slabs in parallel
+// (each slab's own distinct tuples), then the slabs' tuples are numbered in
+// slab order, which is the sequential scan's numbering.
+struct PalKey {
+    uint32_t w[7];
+    bool operator==(const PalKey &o) const { return std::memcmp(w, o.w, sizeof w) == 0; }
+};
+struct PalHash {
+    size_t operator()(const PalKey &k) const {
+        uint64_t h = 1469598103934665603ull;   // FNV-1a over the words
+        for (uint32_t v : k.w) h = (h ^ v) * 1099511628211ull;
+        return (size_t)h;
+    }
+};
+
+bool build_palette_3d(const std::vector<float> *const (&c)[7], int rows, std::vector<uint16_t> &idx,
                       std::vector<ts::Pal3> &table) {
-    struct Key {
-        uint32_t w[7];
-        bool operator==(const Key &o) const { return std::memcmp(w, o.w, sizeof w) == 0; }
-    };
-    struct Hash {
-        size_t operator()(const Key &k) const {
-            uint64_t h = 1469598103934665603ull;   // FNV-1a over the words
-            for (uint32_t v : k.w) h = (h ^ v) * 1099511628211ull;
-            return (size_t)h;
-        }
-    };
     const size_t n = c[0]->size();
+    const size_t per = (n + rows - 1) / rows;
     idx.assign(n, 0);
     table.clear();
-    std::unordered_map<Key, uint16_t, Hash> ids;
-    Key last{};
-    int last_id = -1;
-    for (size_t i = 0; i < n; ++i) {
-        Key k;
-        for (int f = 0; f < 7; ++f) std::memcpy(&k.w[f], &(*c[f])[i], 4);
-        if (last_id >= 0 && k == last) {   // runs along z share a tuple
-            idx[i] = (uint16_t)last_id;
-            continue;
+    std::vector<std::vector<PalKey>> keys(rows);   // each slab's distinct tuples, first occurrence first
+    std::atomic<bool> over{false};
+    parallel_rows(rows, [&](int r) {
+        std::unordered_map<PalKey, uint16_t, PalHash> ids;
+        PalKey last{};
+        int last_id = -1;
+        for (size_t i = r * per; i < std::min(n, (r + 1) * per); ++i) {
+            PalKey k;
+            for (int f = 0; f < 7; ++f) std::memcpy(&k.w[f], &(*c[f])[i], 4);
+            if (last_id >= 0 && k == last) {   // runs along the last axis share a tuple
+                idx[i] = (uint16_t)last_id;
+                continue;
+            }
+            auto it = ids.find(k);
+            int id;
+            if (it != ids.end()) {
+                id = it->second;
+            } else {
+                if (keys[r].size() == 65536) {
+                    over = true;
+                    return;
+                }
+                id = (int)keys[r].size();
+                ids.emplace(k, (uint16_t)id);
+                keys[r].push_back(k);
+            }
+            idx[i] = (uint16_t)id;
+            last = k;
+            last_id = id;
         }
-        auto it = ids.find(k);
-        int id;
-        if (it != ids.end()) {
-            id = it->second;
-        } else {
-            if (table.size() == 65536) return false;
-            id = (int)table.size();
-            ids.emplace(k, (uint16_t)id);
-            const auto v = [&](int f) { return (*c[f])[i]; };
-            table.push_back(ts::Pal3{make_float4(v(0), v(1), v(2), v(3)), make_float4(v(4), v(5), v(6), v(3))});
+    });
+    if (over) return false;
+    std::unordered_map<PalKey, uint16_t, PalHash> global;
+    std::vector<std::vector<uint16_t>> to_global(rows);
+    for (int r = 0; r < rows; ++r)
+        for (const PalKey &k : keys[r]) {
+            auto it = global.find(k);
+            if (it == global.end()) {
+                if (table.size() == 65536) return false;
+                it = global.emplace(k, (uint16_t)table.size()).first;
+                float v[7];
+                std::memcpy(v, k.w, sizeof v);
+                table.push_back(ts::Pal3{make_float4(v[0], v[1], v[2], v[3]), make_float4(v[4], v[5], v[6], v[3])});
+            }
+            to_global[r].push_back(it->second);
         }
-        idx[i] = (uint16_t)id;
-        last = k;
-        last_id = id;
-    }
+    parallel_rows(rows, [&](int r) {
+        for (size_t i = r * per; i < std::min(n, (r + 1) * per); ++i) idx[i] = to_global[r][idx[i]];
+    });
     return true;
 }
 
@@ -336,16 +404,23 @@ static int validate(const ts_desc *d) {
 int ts_create(const ts_desc *d, ts_sim **out) {
     if (!out) return fail(TS_E_ARG, "null output handle");
     *out = nullptr;
+    PhaseClock clk;
     int rc = validate(d);
     if (rc) return rc;
+    clk.mark("validate");
 
     int device = 0;
     TS_CUDA(cudaGetDevice(&device));
-    cudaDeviceProp prop;
-    TS_CUDA(cudaGetDeviceProperties(&prop, device));
-    if (!(prop.major == 10 && prop.minor == 3))
-        return fail(TS_E_NODEV, "device " + std::string(prop.name) + " is sm_" + std::to_string(prop.major) +
-                                    std::to_string(prop.minor) + "; this library is built for sm_103a only");
+    int cc_major = 0, cc_minor = 0, n_sms = 0;   // attribute queries: cheaper than the whole property block
+    TS_CUDA(cudaDeviceGetAttribute(&cc_major, cudaDevAttrComputeCapabilityMajor, device));
+    TS_CUDA(cudaDeviceGetAttribute(&cc_minor, cudaDevAttrComputeCapabilityMinor, device));
+    TS_CUDA(cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, device));
+    if (!(cc_major == 10 && cc_minor == 3)) {
+        cudaDeviceProp prop;
+        TS_CUDA(cudaGetDeviceProperties(&prop, device));
+        return fail(TS_E_NODEV, "device " + std::string(prop.name) + " is sm_" + std::to_string(cc_major) +
+                                    std::to_string(cc_minor) + "; this library is built for sm_103a only");
+    }
 
     ts_sim *s = new ts_sim();
     s->device = device;
@@ -387,7 +462,10 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         const int64_t cells = (int64_t)d->nx * d->ny;
         // measured on GB300: 2 nodes per thread is fastest from ~200k nodes
         // (1024^2 viscoelastic, 512^2 elastic); 4 loses occupancy to registers
-        p.tx = s->dims == 3 ? ts::velocity_tx_3d(d->ord) : (cells >= 200000 ? 2 : 1);
+        // 2D: one node per thread up to 768^2 grids, two from 1024^2
+        // (measured: 512^2 elastic 26.7 against 22.6 Gcell/s, 640^2 visco
+        // 33.9 / 32.1, 768^2 38.6 / 38.2, 1024^2 43.6 / 47.4)
+        p.tx = s->dims == 3 ? ts::velocity_tx_3d(d->ord) : (cells >= 800000 ? 2 : 1);
         if (const char *env = getenv("TS_2D_NODES_PER_THREAD")) {
             const int v = atoi(env);
             if (v == 1 || v == 2 || v == 4) p.tx = v;
@@ -414,6 +492,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     for (int a = 0; a < 3; ++a) p.odl[a] = steps[a] > 0.f ? (float)(1.0 / (double)steps[a] - (double)p.od[a]) : 0.f;
     p.dt = d->dt;
 
+    clk.mark("setup");
     // ---- CPML tables and strips ----
     Axis axes[3];
     axes[0] = make_axis(nx, ord, d->a_x, d->b_x, d->k_x, d->a_xh, d->b_xh, d->k_xh);
@@ -428,6 +507,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         p.strip[a] = axes[a].strip;
     }
 
+    clk.mark("cpml");
     // ---- fields ----
     const int nfields = s->dims == 2 ? 5 : 9;
     const int field_ids2[5] = {TS_VX, TS_VY, TS_SXX, TS_SYY, TS_SXY};
@@ -457,6 +537,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         }
     }
 
+    clk.mark("fields");
     // ---- per-node coefficients (host, reference averaging, folded with dt) ----
     const float dt = d->dt;
     std::vector<float> lam(s->grid_elems, 0.f), mu(s->grid_elems, 0.f), dtr0(s->grid_elems, 0.f),
@@ -467,7 +548,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     if (s->dims == 2) {
         // normal node x-averaged (mu zero where either cs is zero), shear
         // node y-averaged, vy node 4-point averaged (ts_prep.h)
-        for (int x = 0; x < nx; ++x)
+        parallel_rows(nx, [&](int x) {
             for (int y = 0; y < ny; ++y) {
                 const int64_t i = s->at(x, y);
                 const ts::Coef2D c = ts::coef_2d(d, x, y);
@@ -479,8 +560,9 @@ int ts_create(const ts_desc *d, ts_sim **out) {
                 dtr0[i] = c.rho_vx;
                 dtr1[i] = c.rho_vy;
             }
+        });
     } else {
-        for (int x = 0; x < nx; ++x)
+        parallel_rows(nx, [&](int x) {
             for (int y = 0; y < ny; ++y)
                 for (int z = 0; z < nz; ++z) {
                     const int64_t i = s->at(x, y, z);
@@ -499,7 +581,9 @@ int ts_create(const ts_desc *d, ts_sim **out) {
                     dtr0[i] = 0.5f * (rho(x + 1, y, z) + r);   // raw: the kernels divide by rho
                     dtr1[i] = 0.5f * (rho(x, y + 1, z) + r);
                 }
+        });
     }
+    clk.mark("coefficients");
     // ---- attenuation ----
     s->zen_mode = !d->visco ? 0 : (d->g_p ? 2 : 1);
     std::vector<float> gp, gs;
@@ -512,15 +596,17 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         if (s->zen_mode == 2) {
             gp.assign(s->grid_elems, 0.f);
             gs.assign(s->grid_elems, 0.f);
-            for (int x = 0; x < nx; ++x)
+            parallel_rows(nx, [&](int x) {
                 for (int y = 0; y < ny; ++y)
                     for (int z = 0; z < nz; ++z) {
                         gp[s->at(x, y, z)] = d->g_p[href(x, y, z)];
                         gs[s->at(x, y, z)] = d->g_s[href(x, y, z)];
                     }
+            });
         }
     }
 
+    clk.mark("attenuation");
     // ---- coefficients to the device: a palette (3D, 32-bit offsets) or arrays ----
     float *dev = nullptr;
     bool palette = false;
@@ -538,7 +624,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
                                              &mus[0], pal2 ? &zeros : &mus[1], pal2 ? &zeros : &mus[2]};
         std::vector<uint16_t> idx;
         std::vector<ts::Pal3> table;
-        if (build_palette_3d(cols, idx, table)) {
+        if (build_palette_3d(cols, nx, idx, table)) {
             uint16_t *didx = nullptr;
             ts::Pal3 *dtab = nullptr;
             if ((rc = s->upload(&didx, idx)) || (rc = s->upload(&dtab, table))) return bail(rc);
@@ -580,6 +666,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         }
     }
 
+    clk.mark("coef upload");
     // ---- launch geometry ----
     s->n_blocks = s->dims == 2 ? ts::blocks_2d(p) : ts::blocks_3d(p);
     auto block_of = [&](int x, int y, int z) -> int {
@@ -602,30 +689,37 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         };
         std::vector<Cand> cands;
         std::map<int, int> col_of;
-        for (int x = 0; x < nx; ++x)
+        // the nodes whose map entry is not -1, found in parallel, then taken
+        // in the reference's scan order
+        std::vector<std::vector<int2>> marked(nx);
+        parallel_rows(nx, [&](int x) {
             for (int y = 0; y < ny; ++y)
-                for (int z = 0; z < nz; ++z) {
-                    const int idx = d->pos_sources[href(x, y, z)];
-                    if (idx == -1) continue;
-                    float r;
-                    if (s->family == TS_TAICHI2D) {
-                        const bool in_vy = x >= ord - 1 && x < nx - ord && y >= ord - 1 && y < ny - ord;
-                        if (!in_vy || idx < 0 || idx >= d->src_cols) continue;
-                        r = 0.25f * (rho(x, y + 1, 0) + rho(x, y, 0) + rho(x + 1, y + 1, 0) + rho(x + 1, y, 0));
-                    } else if (s->dims == 2) {
-                        r = 0.25f * (rho(x, y, 0) + rho(x + 1, y, 0) + rho(x + 1, y + 1, 0) + rho(x, y + 1, 0));
-                    } else {
-                        r = 0.5f * (rho(x, y + 1, z) + rho(x, y, z));
-                    }
-                    if (!(r > 0.f)) continue;
-                    const float scale = r;   // the kernels divide by rho
-                    if (!col_of.count(idx)) {
-                        const int c = (int)col_of.size();
-                        col_of[idx] = c;
-                        s->src_col_idx.push_back(idx);
-                    }
-                    cands.push_back({block_of(x, y, z), Source{s->at(x, y, z), col_of[idx], scale}});
+                for (int z = 0; z < nz; ++z)
+                    if (d->pos_sources[href(x, y, z)] != -1) marked[x].push_back(make_int2(y, z));
+        });
+        for (int x = 0; x < nx; ++x)
+            for (const int2 yz : marked[x]) {
+                const int y = yz.x, z = yz.y;
+                const int idx = d->pos_sources[href(x, y, z)];
+                float r;
+                if (s->family == TS_TAICHI2D) {
+                    const bool in_vy = x >= ord - 1 && x < nx - ord && y >= ord - 1 && y < ny - ord;
+                    if (!in_vy || idx < 0 || idx >= d->src_cols) continue;
+                    r = 0.25f * (rho(x, y + 1, 0) + rho(x, y, 0) + rho(x + 1, y + 1, 0) + rho(x + 1, y, 0));
+                } else if (s->dims == 2) {
+                    r = 0.25f * (rho(x, y, 0) + rho(x + 1, y, 0) + rho(x + 1, y + 1, 0) + rho(x, y + 1, 0));
+                } else {
+                    r = 0.5f * (rho(x, y + 1, z) + rho(x, y, z));
                 }
+                if (!(r > 0.f)) continue;
+                const float scale = r;   // the kernels divide by rho
+                if (!col_of.count(idx)) {
+                    const int c = (int)col_of.size();
+                    col_of[idx] = c;
+                    s->src_col_idx.push_back(idx);
+                }
+                cands.push_back({block_of(x, y, z), Source{s->at(x, y, z), col_of[idx], scale}});
+            }
         std::stable_sort(cands.begin(), cands.end(), [](const Cand &a, const Cand &b) { return a.blk < b.blk; });
         std::vector<Source> &list = src_list_h;
         std::vector<int> start(s->n_blocks + 1, 0);
@@ -646,6 +740,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         if ((rc = ts_set_sources(s, d->source_term))) return bail(rc);
     }
 
+    clk.mark("sources");
     // ---- receivers ----
     {
         std::vector<int> start(1, 0), first(d->n_rec, 0);
@@ -689,6 +784,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         p.traces = s->traces;
     }
 
+    clk.mark("receivers");
     // ---- stability bookkeeping ----
     p.v2_threshold = s->family == TS_TAICHI2D ? 1.0e38f : FLT_MAX;
     if ((rc = s->alloc(&s->block_max, s->n_blocks, true)) || (rc = s->alloc(&s->first_bad, 1, false)) ||
@@ -707,7 +803,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         int rows = 0, blocks = 0, threads = 0;
         size_t smem = 0;
         if (env && env[0] == '1' &&
-            ts::persist_2d_plan(s->family, ord, s->zen_mode, nx, ny, p.strip[1].width, prop.multiProcessorCount,
+            ts::persist_2d_plan(s->family, ord, s->zen_mode, nx, ny, p.strip[1].width, n_sms,
                                 &rows, &blocks, &threads, &smem)) {
             ts::PersistArgs &a = s->pa;
             constexpr int NH = 3;   // 2 ORD - 1 edge rows per side
@@ -794,11 +890,13 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         }
     }
 
+    clk.mark("paths");
     cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
     e = cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaEventCreate"));
     if ((rc = ts_reset(s))) return bail(rc);
+    clk.mark("reset");
     *out = s;
     return TS_OK;
 }

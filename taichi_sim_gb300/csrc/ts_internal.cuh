@@ -304,7 +304,10 @@ inline int block_of_2d(const StepParams &p, int x, int y) {
 // kernels) or p.tx (velocity kernel: 4 for order 2, 2 above, where 4 spills)
 // consecutive nodes along x (measured on the 256^3 three-mechanism case
 // against 1, 2 and 4).
-constexpr int kBX3 = 32, kBY3 = 8, kTX3S = 4;
+#ifndef TS_STRESS3D_TX
+#define TS_STRESS3D_TX 4
+#endif
+constexpr int kBX3 = 32, kBY3 = 8, kTX3S = TS_STRESS3D_TX;
 // The 8 warps of a block cover kZW3 consecutive 32-node runs along z (the
 // contiguous axis) times 8 / kZW3 rows along y (2 measured best of 1, 2, 4,
 // 8 on the 256^3 case: longer contiguous runs per block, y-neighbours still
