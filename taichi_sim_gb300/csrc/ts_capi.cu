@@ -33,6 +33,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -109,6 +110,78 @@ void parallel_rows(int n, const F &f) {
     for (auto &t : pool) t.join();
 }
 
+// Copies between pageable host memory and the device through a pinned
+// staging buffer shared by the process (allocated on first use, kept until
+// exit): pageable copies run at a few GB/s, pinned ones at the link's rate.
+// Two halves, so the DMA of one chunk overlaps the host copy of the other.
+// Small copies go directly.
+constexpr size_t kStageHalf = (size_t)16 << 20;
+constexpr size_t kStageMin = (size_t)4 << 20;
+std::mutex g_stage_mutex;
+char *g_stage = nullptr;
+cudaEvent_t g_stage_ev[2] = {nullptr, nullptr};
+
+cudaError_t stage_init() {
+    if (g_stage) return cudaSuccess;
+    cudaError_t e = cudaMallocHost(reinterpret_cast<void **>(&g_stage), 2 * kStageHalf);
+    if (e != cudaSuccess) {
+        g_stage = nullptr;
+        return e;
+    }
+    for (auto &ev : g_stage_ev)
+        if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return e;
+    return cudaSuccess;
+}
+
+// `rows` rows of `width` bytes: device rows `dpitch` bytes apart, host rows contiguous.
+cudaError_t stage_d2h(void *dst, const void *src, size_t width, size_t dpitch, size_t rows, cudaStream_t st) {
+    if (width * rows < kStageMin || width > kStageHalf) {
+        cudaError_t e = cudaMemcpy2DAsync(dst, width, src, dpitch, width, rows, cudaMemcpyDeviceToHost, st);
+        return e != cudaSuccess ? e : cudaStreamSynchronize(st);
+    }
+    std::lock_guard<std::mutex> lock(g_stage_mutex);
+    cudaError_t e = stage_init();
+    if (e != cudaSuccess) return e;
+    const size_t per = kStageHalf / width, chunks = (rows + per - 1) / per;
+    for (size_t c = 0; c <= chunks; ++c) {
+        if (c < chunks) {
+            const size_t r0 = c * per, n = std::min(per, rows - r0);
+            char *buf = g_stage + (c & 1) * kStageHalf;
+            if ((e = cudaMemcpy2DAsync(buf, width, static_cast<const char *>(src) + r0 * dpitch, dpitch, width, n,
+                                       cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+                (e = cudaEventRecord(g_stage_ev[c & 1], st)) != cudaSuccess)
+                return e;
+        }
+        if (c > 0) {   // the previous chunk: wait for its DMA, copy it out
+            const size_t q = c - 1, r0 = q * per, n = std::min(per, rows - r0);
+            if ((e = cudaEventSynchronize(g_stage_ev[q & 1])) != cudaSuccess) return e;
+            std::memcpy(static_cast<char *>(dst) + r0 * width, g_stage + (q & 1) * kStageHalf, n * width);
+        }
+    }
+    return cudaSuccess;
+}
+
+cudaError_t stage_h2d(void *dst, const void *src, size_t bytes, cudaStream_t st) {
+    if (bytes < kStageMin) {
+        cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+        return e != cudaSuccess ? e : cudaStreamSynchronize(st);
+    }
+    std::lock_guard<std::mutex> lock(g_stage_mutex);
+    cudaError_t e = stage_init();
+    if (e != cudaSuccess) return e;
+    const size_t chunks = (bytes + kStageHalf - 1) / kStageHalf;
+    for (size_t c = 0; c < chunks; ++c) {
+        const size_t off = c * kStageHalf, n = std::min(kStageHalf, bytes - off);
+        char *buf = g_stage + (c & 1) * kStageHalf;
+        if (c >= 2 && (e = cudaEventSynchronize(g_stage_ev[c & 1])) != cudaSuccess) return e;   // half free again
+        std::memcpy(buf, static_cast<const char *>(src) + off, n);
+        if ((e = cudaMemcpyAsync(static_cast<char *>(dst) + off, buf, n, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (e = cudaEventRecord(g_stage_ev[c & 1], st)) != cudaSuccess)
+            return e;
+    }
+    return cudaStreamSynchronize(st);
+}
+
 // Phase times of ts_create on stderr when TS_CREATE_TIMING=1 (diagnostic).
 struct PhaseClock {
     bool on = false;
@@ -181,7 +254,7 @@ struct ts_sim {
     int upload(T **ptr, const std::vector<T> &h) {
         int rc = alloc(ptr, h.size(), false);
         if (rc) return rc;
-        if (!h.empty()) TS_CUDA(cudaMemcpy(*ptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+        if (!h.empty()) TS_CUDA(stage_h2d(*ptr, h.data(), h.size() * sizeof(T), nullptr));
         h2d_bytes += (int64_t)(h.size() * sizeof(T));
         return TS_OK;
     }
@@ -323,13 +396,27 @@ void ts_destroy(ts_sim *s) {
 
 // Index of the first non-finite value of a float table, or -1.  (Exponent
 // bits all set: Inf or NaN; the loop vectorises.)
-static int64_t first_non_finite(const float *a, int64_t n) {
-    const uint32_t *u = reinterpret_cast<const uint32_t *>(a);
+static int64_t first_non_finite_seq(const uint32_t *u, int64_t n) {
     uint32_t any = 0;
     for (int64_t i = 0; i < n; ++i) any |= ((u[i] & 0x7f800000u) == 0x7f800000u);
     if (!any) return -1;
     for (int64_t i = 0; i < n; ++i)
         if ((u[i] & 0x7f800000u) == 0x7f800000u) return i;
+    return -1;
+}
+static int64_t first_non_finite(const float *a, int64_t n) {
+    const uint32_t *u = reinterpret_cast<const uint32_t *>(a);
+    constexpr int64_t kChunk = 1 << 20;   // large tables: chunks on parallel threads
+    if (n <= kChunk) return first_non_finite_seq(u, n);
+    const int chunks = (int)((n + kChunk - 1) / kChunk);
+    std::vector<int64_t> first(chunks, -1);
+    parallel_rows(chunks, [&](int c) {
+        const int64_t i0 = (int64_t)c * kChunk;
+        const int64_t i = first_non_finite_seq(u + i0, std::min(kChunk, n - i0));
+        if (i >= 0) first[c] = i0 + i;
+    });
+    for (int64_t i : first)
+        if (i >= 0) return i;
     return -1;
 }
 
@@ -642,7 +729,10 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         for (int c = 0; c < 2; ++c) {
             const std::vector<float> &rh = c == 0 ? dtr0 : dtr1;
             std::vector<float2> w(rh.size());
-            for (size_t i = 0; i < rh.size(); ++i) w[i] = dt_over_rho(d->dt, rh[i]);
+            const size_t per = (rh.size() + nx - 1) / nx;
+            parallel_rows(nx, [&](int x) {
+                for (size_t i = x * per; i < std::min(rh.size(), (x + 1) * per); ++i) w[i] = dt_over_rho(d->dt, rh[i]);
+            });
             float2 *dw = nullptr;
             if ((rc = s->upload(&dw, w))) return bail(rc);
             p.dtw[c] = dw;
@@ -1120,7 +1210,8 @@ int ts_read(ts_sim *s, int32_t what, void *dst, size_t bytes) {
     if (what == TS_TRACES) {
         const size_t need = (size_t)s->n_rows * s->n_rec * sizeof(float);
         if (bytes < need) return fail(TS_E_ARG, "destination too small for the traces");
-        if (need) TS_CUDA(cudaMemcpy(dst, s->traces, need, cudaMemcpyDeviceToHost));
+        if (need) TS_CUDA(stage_d2h(dst, s->traces, (size_t)s->n_rec * sizeof(float), (size_t)s->n_rec * sizeof(float),
+                                    (size_t)s->n_rows, s->stream));
         s->d2h_bytes += (int64_t)need;
         return TS_OK;
     }
@@ -1129,8 +1220,7 @@ int ts_read(ts_sim *s, int32_t what, void *dst, size_t bytes) {
     const size_t rows = (size_t)s->nx * (s->dims == 2 ? 1 : s->ny);
     const size_t need = rows * last * sizeof(float);
     if (bytes < need) return fail(TS_E_ARG, "destination too small for the field");
-    TS_CUDA(cudaMemcpy2D(dst, last * sizeof(float), s->field[what], s->pitch * sizeof(float), last * sizeof(float),
-                         rows, cudaMemcpyDeviceToHost));
+    TS_CUDA(stage_d2h(dst, s->field[what], last * sizeof(float), s->pitch * sizeof(float), rows, s->stream));
     s->d2h_bytes += (int64_t)need;
     return TS_OK;
 }
