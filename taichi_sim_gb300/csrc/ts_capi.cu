@@ -37,6 +37,7 @@
 #include <string>
 #include <thread>
 #include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include "../../include/taichi_sim_gb300.h"
@@ -108,6 +109,35 @@ void parallel_rows(int n, const F &f) {
             for (int x; (x = next.fetch_add(1)) < n;) f(x);
         });
     for (auto &t : pool) t.join();
+}
+
+// Host tables of the size of a grid, filled by parallel loops: elements
+// are left uninitialised by the vector (std::allocator would zero 67 MB per
+// 256^3 table on one thread) and written by fill() or by the loops.
+template <typename T>
+struct NoInitAlloc : std::allocator<T> {
+    template <typename U>
+    struct rebind {
+        using other = NoInitAlloc<U>;
+    };
+    NoInitAlloc() = default;
+    template <typename U>
+    NoInitAlloc(const NoInitAlloc<U> &) {}
+    template <typename U>
+    void construct(U *) noexcept {}
+    template <typename U, typename... Args>
+    void construct(U *q, Args &&...args) {
+        ::new (static_cast<void *>(q)) U(std::forward<Args>(args)...);
+    }
+};
+using hvec = std::vector<float, NoInitAlloc<float>>;
+
+hvec filled(size_t n, float v) {
+    hvec out(n);
+    constexpr size_t kPart = (size_t)1 << 20;
+    const int parts = (int)((n + kPart - 1) / kPart);
+    parallel_rows(parts, [&](int q) { std::fill(out.begin() + q * kPart, out.begin() + std::min(n, (q + 1) * kPart), v); });
+    return out;
 }
 
 // Copies between pageable host memory and the device through a pinned
@@ -250,8 +280,8 @@ struct ts_sim {
         return TS_OK;
     }
 
-    template <typename T>
-    int upload(T **ptr, const std::vector<T> &h) {
+    template <typename T, typename A>
+    int upload(T **ptr, const std::vector<T, A> &h) {
         int rc = alloc(ptr, h.size(), false);
         if (rc) return rc;
         if (!h.empty()) TS_CUDA(stage_h2d(*ptr, h.data(), h.size() * sizeof(T), nullptr));
@@ -287,7 +317,7 @@ struct PalHash {
     }
 };
 
-bool build_palette_3d(const std::vector<float> *const (&c)[7], int rows, std::vector<uint16_t> &idx,
+bool build_palette_3d(const hvec *const (&c)[7], int rows, std::vector<uint16_t> &idx,
                       std::vector<ts::Pal3> &table) {
     const size_t n = c[0]->size();
     const size_t per = (n + rows - 1) / rows;
@@ -561,8 +591,8 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         p.xy_sweep_3d = !(xy && xy[0] == '0');
         const char *pair = getenv("TS_3D_STRESS_PAIR");
         p.stress_pair_3d = !(pair && pair[0] == '0');
-        const char *pf = getenv("TS_3D_PREFETCH");   // "0": no L2 prefetch of a thread's later x nodes
-        p.prefetch_3d = !(pf && pf[0] == '0');
+        const char *pf = getenv("TS_3D_PREFETCH");   // "0": no L2 prefetch of a thread's later x nodes; "2": early
+        p.prefetch_3d = !pf ? 1 : pf[0] == '0' ? 0 : pf[0] == '2' ? 2 : 1;
     }
     p.nx = nx;
     p.ny = ny;
@@ -627,11 +657,11 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     clk.mark("fields");
     // ---- per-node coefficients (host, reference averaging, folded with dt) ----
     const float dt = d->dt;
-    std::vector<float> lam(s->grid_elems, 0.f), mu(s->grid_elems, 0.f), dtr0(s->grid_elems, 0.f),
-        dtr1(s->grid_elems, 0.f);
-    std::vector<float> mus[3];
+    const size_t ng = (size_t)s->grid_elems;
+    hvec lam = filled(ng, 0.f), mu = filled(ng, 0.f), dtr0 = filled(ng, 0.f), dtr1 = filled(ng, 0.f);
+    hvec mus[3];
     const int n_shear = s->dims == 2 ? 1 : 3;
-    for (int k = 0; k < n_shear; ++k) mus[k].assign(s->grid_elems, 0.f);
+    for (int k = 0; k < n_shear; ++k) mus[k] = filled(ng, 0.f);
     if (s->dims == 2) {
         // normal node x-averaged (mu zero where either cs is zero), shear
         // node y-averaged, vy node 4-point averaged (ts_prep.h)
@@ -673,7 +703,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     clk.mark("coefficients");
     // ---- attenuation ----
     s->zen_mode = !d->visco ? 0 : (d->g_p ? 2 : 1);
-    std::vector<float> gp, gs;
+    hvec gp, gs;
     if (d->visco) {
         const int L = d->n_sls;
         p.zen = ts::zener_constants(d);
@@ -681,8 +711,8 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         for (int m = 0; m < nmem; ++m)
             if ((rc = s->alloc(&p.r[m], s->grid_elems * L, true))) return bail(rc);
         if (s->zen_mode == 2) {
-            gp.assign(s->grid_elems, 0.f);
-            gs.assign(s->grid_elems, 0.f);
+            gp = filled(ng, 0.f);
+            gs = filled(ng, 0.f);
             parallel_rows(nx, [&](int x) {
                 for (int y = 0; y < ny; ++y)
                     for (int z = 0; z < nz; ++z) {
@@ -705,9 +735,9 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     const bool pal2 = s->dims == 2 && s->family == TS_WGSL2D && ord == 2 && !(pal2_env && pal2_env[0] == '0') &&
                       !(pers_env && pers_env[0] == '1');
     if (pal3 || pal2) {
-        const std::vector<float> ones(gp.empty() ? s->grid_elems : 0, 1.f);
-        const std::vector<float> zeros(pal2 ? s->grid_elems : 0, 0.f);
-        const std::vector<float> *cols[7] = {&lam, &mu, gp.empty() ? &ones : &gp, gs.empty() ? &ones : &gs,
+        const hvec ones = filled(gp.empty() ? ng : 0, 1.f);
+        const hvec zeros = filled(pal2 ? ng : 0, 0.f);
+        const hvec *cols[7] = {&lam, &mu, gp.empty() ? &ones : &gp, gs.empty() ? &ones : &gs,
                                              &mus[0], pal2 ? &zeros : &mus[1], pal2 ? &zeros : &mus[2]};
         std::vector<uint16_t> idx;
         std::vector<ts::Pal3> table;
@@ -727,7 +757,7 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         p.dtr[1] = dev;
     } else {   // dt / rho as (hi, lo) pairs
         for (int c = 0; c < 2; ++c) {
-            const std::vector<float> &rh = c == 0 ? dtr0 : dtr1;
+            const hvec &rh = c == 0 ? dtr0 : dtr1;
             std::vector<float2> w(rh.size());
             const size_t per = (rh.size() + nx - 1) / nx;
             parallel_rows(nx, [&](int x) {

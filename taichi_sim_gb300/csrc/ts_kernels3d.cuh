@@ -158,8 +158,29 @@ __device__ __forceinline__ void normal3d_body(const StepParams &p, int bz) {
     const int sy = strip_index(p.strip[1], y), sz = strip_index(p.strip[2], z);
     const int n_mech = NS == 3 ? 3 : p.zen.n;
     constexpr int R = NS > 0 ? NS : 1;
+    // L2 prefetch of the nodes' stresses and memory variables (last written
+    // two launches back): mode 1 the later nodes after the wait, mode 2 every
+    // node before it, overlapping the previous launch's drain
+    if (p.prefetch_3d == 2 && yz_n) {
+#pragma unroll
+        for (int t = 0; t < kTX3S; ++t) {
+            const int x = x0 + t;
+            if (x >= ORD - 1 && x < p.nx - ORD) {
+                const I i = (I)x * X + yz;
+                prefetch_l2(p.s[0] + i);
+                prefetch_l2(p.s[1] + i);
+                prefetch_l2(p.s[2] + i);
+                if (ZM != 0)
+                    for (int l = 0; l < n_mech; ++l) {
+                        prefetch_l2(p.r[0] + l * G + i);
+                        prefetch_l2(p.r[1] + l * G + i);
+                        prefetch_l2(p.r[2] + l * G + i);
+                    }
+            }
+        }
+    }
     pdl_wait();
-    if (p.prefetch_3d && yz_n) {   // the later nodes' stresses and memory variables
+    if (p.prefetch_3d == 1 && yz_n) {   // the later nodes' stresses and memory variables
 #pragma unroll
         for (int t = 1; t < kTX3S; ++t) {
             const int x = x0 + t;
@@ -296,8 +317,26 @@ __device__ __forceinline__ void shear3d_body(const StepParams &p, int bz) {
     const int sy = strip_index(p.strip[1], y), sz = strip_index(p.strip[2], z);
     const int n_mech = NS == 3 ? 3 : p.zen.n;
     constexpr int R = NS > 0 ? NS : 1;
+    if (p.prefetch_3d == 2 && yz_s) {   // as in normal3d_body
+#pragma unroll
+        for (int t = 0; t < kTX3S; ++t) {
+            const int x = x0 + t;
+            if (x >= ORD - 1 && x < p.nx - ORD + 1) {
+                const I i = (I)x * X + yz;
+                prefetch_l2(p.s[3] + i);
+                prefetch_l2(p.s[4] + i);
+                prefetch_l2(p.s[5] + i);
+                if (ZM != 0)
+                    for (int l = 0; l < n_mech; ++l) {
+                        prefetch_l2(p.r[3] + l * G + i);
+                        prefetch_l2(p.r[4] + l * G + i);
+                        prefetch_l2(p.r[5] + l * G + i);
+                    }
+            }
+        }
+    }
     pdl_wait();
-    if (p.prefetch_3d && yz_s) {   // the later nodes' stresses and memory variables
+    if (p.prefetch_3d == 1 && yz_s) {   // the later nodes' stresses and memory variables
 #pragma unroll
         for (int t = 1; t < kTX3S; ++t) {
             const int x = x0 + t;
@@ -504,10 +543,9 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
     // general one
     const bool fast = interior_warp<ORD, TX>(p, y, z, x0, sy, sz) && q0 == q1;
     const bool fast_xy = !fast && q0 == q1 && p.xy_sweep_3d && xy_interior_warp<ORD, TX>(p, y, z, x0, sy);
-    pdl_wait();
-    if (p.prefetch_3d && col) {   // the later nodes' velocities, dt / rho and stresses
+    if (p.prefetch_3d == 2 && col) {   // velocities (last written two launches back) and dt / rho, every node
 #pragma unroll
-        for (int t = 1; t < TX; ++t) {
+        for (int t = 0; t < TX; ++t) {
             const int x = x0 + t;
             if (x < p.nx) {
                 const I i = (I)x * X + yz;
@@ -516,6 +554,23 @@ __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(c
                 prefetch_l2(p.v[2] + i);
                 prefetch_l2(p.dtw[0] + i);
                 prefetch_l2(p.dtw[1] + i);
+            }
+        }
+    }
+    pdl_wait();
+    if (p.prefetch_3d && col) {   // the later nodes' velocities, dt / rho (mode 1) and stresses
+#pragma unroll
+        for (int t = 1; t < TX; ++t) {
+            const int x = x0 + t;
+            if (x < p.nx) {
+                const I i = (I)x * X + yz;
+                if (p.prefetch_3d == 1) {
+                    prefetch_l2(p.v[0] + i);
+                    prefetch_l2(p.v[1] + i);
+                    prefetch_l2(p.v[2] + i);
+                    prefetch_l2(p.dtw[0] + i);
+                    prefetch_l2(p.dtw[1] + i);
+                }
 #pragma unroll
                 for (int f = 0; f < 6; ++f) prefetch_l2(p.s[f] + i);
             }

@@ -4,8 +4,6 @@
 #include <cuda_runtime.h>
 #include "ts_kernels2d.cuh"
 
-#include <cstdlib>
-
 namespace ts {
 namespace {
 
@@ -19,17 +17,6 @@ void launch_tx(const StepParams &p, int zen_mode, int j, cudaStream_t st, int pa
     dim3 grid((p.ny + kBX2 - 1) / kBX2, (p.nx + kBY2 * TX - 1) / (kBY2 * TX));
     const bool three = p.zen.n == 3;
     if (p.family == kTaichi) {
-        static const int minb = getenv("TS_TAICHI_MINB") ? atoi(getenv("TS_TAICHI_MINB")) : 0;
-        if (ORD == 2 && TX == 1 && minb == 5) {
-            if (parts & 1) launch_pdl(k_stress2d<ORD, 0, 0, 0, TX, false, 6>, grid, block, st, p);
-            if (parts & 2) launch_pdl(k_velocity2d<ORD, 0, TX, false, 5>, grid, block, st, p, j);
-            return;
-        }
-        if (ORD == 2 && TX == 1 && minb == 6) {
-            if (parts & 1) launch_pdl(k_stress2d<ORD, 0, 0, 0, TX, false, 8>, grid, block, st, p);
-            if (parts & 2) launch_pdl(k_velocity2d<ORD, 0, TX, false, 6>, grid, block, st, p, j);
-            return;
-        }
         if (parts & 1) launch_pdl(k_stress2d<ORD, 0, 0, 0, TX>, grid, block, st, p);
         if (parts & 2) launch_pdl(k_velocity2d<ORD, 0, TX>, grid, block, st, p, j);
         return;
