@@ -54,8 +54,7 @@
 namespace ts {
 namespace {
 
-constexpr int kTX = 2;     // nodes per thread along x of the forward kernels
-constexpr int kAdjTx = 1;  // and of the adjoint kernels
+constexpr int kAdjTx = 1;  // nodes per thread along x of the adjoint kernels
 
 // Everything the adjoint kernels read, passed by value.
 struct AdjState {
@@ -575,7 +574,8 @@ int ts_adj_create(const ts_desc *d, int32_t checkpoint_every, ts_adj **out) {
     StepParams &sp = a->sp;
     AdjState &as = a->as;
     sp.family = TS_WGSL2D;
-    sp.tx = kTX;
+    // the forward kernels: the stepper's choice at order 2 (one or two), two above
+    sp.tx = d->ord == 2 ? std::min(2, nodes_per_thread_2d((int64_t)d->nx * d->ny)) : 2;
     sp.nx = a->nx;
     sp.ny = a->ny;
     sp.nz = 1;
@@ -678,7 +678,7 @@ int ts_adj_create(const ts_desc *d, int32_t checkpoint_every, ts_adj **out) {
         };
         int *dstart = nullptr, *astart = nullptr;
         Source *asrc = nullptr;
-        if ((rc = binned(kTX, a->n_blocks, &a->src, &dstart)) || (rc = binned(kAdjTx, n_blocks_adj, &asrc, &astart)))
+        if ((rc = binned(sp.tx, a->n_blocks, &a->src, &dstart)) || (rc = binned(kAdjTx, n_blocks_adj, &asrc, &astart)))
             return bail(rc);
         a->n_src = (int)nodes.size();
         sp.src = a->src;

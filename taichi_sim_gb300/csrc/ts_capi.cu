@@ -297,6 +297,14 @@ struct ts_sim {
 
 using ts::Axis;
 
+int ts::nodes_per_thread_2d(int64_t cells) {
+    if (const char *env = getenv("TS_2D_NODES_PER_THREAD")) {
+        const int v = atoi(env);
+        if (v == 1 || v == 2 || v == 4) return v;
+    }
+    return cells >= 800000 ? 2 : 1;
+}
+
 // Coefficient palette of a 3D model (and of the 2D order-2 WGSL stepper):
 // the distinct tuples of the stress kernels' per-node coefficients (compared
 // bit for bit) and each node's 16-bit index into them, numbered in the order
@@ -577,22 +585,15 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     // index/region/bookkeeping instructions per node as that allows
     {
         const int64_t cells = (int64_t)d->nx * d->ny;
-        // measured on GB300: 2 nodes per thread is fastest from ~200k nodes
-        // (1024^2 viscoelastic, 512^2 elastic); 4 loses occupancy to registers
-        // 2D: one node per thread up to 768^2 grids, two from 1024^2
-        // (measured: 512^2 elastic 26.7 against 22.6 Gcell/s, 640^2 visco
-        // 33.9 / 32.1, 768^2 38.6 / 38.2, 1024^2 43.6 / 47.4)
-        p.tx = s->dims == 3 ? ts::velocity_tx_3d(d->ord) : (cells >= 800000 ? 2 : 1);
-        if (const char *env = getenv("TS_2D_NODES_PER_THREAD")) {
-            const int v = atoi(env);
-            if (v == 1 || v == 2 || v == 4) p.tx = v;
-        }
+        p.tx = s->dims == 3 ? ts::velocity_tx_3d(d->ord) : ts::nodes_per_thread_2d(cells);
         const char *xy = getenv("TS_3D_XY_SWEEP");
         p.xy_sweep_3d = !(xy && xy[0] == '0');
         const char *pair = getenv("TS_3D_STRESS_PAIR");
         p.stress_pair_3d = !(pair && pair[0] == '0');
-        const char *pf = getenv("TS_3D_PREFETCH");   // "0": no L2 prefetch of a thread's later x nodes; "2": early
-        p.prefetch_3d = !pf ? 1 : pf[0] == '0' ? 0 : pf[0] == '2' ? 2 : 1;
+        // L2 prefetch in the 3D kernels: 2 (default) the state last written
+        // two launches back before the wait, 1 after it, 0 none
+        const char *pf = getenv("TS_3D_PREFETCH");
+        p.prefetch_3d = !pf ? 2 : pf[0] == '0' ? 0 : pf[0] == '1' ? 1 : 2;
     }
     p.nx = nx;
     p.ny = ny;

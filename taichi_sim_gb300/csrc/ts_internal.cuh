@@ -69,7 +69,8 @@ struct StepParams {
     int tx;                // 2D: nodes each thread updates along x (1, 2 or 4)
     int xy_sweep_3d;       // 3D velocity kernel: warps interior in x and y take the x-y sweep
     int stress_pair_3d;    // 3D: normal and shear stress updates in one launch (k_stress3d)
-    int prefetch_3d;       // 3D: the kernels prefetch the state of a thread's later x nodes into L2 first
+    int prefetch_3d;       // 3D L2 prefetch of a thread's nodes: 2 before the wait (state last written two
+                           // launches back), then the rest; 1 the later nodes after the wait; 0 none
     int nx, ny, nz;        // nz = 1 in 2D
     int pitch;             // padded last-axis length (floats)
     int64_t plane;         // ny * pitch (3D x stride); 2D: pitch
@@ -300,6 +301,13 @@ inline int block_of_2d(const StepParams &p, int x, int y) {
     const int gx = (p.ny + kBX2 - 1) / kBX2;
     return (x / (kBY2 * p.tx)) * gx + y / kBX2;
 }
+// 2D nodes per thread along x: one up to 768^2 grids (the L2-resident
+// small grids want more warps in flight), two from 1024^2 (fewer index and
+// bookkeeping instructions per node); TS_2D_NODES_PER_THREAD = 1, 2 or 4
+// overrides it.  Measured: elastic 512^2 26.7 against 22.6 Gcell/s,
+// viscoelastic 640^2 33.9 / 32.1, 768^2 38.6 / 38.2, 1024^2 43.6 / 47.4.
+int nodes_per_thread_2d(int64_t cells);
+
 // 3D kernels: blocks of 32 (z) x 8 (y) threads, each updating kTX3S (stress
 // kernels) or p.tx (velocity kernel: 4 for order 2, 2 above, where 4 spills)
 // consecutive nodes along x (measured on the 256^3 three-mechanism case

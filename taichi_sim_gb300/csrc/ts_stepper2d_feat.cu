@@ -1,5 +1,5 @@
 // The 2D step kernels of the adjoint's forward pass (family TS_WGSL2D with
-// the coefficients folded with dt, kWgslFolded; two nodes per thread):
+// the coefficients folded with dt, kWgslFolded; p.tx nodes per thread):
 // with and without the record of the per-node quantities the adjoint
 // multiplies by, in their own translation unit so that they compile in
 // parallel with the stepper's.
@@ -9,9 +9,8 @@
 namespace ts {
 namespace {
 
-template <int ORD, int MINB, int MINB_Q>
+template <int ORD, int MINB, int MINB_Q, int TX>
 void launch_feat_mb(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
-    constexpr int TX = 2;
     const dim3 block(kBX2, kBY2), grid((p.ny + kBX2 - 1) / kBX2, (p.nx + kBY2 * TX - 1) / (kBY2 * TX));
     const bool three = p.zen.n == 3;
     if (zen_mode == 0) launch_pdl(k_stress2d<ORD, kWgslFolded, 0, 0, TX, true, MINB>, grid, block, st, p);
@@ -23,9 +22,9 @@ void launch_feat_mb(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
 }
 
 // the same step without the record (the forward's unrecorded segments)
-template <int ORD>
-void launch_folded(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
-    constexpr int TX = 2, MB = ORD == 2 ? 4 : 0;
+template <int ORD, int TX>
+void launch_folded_tx(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
+    constexpr int MB = ORD == 2 ? 4 : 0;
     const dim3 block(kBX2, kBY2), grid((p.ny + kBX2 - 1) / kBX2, (p.nx + kBY2 * TX - 1) / (kBY2 * TX));
     const bool three = p.zen.n == 3;
     if (zen_mode == 0) launch_pdl(k_stress2d<ORD, kWgslFolded, 0, 0, TX>, grid, block, st, p);
@@ -34,6 +33,13 @@ void launch_folded(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
     else if (three) launch_pdl(k_stress2d<ORD, kWgslFolded, 2, 3, TX, false, MB>, grid, block, st, p);
     else launch_pdl(k_stress2d<ORD, kWgslFolded, 2, kMaxSls, TX>, grid, block, st, p);
     launch_pdl(k_velocity2d<ORD, kWgslFolded, TX, false, MB>, grid, block, st, p, j);
+}
+
+// Nodes per thread (p.tx): 1 or 2 at order 2 (adjoint_nodes_per_thread), 2 above.
+template <int ORD>
+void launch_folded(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
+    if (ORD == 2 && p.tx == 1) launch_folded_tx<ORD, 1>(p, zen_mode, j, st);
+    else launch_folded_tx<ORD, 2>(p, zen_mode, j, st);
 }
 
 // Register budget: order 2 takes 4 resident blocks per SM (64 registers:
@@ -45,7 +51,8 @@ template <int ORD>
 void launch_feat(const StepParams &p, int zen_mode, int j, cudaStream_t st) {
     constexpr int mb = ORD == 2 ? 4 : (ORD <= 4 ? 3 : 0);
     constexpr int mbq = ORD <= 4 ? 3 : 0;
-    launch_feat_mb<ORD, mb, mbq>(p, zen_mode, j, st);
+    if (ORD == 2 && p.tx == 1) launch_feat_mb<ORD, mb, mbq, 1>(p, zen_mode, j, st);
+    else launch_feat_mb<ORD, mb, mbq, 2>(p, zen_mode, j, st);
 }
 
 }  // namespace
