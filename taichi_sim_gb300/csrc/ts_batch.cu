@@ -32,6 +32,7 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <cstdlib>
 #include <map>
 #include <string>
 #include <type_traits>
@@ -94,6 +95,7 @@ struct BParams {
     int *first_bad;
     const int *step_base;
     int rec_work;
+    int prefetch;   // L2 prefetch, before the wait, of each thread's own state (last written two launches back)
 };
 
 // b psi + a d, then d / k + psi (the shader's division, rounded as one)
@@ -233,6 +235,22 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocks<CY, SPT>::v)) k_bstress(co
     float *__restrict__ r0 = h.r[0];
     float *__restrict__ r1 = h.r[1];
     float *__restrict__ r2 = h.r[2];
+    if (p.prefetch) {   // stresses and memory variables, written by this kernel's previous launch
+#pragma unroll
+        for (int t = 0; t < TX; ++t)
+            if (at.x0 + t < nx) {
+                const int i = at.i0 + t * X;
+                prefetch_l2(s0 + i);
+                prefetch_l2(s1 + i);
+                prefetch_l2(s2 + i);
+                if (ZM != 0)
+                    for (int l = 0; l < n_mech; ++l) {
+                        prefetch_l2(r0 + l * G + i);
+                        prefetch_l2(r1 + l * G + i);
+                        prefetch_l2(r2 + l * G + i);
+                    }
+            }
+    }
     pdl_wait();
     // Interior chunks (every node of the thread inside both update regions and
     // outside the CPML strips, window rows inside the grid) take a sweep with
@@ -428,6 +446,17 @@ __global__ void __launch_bounds__(32 * CY, (MinBlocksV<CY>::v)) k_bvelocity(cons
     const float2 *__restrict__ dtw1 = h.dtw1;
     float *__restrict__ v0 = h.v[0];
     float *__restrict__ v1 = h.v[1];
+    if (p.prefetch && at.live) {   // velocities (this kernel's previous launch) and dt / rho
+#pragma unroll
+        for (int t = 0; t < TX; ++t)
+            if (at.x0 + t < nx) {
+                const int i = at.i0 + t * X, cell = at.cell0 + t * ny;
+                prefetch_l2(v0 + i);
+                prefetch_l2(v1 + i);
+                prefetch_l2(dtw0 + cell);
+                prefetch_l2(dtw1 + cell);
+            }
+    }
     pdl_wait();
     const int k = *p.step_base + j;
     // source nodes among this thread's TX nodes: one bin per (x-chunk, y-block)
@@ -975,6 +1004,8 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
     p.rows = b->rows;
     p.v2_threshold = FLT_MAX;
     p.rec_work = rec0;
+    const char *pf = getenv("TS_BATCH_PREFETCH");   // "1": prefetch each thread's own state before the wait
+    p.prefetch = pf && pf[0] == '1';
     if ((rc = b->alloc(&p.block_max, b->n_blocks[1], true))) return bail(rc);
     int *fb = nullptr, *sb = nullptr;
     if ((rc = b->alloc(&fb, 1, false)) || (rc = b->alloc(&sb, 1, false))) return bail(rc);
