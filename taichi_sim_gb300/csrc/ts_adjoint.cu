@@ -40,7 +40,6 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <cstdlib>
 #include <cfloat>
 #include <cstring>
 #include <string>
@@ -85,7 +84,6 @@ struct AdjState {
     // velocity nodes: dsxx/dx~, dsxy/dy~ (vx), dsxy/dx~, dsyy/dy~ (vy)
     float *ds[4];
     float *gL, *gM, *gMs, *gBx, *gBy;
-    int prefetch;   // the velocity kernel prefetches the step's record of its nodes into L2 before the wait
 };
 
 // adjoint of cpml(): given the adjoint of d~ and the carried adjoint of p',
@@ -118,15 +116,6 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_adj_velocity(const AdjStat
     // warps wholly in the interior (no source node in the block) sweep
     // without per-node region, strip, bounds or source tests
     const bool fast = interior_warp<ORD, TX>(a, y, x0, sy) && q0 == q1;
-    if (a.prefetch && live_col) {   // the record of this step (both kernels' features), written by the forward
-#pragma unroll
-        for (int t = 0; t < TX; ++t)
-            if (x0 + t < nx) {
-                const int64_t i = (int64_t)(x0 + t) * P + y;
-#pragma unroll
-                for (int f = 0; f < kFeat; ++f) prefetch_l2(rec + f * G + i);
-            }
-    }
     pdl_wait();
     auto sweep = [&](auto fast_tag) {
         constexpr bool FAST = decltype(fast_tag)::value;
@@ -594,8 +583,6 @@ int ts_adj_create(const ts_desc *d, int32_t checkpoint_every, ts_adj **out) {
     sp.plane = a->P;
     sp.grid_elems = G;
     as.nx = a->nx;
-    const char *pf = getenv("TS_ADJ_PREFETCH");   // "1": L2 prefetch of each step's record before the wait
-    as.prefetch = pf && pf[0] == '1';
     as.ny = a->ny;
     as.P = a->P;
     as.G = G;
