@@ -592,8 +592,6 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         p.stress_pair_3d = !(pair && pair[0] == '0');
         // L2 prefetch in the 3D kernels: 2 (default) the state last written
         // two launches back before the wait, 1 after it, 0 none
-        const char *pf2 = getenv("TS_2D_PREFETCH");   // "1": 2D L2 prefetch before the wait (experiment)
-        p.prefetch_2d = pf2 && pf2[0] == '1';
         const char *pf = getenv("TS_3D_PREFETCH");
         p.prefetch_3d = !pf ? 2 : pf[0] == '0' ? 0 : pf[0] == '1' ? 1 : 2;
     }

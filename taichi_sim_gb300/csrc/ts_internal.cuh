@@ -69,7 +69,6 @@ struct StepParams {
     int tx;                // 2D: nodes each thread updates along x (1, 2 or 4)
     int xy_sweep_3d;       // 3D velocity kernel: warps interior in x and y take the x-y sweep
     int stress_pair_3d;    // 3D: normal and shear stress updates in one launch (k_stress3d)
-    int prefetch_2d;       // 2D stepper: L2 prefetch of the nodes' own state before the wait
     int prefetch_3d;       // 3D L2 prefetch of a thread's nodes: 2 before the wait (state last written two
                            // launches back), then the rest; 1 the later nodes after the wait; 0 none
     int nx, ny, nz;        // nz = 1 in 2D

@@ -137,22 +137,6 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
     constexpr int R = NS > 0 ? NS : 1;
     const bool yn = y >= ORD && y < p.ny - ORD + 1;   // normal-stress rows in y
     const bool ys = y >= ORD - 1 && y < p.ny - ORD;   // shear-stress rows in y
-    if (p.prefetch_2d) {   // the nodes' stresses and memory variables (written two launches back)
-#pragma unroll
-        for (int t = 0; t < TX; ++t)
-            if (x0 + t < nx) {
-                const int64_t i = (int64_t)(x0 + t) * P + y;
-                prefetch_l2(p.s[0] + i);
-                prefetch_l2(p.s[1] + i);
-                prefetch_l2(p.s[3] + i);
-                if (ZM != 0)
-                    for (int l = 0; l < n_mech; ++l) {
-                        prefetch_l2(p.r[0] + l * p.grid_elems + i);
-                        prefetch_l2(p.r[1] + l * p.grid_elems + i);
-                        prefetch_l2(p.r[2] + l * p.grid_elems + i);
-                    }
-            }
-    }
     pdl_wait();
     auto sweep = [&](auto fast_tag) {
         constexpr bool FAST = decltype(fast_tag)::value;
@@ -362,17 +346,6 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
     const bool yvx = FAM == kTaichi ? (y >= ORD && y < p.ny - ORD + 1) : (yvy && y >= ORD);
     const int q0 = __ldg(p.src_block_start + blk), q1 = __ldg(p.src_block_start + blk + 1);
     const bool fast = interior_warp<ORD, TX>(p, y, x0, sy) && q0 == q1;   // no source node in the block
-    if (p.prefetch_2d && live_col) {   // the nodes' velocities (written two launches back) and densities
-#pragma unroll
-        for (int t = 0; t < TX; ++t)
-            if (x0 + t < nx) {
-                const int64_t i = (int64_t)(x0 + t) * P + y;
-                prefetch_l2(p.v[0] + i);
-                prefetch_l2(p.v[1] + i);
-                prefetch_l2(p.dtr[0] + i);
-                prefetch_l2(p.dtr[1] + i);
-            }
-    }
     pdl_wait();
     const int k = *p.step_base + j;
     unsigned vmax = 0u;  // max |v|^2 as float bits (v2 >= 0 or NaN: NaN ranks highest)
