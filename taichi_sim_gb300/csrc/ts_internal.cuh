@@ -69,6 +69,7 @@ struct StepParams {
     int tx;                // 2D: nodes each thread updates along x (1, 2 or 4)
     int xy_sweep_3d;       // 3D velocity kernel: warps interior in x and y take the x-y sweep
     int stress_pair_3d;    // 3D: normal and shear stress updates in one launch (k_stress3d)
+    int snake_3d;          // 3D velocity kernel: x-chunks in reverse launch order
     int prefetch_3d;       // 3D L2 prefetch of a thread's nodes: 2 before the wait (state last written two
                            // launches back), then the rest; 1 the later nodes after the wait; 0 none
     int nx, ny, nz;        // nz = 1 in 2D
@@ -328,8 +329,9 @@ constexpr int velocity_tx_3d(int ord) { return ord == 2 ? TS_VELOCITY3D_TX : 2; 
 
 // Flat index of the 3D velocity block that updates node (x, y, z).
 inline int block_of_3d(const StepParams &p, int x, int y, int z) {
-    const int gx = (p.nz + kZB3 - 1) / kZB3, gy = (p.ny + kYB3 - 1) / kYB3;
-    return ((x / p.tx) * gy + y / kYB3) * gx + z / kZB3;
+    const int gx = (p.nz + kZB3 - 1) / kZB3, gy = (p.ny + kYB3 - 1) / kYB3, nch = (p.nx + p.tx - 1) / p.tx;
+    const int bz = p.snake_3d ? nch - 1 - x / p.tx : x / p.tx;   // launch order of the x-chunk
+    return (bz * gy + y / kYB3) * gx + z / kZB3;
 }
 
 }  // namespace ts

@@ -523,7 +523,9 @@ template <int ORD, typename I, int TX>
 __global__ void __launch_bounds__(kBX3 *kBY3, kVelocityMinBlocks) k_velocity3d(const StepParams p, const int j) {
     const int z = blockIdx.x * kZB3 + (threadIdx.y % kZW3) * kBX3 + threadIdx.x;
     const int y = blockIdx.y * kYB3 + threadIdx.y / kZW3;
-    const int x0 = blockIdx.z * TX;
+    // x-chunks in reverse launch order with snake_3d: the stress launch before
+    // wrote the high chunks last, so they are the ones still in L2
+    const int x0 = (p.snake_3d ? gridDim.z - 1 - blockIdx.z : blockIdx.z) * TX;
     const int tid = threadIdx.y * kBX3 + threadIdx.x;
     const int blk = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
     const bool col = y < p.ny && z < p.nz;
