@@ -596,8 +596,6 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         // starts on the chunks the launch before it wrote last (still in L2)
         const char *sn = getenv("TS_3D_SNAKE");   // "0": forwards
         p.snake_3d = !(sn && sn[0] == '0');
-        const char *sn2 = getenv("TS_2D_SNAKE");
-        p.snake_2d = sn2 && sn2[0] == '1';
         const char *pf = getenv("TS_3D_PREFETCH");
         p.prefetch_3d = !pf ? 2 : pf[0] == '0' ? 0 : pf[0] == '1' ? 1 : 2;
     }

@@ -69,7 +69,6 @@ struct StepParams {
     int tx;                // 2D: nodes each thread updates along x (1, 2 or 4)
     int xy_sweep_3d;       // 3D velocity kernel: warps interior in x and y take the x-y sweep
     int stress_pair_3d;    // 3D: normal and shear stress updates in one launch (k_stress3d)
-    int snake_2d;          // 2D stepper's velocity kernel: x-chunks in reverse launch order
     int snake_3d;          // 3D velocity kernel: x-chunks in reverse launch order
     int prefetch_3d;       // 3D L2 prefetch of a thread's nodes: 2 before the wait (state last written two
                            // launches back), then the rest; 1 the later nodes after the wait; 0 none
@@ -300,9 +299,8 @@ constexpr int kBX2 = 32, kBY2 = 8;              // 2D block: 32 (y) x 8 (x) thre
 
 // Flat index of the 2D block that updates node (x, y).
 inline int block_of_2d(const StepParams &p, int x, int y) {
-    const int gx = (p.ny + kBX2 - 1) / kBX2, nby = (p.nx + kBY2 * p.tx - 1) / (kBY2 * p.tx);
-    const int by = p.snake_2d ? nby - 1 - x / (kBY2 * p.tx) : x / (kBY2 * p.tx);   // launch order of the x-chunk
-    return by * gx + y / kBX2;
+    const int gx = (p.ny + kBX2 - 1) / kBX2;
+    return (x / (kBY2 * p.tx)) * gx + y / kBX2;
 }
 // 2D nodes per thread along x: one up to 768^2 grids (the L2-resident
 // small grids want more warps in flight), two from 1024^2 (fewer index and

@@ -332,9 +332,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
 template <int ORD, int FAM, int TX, bool FEAT = false, int MINB = 0>
 __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParams p, const int j) {
     const int y = blockIdx.x * kBX2 + threadIdx.x;
-    // x-chunks in reverse launch order with snake_2d: the stress launch before
-    // wrote the high chunks last, so they are the ones still in L2
-    const int x0 = ((p.snake_2d ? gridDim.y - 1 - blockIdx.y : blockIdx.y) * kBY2 + threadIdx.y) * TX;
+    const int x0 = (blockIdx.y * kBY2 + threadIdx.y) * TX;
     const int tid = threadIdx.y * kBX2 + threadIdx.x;
     const int blk = blockIdx.y * gridDim.x + blockIdx.x;
     const int P = p.pitch, nx = p.nx;
