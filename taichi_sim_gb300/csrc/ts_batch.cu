@@ -96,7 +96,6 @@ struct BParams {
     const int *step_base;
     int rec_work;
     int prefetch;   // L2 prefetch, before the wait, of each thread's own state (last written two launches back)
-    int snake;      // the velocity launch visits its blocks in reverse order
 };
 
 // b psi + a d, then d / k + psi (the shader's division, rounded as one)
@@ -118,9 +117,7 @@ struct Loc {
 template <int KIND, int CY, int TX, int SPT>
 __device__ __forceinline__ Loc locate(const BParams &p) {
     constexpr int W = 32 * SPT;
-    // the velocity launch in reverse order with p.snake: the stress launch
-    // before wrote the last blocks' state last, so that is what L2 holds
-    const int b = (KIND == 1 && p.snake) ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+    const int b = blockIdx.x;
     int q = 0;
 #pragma unroll 1
     while (q + 1 < p.n_ph && b >= p.block_end[KIND][q]) ++q;
@@ -1011,8 +1008,6 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
     // 47.6 Gcell/s); TS_BATCH_PREFETCH=0 turns it off
     const char *pf = getenv("TS_BATCH_PREFETCH");
     p.prefetch = !(pf && pf[0] == '0');
-    const char *sn = getenv("TS_BATCH_SNAKE");   // "1": reverse block order in the velocity launch (experiment)
-    p.snake = sn && sn[0] == '1';
     if ((rc = b->alloc(&p.block_max, b->n_blocks[1], true))) return bail(rc);
     int *fb = nullptr, *sb = nullptr;
     if ((rc = b->alloc(&fb, 1, false)) || (rc = b->alloc(&sb, 1, false))) return bail(rc);
