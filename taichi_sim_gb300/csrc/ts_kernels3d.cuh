@@ -88,7 +88,10 @@ __device__ __forceinline__ float deriv(const Pairs<ORD> &q, const StepParams &p,
 #ifndef TS_VELOCITY3D_MIN_BLOCKS
 #define TS_VELOCITY3D_MIN_BLOCKS 3
 #endif
-constexpr int kStressMinBlocks = 4, kVelocityMinBlocks = TS_VELOCITY3D_MIN_BLOCKS;
+#ifndef TS_STRESS3D_MIN_BLOCKS
+#define TS_STRESS3D_MIN_BLOCKS 4
+#endif
+constexpr int kStressMinBlocks = TS_STRESS3D_MIN_BLOCKS, kVelocityMinBlocks = TS_VELOCITY3D_MIN_BLOCKS;
 // x window of 2*ORD planes of one field at (y, z), first plane r0; planes
 // outside the grid read 0
 // (CHECK = false: every plane is known to lie inside the grid)
