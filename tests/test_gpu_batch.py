@@ -59,6 +59,24 @@ def test_batch_matches_single_shots(shape):
                 assert rel_l2(syy[s], want_f) <= TOL, (q, s, rel_l2(syy[s], want_f))
 
 
+def test_batch_without_prefetch_is_identical(monkeypatch):
+    """The batched kernels' L2 prefetch is a hint: with TS_BATCH_PREFETCH=0
+    the batch gives the same bits."""
+    sims = _phantoms(steps=120)
+    shots = [fmc_shot_sources(s) for s in sims]
+    out = {}
+    for flag in ("1", "0"):
+        monkeypatch.setenv("TS_BATCH_PREFETCH", flag)
+        with BatchStepper(sims, shots, block_cells=4, nodes_per_thread=2, shots_per_thread=2) as b:
+            b.run(120)
+            assert b.status()[2] == -1
+            out[flag] = [(b.traces(q), b.field(q, "syy")) for q in range(len(sims))]
+    for q in range(len(sims)):
+        assert np.abs(out["1"][q][0]).max() > 0
+        np.testing.assert_array_equal(out["0"][q][0], out["1"][q][0])
+        np.testing.assert_array_equal(out["0"][q][1], out["1"][q][1])
+
+
 def test_single_shot_matches_oracle():
     sim = _phantoms(steps=120)[1]
     table = fmc_shot_sources(sim)[3]

@@ -143,6 +143,19 @@ def test_parity_3d(name, palette, monkeypatch):
     _compare(sim, engine.WGSL3D, ["vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "sxz", "syz"])
 
 
+@pytest.mark.parametrize("option", ["TS_3D_PREFETCH=0", "TS_3D_PREFETCH=1", "TS_3D_SNAKE=0",
+                                    "TS_3D_STRESS_PAIR=0", "TS_3D_XY_SWEEP=0"])
+@pytest.mark.parametrize("name", ["wgsl3d_visco_deep", "wgsl3d_mono"])
+def test_parity_3d_launch_options(name, option, monkeypatch):
+    """The 3D launch options that are not the default (no L2 prefetch or the
+    prefetch after the wait only, the velocity launch walking its x-chunks
+    forwards, two stress launches, no x-y sweep) compute the same update."""
+    key, value = option.split("=")
+    monkeypatch.setenv(key, value)
+    sim = Simulator3D(CASES_3D[name]())
+    _compare(sim, engine.WGSL3D, ["vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "sxz", "syz"])
+
+
 def test_chunked_equals_single_run():
     """Steps split over many ts_run calls (graph and non-graph paths) give
     bit-identical results to one call."""
