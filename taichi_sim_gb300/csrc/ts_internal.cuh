@@ -321,7 +321,10 @@ constexpr int kBX3 = 32, kBY3 = 8, kTX3S = TS_STRESS3D_TX;
 // contiguous axis) times 8 / kZW3 rows along y (2 measured best of 1, 2, 4,
 // 8 on the 256^3 case: longer contiguous runs per block, y-neighbours still
 // shared in L1).
-constexpr int kZW3 = 2, kZB3 = kBX3 * kZW3, kYB3 = kBY3 / kZW3;
+#ifndef TS_3D_Z_RUNS
+#define TS_3D_Z_RUNS 2
+#endif
+constexpr int kZW3 = TS_3D_Z_RUNS, kZB3 = kBX3 * kZW3, kYB3 = kBY3 / kZW3;
 #ifndef TS_VELOCITY3D_TX
 #define TS_VELOCITY3D_TX 4
 #endif
