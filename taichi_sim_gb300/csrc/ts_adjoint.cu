@@ -701,8 +701,9 @@ int ts_adj_create(const ts_desc *d, int32_t checkpoint_every, ts_adj **out) {
             return bail(afail(TS_E_ARG, "more receivers than threads of a step launch"));
         std::vector<int> start(1, 0), first(std::max(1, d->n_rec), 0);
         std::vector<int64_t> cells;
+        const int rec_groups = receiver_groups(d, 3);
         for (int r = 0; r < d->n_rec; ++r) {
-            for (int pt = receiver_first_point(d, r, 3); pt >= 0 && pt < d->n_rec_pt && d->info_rec_pt[pt * 3 + 2] == r;
+            for (int pt = receiver_first_point(d, r, rec_groups); pt >= 0 && pt < d->n_rec_pt && d->info_rec_pt[pt * 3 + 2] == r;
                  ++pt) {
                 const int x = d->info_rec_pt[pt * 3], y = d->info_rec_pt[pt * 3 + 1];
                 if (x >= 0 && x < a->nx && y >= 0 && y < a->ny) cells.push_back((int64_t)x * a->P + y);

@@ -964,8 +964,9 @@ int ts_batch_create(const ts_batch_desc *bd, ts_batch **out) {
         h.shot_tab = dtab;
         // receivers (WGSL order over info_rec_pt)
         std::vector<int> rstart(1, 0), rcell, rfirst(std::max(1, d->n_rec), 0);
+        const int rec_groups = receiver_groups(d, 3);
         for (int r = 0; r < d->n_rec; ++r) {
-            for (int pt = receiver_first_point(d, r, 3); pt >= 0 && pt < d->n_rec_pt && d->info_rec_pt[pt * 3 + 2] == r; ++pt) {
+            for (int pt = receiver_first_point(d, r, rec_groups); pt >= 0 && pt < d->n_rec_pt && d->info_rec_pt[pt * 3 + 2] == r; ++pt) {
                 const int x = d->info_rec_pt[pt * 3], y = d->info_rec_pt[pt * 3 + 1];
                 if (x >= 0 && x < h.nx && y >= 0 && y < h.ny) rcell.push_back(x * h.ny + y);
             }

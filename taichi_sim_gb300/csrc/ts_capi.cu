@@ -151,6 +151,26 @@ std::mutex g_stage_mutex;
 char *g_stage = nullptr;
 cudaEvent_t g_stage_ev[2] = {nullptr, nullptr};
 
+// Host copy of one staging chunk on up to 8 threads (one thread's memcpy
+// runs well below the host memory bandwidth).
+void host_copy(void *dst, const void *src, size_t bytes) {
+    constexpr size_t kPart = (size_t)2 << 20;
+    const int parts = (int)std::min<size_t>(8, (bytes + kPart - 1) / kPart);
+    if (parts <= 1) {
+        std::memcpy(dst, src, bytes);
+        return;
+    }
+    const size_t per = (bytes + parts - 1) / parts;
+    std::vector<std::thread> pool;
+    for (int t = 1; t < parts; ++t)
+        pool.emplace_back([=] {
+            const size_t o = t * per;
+            if (o < bytes) std::memcpy(static_cast<char *>(dst) + o, static_cast<const char *>(src) + o, std::min(per, bytes - o));
+        });
+    std::memcpy(dst, src, std::min(per, bytes));
+    for (auto &th : pool) th.join();
+}
+
 cudaError_t stage_init() {
     if (g_stage) return cudaSuccess;
     cudaError_t e = cudaMallocHost(reinterpret_cast<void **>(&g_stage), 2 * kStageHalf);
@@ -185,7 +205,7 @@ cudaError_t stage_d2h(void *dst, const void *src, size_t width, size_t dpitch, s
         if (c > 0) {   // the previous chunk: wait for its DMA, copy it out
             const size_t q = c - 1, r0 = q * per, n = std::min(per, rows - r0);
             if ((e = cudaEventSynchronize(g_stage_ev[q & 1])) != cudaSuccess) return e;
-            std::memcpy(static_cast<char *>(dst) + r0 * width, g_stage + (q & 1) * kStageHalf, n * width);
+            host_copy(static_cast<char *>(dst) + r0 * width, g_stage + (q & 1) * kStageHalf, n * width);
         }
     }
     return cudaSuccess;
@@ -204,7 +224,7 @@ cudaError_t stage_h2d(void *dst, const void *src, size_t bytes, cudaStream_t st)
         const size_t off = c * kStageHalf, n = std::min(kStageHalf, bytes - off);
         char *buf = g_stage + (c & 1) * kStageHalf;
         if (c >= 2 && (e = cudaEventSynchronize(g_stage_ev[c & 1])) != cudaSuccess) return e;   // half free again
-        std::memcpy(buf, static_cast<const char *>(src) + off, n);
+        host_copy(buf, static_cast<const char *>(src) + off, n);
         if ((e = cudaMemcpyAsync(static_cast<char *>(dst) + off, buf, n, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
             (e = cudaEventRecord(g_stage_ev[c & 1], st)) != cudaSuccess)
             return e;
@@ -684,24 +704,37 @@ int ts_create(const ts_desc *d, ts_sim **out) {
             }
         });
     } else {
+        // one expression for every node; `at(a, b, c)` reads (rho, cs, cp) at
+        // (x + a, y + b, z + c), without bounds tests away from the far faces
+        auto node = [&](int64_t i, const auto &rho_at, const auto &cs_at, float cp) {
+            const float r = rho_at(0, 0, 0), cs = cs_at(0, 0, 0);
+            lam[i] = r * (cp * cp - 2.f * cs * cs);   // raw: the kernels multiply by dt
+            mu[i] = r * (cs * cs);
+            const float rxy = 0.25f * (rho_at(1, 0, 0) + rho_at(0, 0, 0) + rho_at(0, 1, 0) + rho_at(1, 1, 0));
+            const float cxy = 0.25f * (cs_at(1, 0, 0) + cs_at(0, 0, 0) + cs_at(0, 1, 0) + cs_at(1, 1, 0));
+            const float rxz = 0.25f * (rho_at(1, 0, 0) + rho_at(0, 0, 0) + rho_at(0, 0, 1) + rho_at(1, 0, 1));
+            const float cxz = 0.25f * (cs_at(1, 0, 0) + cs_at(0, 0, 0) + cs_at(0, 0, 1) + cs_at(1, 0, 1));
+            const float ryz = 0.25f * (rho_at(0, 1, 0) + rho_at(0, 0, 0) + rho_at(0, 0, 1) + rho_at(0, 1, 1));
+            const float cyz = 0.25f * (cs_at(0, 1, 0) + cs_at(0, 0, 0) + cs_at(0, 0, 1) + cs_at(0, 1, 1));
+            mus[0][i] = rxy * (cxy * cxy);
+            mus[1][i] = rxz * (cxz * cxz);
+            mus[2][i] = ryz * (cyz * cyz);
+            dtr0[i] = 0.5f * (rho_at(1, 0, 0) + r);   // raw: the kernels divide by rho
+            dtr1[i] = 0.5f * (rho_at(0, 1, 0) + r);
+        };
+        const int64_t SX = (int64_t)ny * nz, SY = nz;
         parallel_rows(nx, [&](int x) {
             for (int y = 0; y < ny; ++y)
                 for (int z = 0; z < nz; ++z) {
-                    const int64_t i = s->at(x, y, z);
-                    const float r = rho(x, y, z), cp = cpv(x, y, z), cs = csv(x, y, z);
-                    lam[i] = r * (cp * cp - 2.f * cs * cs);   // raw: the kernels multiply by dt
-                    mu[i] = r * (cs * cs);
-                    const float rxy = 0.25f * (rho(x + 1, y, z) + rho(x, y, z) + rho(x, y + 1, z) + rho(x + 1, y + 1, z));
-                    const float cxy = 0.25f * (csv(x + 1, y, z) + csv(x, y, z) + csv(x, y + 1, z) + csv(x + 1, y + 1, z));
-                    const float rxz = 0.25f * (rho(x + 1, y, z) + rho(x, y, z) + rho(x, y, z + 1) + rho(x + 1, y, z + 1));
-                    const float cxz = 0.25f * (csv(x + 1, y, z) + csv(x, y, z) + csv(x, y, z + 1) + csv(x + 1, y, z + 1));
-                    const float ryz = 0.25f * (rho(x, y + 1, z) + rho(x, y, z) + rho(x, y, z + 1) + rho(x, y + 1, z + 1));
-                    const float cyz = 0.25f * (csv(x, y + 1, z) + csv(x, y, z) + csv(x, y, z + 1) + csv(x, y + 1, z + 1));
-                    mus[0][i] = rxy * (cxy * cxy);
-                    mus[1][i] = rxz * (cxz * cxz);
-                    mus[2][i] = ryz * (cyz * cyz);
-                    dtr0[i] = 0.5f * (rho(x + 1, y, z) + r);   // raw: the kernels divide by rho
-                    dtr1[i] = 0.5f * (rho(x, y + 1, z) + r);
+                    const int64_t i = s->at(x, y, z), h = href(x, y, z);
+                    if (x + 1 < nx && y + 1 < ny && z + 1 < nz) {
+                        const float *R = d->rho + h, *C = d->cs + h;
+                        node(i, [&](int a, int b, int c) { return R[a * SX + b * SY + c]; },
+                             [&](int a, int b, int c) { return C[a * SX + b * SY + c]; }, d->cp[h]);
+                    } else {
+                        node(i, [&](int a, int b, int c) { return rho(x + a, y + b, z + c); },
+                             [&](int a, int b, int c) { return csv(x + a, y + b, z + c); }, cpv(x, y, z));
+                    }
                 }
         });
     }
@@ -884,8 +917,9 @@ int ts_create(const ts_desc *d, ts_sim **out) {
             }
         } else {
             const int cols = 1 + s->dims;  // [ix, iy(, iz), receiver]
+            const int rec_groups = ts::receiver_groups(d, cols);
             for (int r = 0; r < d->n_rec; ++r) {
-                for (int pt = ts::receiver_first_point(d, r, cols); pt >= 0 && pt < d->n_rec_pt && d->info_rec_pt[pt * cols + cols - 1] == r;
+                for (int pt = ts::receiver_first_point(d, r, rec_groups); pt >= 0 && pt < d->n_rec_pt && d->info_rec_pt[pt * cols + cols - 1] == r;
                      ++pt) {
                     const int *q = d->info_rec_pt + pt * cols;
                     const int x = q[0], y = q[1], z = s->dims == 3 ? q[2] : 0;

@@ -50,11 +50,15 @@ inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 // (sim_support/simulator.py:289-294), which is fewer than n_rec when some
 // receiving elements lie outside the ROI; an entry past its end reads as
 // "no point" (-1) instead of past the array.
-inline int receiver_first_point(const ts_desc *d, int r, int cols) {
-    if (d->n_rec_pt <= 0) return -1;
+inline int receiver_groups(const ts_desc *d, int cols) {
+    if (d->n_rec_pt <= 0) return 0;
     int groups = 1;
     for (int pt = 1; pt < d->n_rec_pt; ++pt)
         if (d->info_rec_pt[pt * cols + cols - 1] != d->info_rec_pt[(pt - 1) * cols + cols - 1]) ++groups;
+    return groups;
+}
+// (groups: receiver_groups(d, cols), counted once per table, not per receiver)
+inline int receiver_first_point(const ts_desc *d, int r, int groups) {
     return r < groups ? d->offset_sensors[r] : -1;
 }
 
