@@ -680,8 +680,8 @@ int ts_create(const ts_desc *d, ts_sim **out) {
     }
 
     clk.mark("fields");
-    // ---- per-node coefficients (host, reference averaging, folded with dt) ----
-    const float dt = d->dt;
+    // ---- per-node coefficients (host, reference averaging; raw: the kernels
+    // multiply by dt and divide by rho as the reference does) ----
     const size_t ng = (size_t)s->grid_elems;
     hvec lam = filled(ng, 0.f), mu = filled(ng, 0.f), dtr0 = filled(ng, 0.f), dtr1 = filled(ng, 0.f);
     hvec mus[3];
