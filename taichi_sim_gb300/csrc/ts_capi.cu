@@ -601,6 +601,8 @@ int ts_create(const ts_desc *d, ts_sim **out) {
 
     StepParams &p = s->p;
     p.family = s->family;
+    const char *te = getenv("TS_TAICHI_EXACT");   // "0": the Taichi semantics in the unbiased arithmetic
+    p.taichi_exact = !(te && te[0] == '0');
     // nodes per thread along x (2D; 3D velocity kernel): enough blocks to fill the GPU, as few
     // index/region/bookkeeping instructions per node as that allows
     {

@@ -49,18 +49,24 @@ namespace {
 // update carries a rounding bias that repeats at every node and time step;
 // kWgslFolded is the WGSL semantics with dt, 1/dx and 1/rho folded into the
 // coefficients (arrays hold lambda dt, mu dt, dt / rho), the form the
-// adjoint differentiates (ts_adjoint.cu).
-constexpr int kTaichi = 0, kWgslFolded = 1, kWgsl = 2;
+// adjoint differentiates (ts_adjoint.cu); kTaichiU is the Taichi kernels'
+// semantics (update regions, the source inside the velocity update) in
+// kWgsl's unbiased arithmetic.
+constexpr int kTaichi = 0, kWgslFolded = 1, kWgsl = 2, kTaichiU = 3;
+// the Taichi kernels' update regions and source injection
+constexpr bool taichi_semantics(int fam) { return fam == kTaichi || fam == kTaichiU; }
+// the unbiased arithmetic: raw coefficients, sums times 1/d as a pair, updates times dt, divisions by rho
+constexpr bool unbiased(int fam) { return fam == kWgsl || fam == kTaichiU; }
 
 // weight of derivative term c along axis a: coef / d (folded) or coef
 template <int FAM>
 __device__ __forceinline__ float dw(const StepParams &p, int a, int c) {
-    return FAM == kWgsl ? p.coef[c] : p.cd[a][c];
+    return unbiased(FAM) ? p.coef[c] : p.cd[a][c];
 }
 // a derivative's sum of weighted differences, divided by the grid step (kWgsl)
 template <int FAM>
 __device__ __forceinline__ float dfin(float s, const StepParams &p, int a) {
-    return FAM == kWgsl ? dscale(s, p.od[a], p.odl[a]) : s;
+    return unbiased(FAM) ? dscale(s, p.od[a], p.odl[a]) : s;
 }
 
 // Loads.  ldg: data no kernel writes (coefficients, tables), through the
@@ -82,7 +88,7 @@ __device__ __forceinline__ float cpml(float d, float psi_old, float &psi_new, co
 template <int FAM>
 __device__ __forceinline__ float cpmlf(float d, float psi_old, float &psi_new, const Cpml &t) {
     if (FAM == kTaichi) return taichi_cpml(d, psi_old, psi_new, t);
-    if (FAM == kWgsl) {
+    if (unbiased(FAM)) {
         psi_new = fmaf(t.b, psi_old, t.a * d);
         return qdiv(d, t.k, t.ik) + psi_new;
     }
@@ -257,7 +263,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
                             ux = fmaf(hl, srxx, fmaf(M, sryy, ux));
                             uy = fmaf(hl, srxx, fmaf(-M, sryy, uy));
                         }
-                        if (FAM == kWgsl) {   // (...) dt, wgsl:915-916
+                        if (unbiased(FAM)) {   // (...) dt, wgsl:915-916
                             sxx += ux * p.dt;
                             syy += uy * p.dt;
                         } else {
@@ -314,7 +320,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
                             u = fmaf(0.5f * Ms, sr, u);
                         }
                         if (FEAT) p.feat[kFeatShear * p.grid_elems + i] = fmaf(0.5f, sr, e);
-                        p.s[3][i] = FAM == kWgsl ? sxy + u * p.dt : sxy + u;
+                        p.s[3][i] = unbiased(FAM) ? sxy + u * p.dt : sxy + u;
                     }
                 }
             }
@@ -343,7 +349,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
     const int sy = live_col ? strip_index(p.strip[1], y) : -1;
     // y-part of the regions
     const bool yvy = y >= ORD - 1 && y < p.ny - ORD;
-    const bool yvx = FAM == kTaichi ? (y >= ORD && y < p.ny - ORD + 1) : (yvy && y >= ORD);
+    const bool yvx = taichi_semantics(FAM) ? (y >= ORD && y < p.ny - ORD + 1) : (yvy && y >= ORD);
     const int q0 = __ldg(p.src_block_start + blk), q1 = __ldg(p.src_block_start + blk + 1);
     const bool fast = interior_warp<ORD, TX>(p, y, x0, sy) && q0 == q1;   // no source node in the block
     pdl_wait();
@@ -398,7 +404,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             a = dfin<FAM>(a, p, 0);
             b = dfin<FAM>(b, p, 1);
             const float fax = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
-            const float vxn = FAM == kTaichi ? taichi_velocity(vx0[t], fax, 0.f, dx0[t], p.dt) : FAM == kWgsl ? wgsl_velocity_rho(vx0[t], fax, dx0[t], p.dt)
+            const float vxn = FAM == kTaichi ? taichi_velocity(vx0[t], fax, 0.f, dx0[t], p.dt) : unbiased(FAM) ? wgsl_velocity_rho(vx0[t], fax, dx0[t], p.dt)
                                                    : fmaf(fax, dx0[t], vx0[t]);
             a = 0.f;
             b = 0.f;
@@ -415,7 +421,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             a = dfin<FAM>(a, p, 0);
             b = dfin<FAM>(b, p, 1);
             const float fay = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
-            const float vyn = FAM == kTaichi ? taichi_velocity(vy0[t], fay, 0.f, dy0[t], p.dt) : FAM == kWgsl ? wgsl_velocity_rho(vy0[t], fay, dy0[t], p.dt)
+            const float vyn = FAM == kTaichi ? taichi_velocity(vy0[t], fay, 0.f, dy0[t], p.dt) : unbiased(FAM) ? wgsl_velocity_rho(vy0[t], fay, dy0[t], p.dt)
                                                    : fmaf(fay, dy0[t], vy0[t]);
             p.v[0][i] = vxn;
             p.v[1][i] = vyn;
@@ -444,7 +450,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
             if (!FAST && x >= nx) break;
             const int64_t i = (int64_t)x * P + y;
             const bool in_vy = FAST || (yvy && x >= ORD - 1 && x < nx - ORD);
-            const bool in_vx = FAST || (FAM == kTaichi ? (yvx && x >= ORD && x < nx - ORD + 1) : (yvx && in_vy && x >= ORD));
+            const bool in_vx = FAST || (taichi_semantics(FAM) ? (yvx && x >= ORD && x < nx - ORD + 1) : (yvx && in_vy && x >= ORD));
             const int sx = FAST ? -1 : strip_index(p.strip[0], x);
             const int64_t ix = (int64_t)sx * P + y, iy = (int64_t)x * p.strip[1].width + syl;
             // ---- loads ----
@@ -495,7 +501,7 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                 }
                 fax = FAM == kTaichi ? __fadd_rn(a, b) : a + b;
                 vxn = FAM == kTaichi ? taichi_velocity(vx0, fax, 0.f, dx0, p.dt)
-                      : FAM == kWgsl   ? wgsl_velocity_rho(vx0, fax, dx0, p.dt)
+                      : unbiased(FAM)  ? wgsl_velocity_rho(vx0, fax, dx0, p.dt)
                                        : fmaf(fax, dx0, vx0);
             }
             if (in_vy) {
@@ -532,11 +538,22 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_velocity2d(const StepParam
                         }
                     }
                     vyn = taichi_velocity(vy0, fay, src, dy0, p.dt);
+                } else if (FAM == kTaichiU) {
+                    // the source inside the update, as the Taichi kernel adds it, in the unbiased arithmetic
+                    float src = 0.f;
+                    if constexpr (!FAST) {
+                        for (int q = q0; q < q1; ++q) {
+                            const Source s = p.src[q];
+                            if (s.cell == i && k < p.src_rows)
+                                src = wgsl_source(__ldg(p.src_tab + (int64_t)k * p.src_ncol + s.col), s.scale, p.dt);
+                        }
+                    }
+                    vyn = dy0 > 0.f ? vy0 + (src + qdiv(fay * p.dt, dy0, __frcp_rn(dy0))) : vy0;
                 } else {
                     vyn = FAM == kWgsl ? wgsl_velocity_rho(vy0, fay, dy0, p.dt) : fmaf(fay, dy0, vy0);
                 }
             }
-            if constexpr (!FAST && FAM != kTaichi) {
+            if constexpr (!FAST && !taichi_semantics(FAM)) {
                 for (int q = q0; q < q1; ++q) {
                     const Source s = p.src[q];
                     if (s.cell == i && k < p.src_rows)

@@ -16,9 +16,14 @@ void launch_tx(const StepParams &p, int zen_mode, int j, cudaStream_t st, int pa
     dim3 block(kBX2, kBY2);
     dim3 grid((p.ny + kBX2 - 1) / kBX2, (p.nx + kBY2 * TX - 1) / (kBY2 * TX));
     const bool three = p.zen.n == 3;
-    if (p.family == kTaichi) {
-        if (parts & 1) launch_pdl(k_stress2d<ORD, 0, 0, 0, TX>, grid, block, st, p);
-        if (parts & 2) launch_pdl(k_velocity2d<ORD, 0, TX>, grid, block, st, p, j);
+    if (p.family == kTaichi) {   // Taichi semantics: exact or unbiased arithmetic
+        if (p.taichi_exact) {
+            if (parts & 1) launch_pdl(k_stress2d<ORD, kTaichi, 0, 0, TX>, grid, block, st, p);
+            if (parts & 2) launch_pdl(k_velocity2d<ORD, kTaichi, TX>, grid, block, st, p, j);
+        } else {
+            if (parts & 1) launch_pdl(k_stress2d<ORD, kTaichiU, 0, 0, TX>, grid, block, st, p);
+            if (parts & 2) launch_pdl(k_velocity2d<ORD, kTaichiU, TX>, grid, block, st, p, j);
+        }
         return;
     }
     if constexpr (ORD == 2) {   // coefficient palette (order 2 only, the benchmark's)
