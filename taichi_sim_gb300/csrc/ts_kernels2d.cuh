@@ -66,7 +66,9 @@ __device__ __forceinline__ float dw(const StepParams &p, int a, int c) {
 // a derivative's sum of weighted differences, divided by the grid step (kWgsl)
 template <int FAM>
 __device__ __forceinline__ float dfin(float s, const StepParams &p, int a) {
-    return unbiased(FAM) ? dscale(s, p.od[a], p.odl[a]) : s;
+    // kTaichiU: times the reference's own rounded 1/d, as the Taichi kernels
+    // scale every term (their constant's rounding is part of what they compute)
+    return FAM == kWgsl ? dscale(s, p.od[a], p.odl[a]) : FAM == kTaichiU ? s * p.od[a] : s;
 }
 
 // Loads.  ldg: data no kernel writes (coefficients, tables), through the
@@ -243,6 +245,12 @@ __global__ void __launch_bounds__(kBX2 *kBY2, MINB) k_stress2d(const StepParams 
                         const float dl = __fmul_rn(L, __fadd_rn(ddx, ddy));
                         sxx = taichi_normal(sxx, dl, M, ddx, p.dt);
                         syy = taichi_normal(syy, dl, M, ddy, p.dt);
+                    } else if (FAM == kTaichiU) {
+                        // (lambda div + 2 mu d) dt with no per-node constant folded (lambda + 2 mu
+                        // rounded once per node would bias every step alike)
+                        const float dl = L * (ddx + ddy);
+                        sxx += fmaf(2.f * M, ddx, dl) * p.dt;
+                        syy += fmaf(2.f * M, ddy, dl) * p.dt;
                     } else {
                         const float L2M = fmaf(2.f, M, L);
                         float ux = fmaf(L2M, ddx, L * ddy), uy = fmaf(L, ddx, L2M * ddy);
