@@ -176,6 +176,9 @@ def workload_config(name, sim):
     return {"workload": name, "grid": list(sim.grid_shape()), "time_steps_per_step": int(sim._n_steps),
             "family": FAMILY[name], "receivers": int(sim._n_rec),
             "zener": "L=3 fitted 2-8 MHz, per-cell Q" if name != "elastic2d" else None,
+            "arithmetic": ("every operation rounded on its own (TS_TAICHI_EXACT=1)"
+                           if os.environ.get("TS_TAICHI_EXACT") == "1" else "the reference's constants, no rounding bias")
+            if name == "elastic2d" else "unbiased (raw coefficients, 1/d as a pair, divisions by rho)",
             "l2": "256 MiB flush written after every simulation (inside the timed region)"}
 
 
@@ -206,6 +209,7 @@ def run_reference(args):
     dt = time.time() - t
     value = cells * sample * args.steps / dt / 1e9
     cfg = workload_config(name, sim)
+    cfg["arithmetic"] = "strict IEEE float, the reference's operation order (CPU restatement)"
     cfg["parallelism"] = "single GPU"
     desc = (f"{sample} of the {sim._n_steps} time steps of the full {'x'.join(map(str, sim.grid_shape()))} grid "
             f"per bench step (C restatement of the reference kernels, OpenMP, {cores} threads)")

@@ -57,7 +57,9 @@ extern "C" {
 #define TS_E_TIMEOUT 6    /* a bounded wait between thread blocks gave up (state invalid until ts_reset) */
 
 /* kernel families: which reference backend's semantics to follow */
-#define TS_TAICHI2D 0     /* sim_taichi_elastic.py:138-309 (2D elastic) */
+#define TS_TAICHI2D 0     /* sim_taichi_elastic.py:138-309 (2D elastic); the arithmetic keeps the
+                             reference's constants without rounding bias, or with TS_TAICHI_EXACT=1
+                             in the environment at ts_create rounds every operation on its own */
 #define TS_WGSL2D 1       /* shader_webgpu_viscoelastic.wgsl:829-1141 */
 #define TS_WGSL3D 2       /* shader_webgpu_3D_viscoelastic.wgsl:1341-1850 */
 
@@ -181,7 +183,9 @@ int ts_launches_per_step(const ts_sim *sim, int32_t *launches);
  * TS_PATH_PERSISTENT, every step of the call in one cooperative launch that
  * keeps the wavefield on chip (opt-in with TS_2D_PERSISTENT=1 in the
  * environment at ts_create, for 2D elastic models of order 2 whose row
- * slabs fit shared memory).  Both give the same bits. */
+ * slabs fit shared memory).  Both give the same bits (for family
+ * TS_TAICHI2D, with TS_TAICHI_EXACT=1: the persistent kernel rounds every
+ * operation on its own, as the stepped path then does). */
 #define TS_PATH_STEPPED 0
 #define TS_PATH_PERSISTENT 1
 int ts_step_path(const ts_sim *sim, int32_t *path);

@@ -601,8 +601,11 @@ int ts_create(const ts_desc *d, ts_sim **out) {
 
     StepParams &p = s->p;
     p.family = s->family;
-    const char *te = getenv("TS_TAICHI_EXACT");   // "0": the Taichi semantics in the unbiased arithmetic
-    p.taichi_exact = !(te && te[0] == '0');
+    // family TS_TAICHI2D: the unbiased arithmetic by default; TS_TAICHI_EXACT=1
+    // rounds every operation on its own, bit for bit the float oracle (and the
+    // persistent path, which computes that form)
+    const char *te = getenv("TS_TAICHI_EXACT");
+    p.taichi_exact = te && te[0] == '1';
     // nodes per thread along x (2D; 3D velocity kernel): enough blocks to fill the GPU, as few
     // index/region/bookkeeping instructions per node as that allows
     {

@@ -66,7 +66,8 @@ struct alignas(16) Pal3 {
 
 struct StepParams {
     int family;
-    int taichi_exact;      // family TS_TAICHI2D: every operation rounded on its own, as the float oracle
+    int taichi_exact;      // family TS_TAICHI2D: every operation rounded on its own (as the float oracle),
+                           // else the unbiased arithmetic (kTaichiU)
     int tx;                // 2D: nodes each thread updates along x (1, 2 or 4)
     int xy_sweep_3d;       // 3D velocity kernel: warps interior in x and y take the x-y sweep
     int stress_pair_3d;    // 3D: normal and shear stress updates in one launch (k_stress3d)

@@ -16,10 +16,10 @@ the tests are ordered and named by workload.
 with the Taichi semantics (sim_taichi_elastic.py:311-351) and compares the
 traces with the B-scan the reference shipped
 (``pedro/results/result_teste_aco.npy``, a Taichi GPU run with fast math):
-relative L2 <= 1e-5 (the Taichi-family kernels equal the float oracle bit
-for bit, which reaches 7.4e-6 over the same 10000 steps), the same first
-non-zero row (335) and the same arrival row of the largest sample in every
-column.
+relative L2 <= 1e-5 in both arithmetic forms of the Taichi family (the
+exact form equals the float oracle bit for bit, which reaches 7.4e-6 over
+the same 10000 steps), the same first non-zero row (335) and the same
+arrival row of the largest sample in every column.
 """
 import numpy as np
 import pytest
@@ -38,7 +38,12 @@ F2 = ("vx", "vy", "sxx", "syy", "sxy")
 F3 = ("vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "sxz", "syz")
 
 
-def test_golden_teste_pedro():
+@pytest.mark.parametrize("exact", ["0", "1"], ids=["unbiased", "exact"])
+def test_golden_teste_pedro(exact, monkeypatch):
+    """Both arithmetic forms of the Taichi family: the default (the
+    reference's constants, no rounding bias) and every operation rounded on
+    its own (TS_TAICHI_EXACT=1, bit for bit the float oracle)."""
+    monkeypatch.setenv("TS_TAICHI_EXACT", exact)
     dims, cfg = config_with_maps("teste_pedro")
     sim = Simulator(cfg)
     assert sim.grid_shape() == (725, 572) and sim._n_steps == 10000
@@ -48,6 +53,7 @@ def test_golden_teste_pedro():
     g = golden_bscan()
     assert tr.shape == g.shape
     err = rel_l2(tr, g)
+    print(f"teste_pedro, {'exact' if exact == '1' else 'unbiased'} arithmetic: traces vs golden B-scan {err:.3e}")
     assert int(np.nonzero(np.abs(tr).sum(1))[0][0]) == 335
     assert err <= TOL, err
     np.testing.assert_array_equal(np.argmax(np.abs(tr), axis=0), np.argmax(np.abs(g), axis=0))
@@ -79,11 +85,14 @@ def _check_stepper(sim, family, names, n_steps, exact=False):
     return errs
 
 
-def test_full_elastic2d_512_2000_steps():
-    """Taichi semantics, bit for bit the float oracle."""
+@pytest.mark.parametrize("exact", ["0", "1"], ids=["unbiased", "exact"])
+def test_full_elastic2d_512_2000_steps(exact, monkeypatch):
+    """Taichi semantics: within the tolerance in the default arithmetic, bit
+    for bit the float oracle with every operation rounded on its own."""
+    monkeypatch.setenv("TS_TAICHI_EXACT", exact)
     sim = Simulator(workloads.elastic2d_512())
     assert sim.grid_shape() == (512, 512)
-    _check_stepper(sim, engine.TAICHI2D, F2, 2000, exact=True)
+    _check_stepper(sim, engine.TAICHI2D, F2, 2000, exact=exact == "1")
 
 
 def test_full_visco2d_1024_4000_steps():

@@ -118,10 +118,13 @@ TAICHI_CASES = sorted(n for n, (_, f) in CASES_2D.items() if f == engine.TAICHI2
 @pytest.mark.parametrize("persistent", ["0", "1"], ids=["regular", "persistent"])
 @pytest.mark.parametrize("name", TAICHI_CASES)
 def test_taichi_family_is_bit_exact(name, persistent, monkeypatch):
-    """The Taichi family keeps the reference's operation order with every
-    operation rounded on its own, so every field and trace equals the
-    strict-IEEE float oracle bit for bit, on both 2D paths (the persistent
-    one serves order 2 only; other orders take the regular one)."""
+    """The Taichi family's exact form (TS_TAICHI_EXACT=1) keeps the
+    reference's operation order with every operation rounded on its own, so
+    every field and trace equals the strict-IEEE float oracle bit for bit, on
+    both 2D paths (the persistent one serves order 2 only; other orders take
+    the regular one).  The default form is held to the tolerance by the
+    parity cases above."""
+    monkeypatch.setenv("TS_TAICHI_EXACT", "1")
     monkeypatch.setenv("TS_2D_PERSISTENT", persistent)
     build, family = CASES_2D[name]
     sim = Simulator(build())

@@ -33,6 +33,7 @@ CASES = {
 
 def _run(sim, family, chunks, monkeypatch, persistent):
     monkeypatch.setenv("TS_2D_PERSISTENT", "1" if persistent else "0")
+    monkeypatch.setenv("TS_TAICHI_EXACT", "1")   # the persistent kernel's form of the Taichi arithmetic
     with engine.Stepper(sim, family=family) as st:
         before = st.launch_count()
         for n in chunks:
