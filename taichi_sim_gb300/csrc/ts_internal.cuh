@@ -286,13 +286,18 @@ inline void launch_pdl(void (*kern)(Params...), dim3 grid, dim3 block, cudaStrea
 // one step: 1 = stress, 2 = velocity, 3 = both (in that order).
 void launch_step_2d(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st, int parts = 3);
 // Family TS_WGSL2D step with coefficients folded with dt (the adjoint's
-// forward; p.tx must be 2, ord 2 or 4), without and with the adjoint record
-// written to p.feat.
+// forward; p.tx 1 or 2 at order 2, 2 above; folded: ord 2 or 4), without and
+// with the adjoint record written to p.feat.
 void launch_step_2d_folded(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st);
 void launch_step_2d_feat(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st);
 void launch_step_3d(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st, int parts = 3);
 // the palette instantiations of the stress kernels (p.pal set; 32-bit offsets)
 void launch_step_3d_pal(const StepParams &p, int ord, int zen_mode, int j, cudaStream_t st, int parts);
+// the array instantiations of orders 3 to 6 (ts_stepper3d_o<N>.cu)
+void launch_step_3d_arrays_3(const StepParams &p, int zen_mode, int j, cudaStream_t st, int parts);
+void launch_step_3d_arrays_4(const StepParams &p, int zen_mode, int j, cudaStream_t st, int parts);
+void launch_step_3d_arrays_5(const StepParams &p, int zen_mode, int j, cudaStream_t st, int parts);
+void launch_step_3d_arrays_6(const StepParams &p, int zen_mode, int j, cudaStream_t st, int parts);
 void launch_reset_scalars(int *first_bad, int *step_base, cudaStream_t st);
 void launch_advance(int *step_base, int n, cudaStream_t st);
 int blocks_2d(const StepParams &p);
