@@ -613,8 +613,6 @@ int ts_create(const ts_desc *d, ts_sim **out) {
         p.tx = s->dims == 3 ? ts::velocity_tx_3d(d->ord) : ts::nodes_per_thread_2d(cells);
         const char *xy = getenv("TS_3D_XY_SWEEP");
         p.xy_sweep_3d = !(xy && xy[0] == '0');
-        const char *ssw = getenv("TS_3D_STRESS_SWEEP");   // "1": interior sweep in the stress kernels (experiment)
-        p.stress_sweep_3d = ssw && ssw[0] == '1';
         const char *pair = getenv("TS_3D_STRESS_PAIR");
         p.stress_pair_3d = !(pair && pair[0] == '0');
         // L2 prefetch in the 3D kernels: 2 (default) the state last written

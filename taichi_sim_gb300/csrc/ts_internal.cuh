@@ -71,7 +71,6 @@ struct StepParams {
     int tx;                // 2D: nodes each thread updates along x (1, 2 or 4)
     int xy_sweep_3d;       // 3D velocity kernel: warps interior in x and y take the x-y sweep
     int stress_pair_3d;    // 3D: normal and shear stress updates in one launch (k_stress3d)
-    int stress_sweep_3d;   // 3D stress kernels: interior warps sweep without per-node tests
     int snake_3d;          // 3D velocity kernel: x-chunks in reverse launch order
     int prefetch_3d;       // 3D L2 prefetch of a thread's nodes: 2 before the wait (state last written two
                            // launches back), then the rest; 1 the later nodes after the wait; 0 none

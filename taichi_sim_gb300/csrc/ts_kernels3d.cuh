@@ -88,12 +88,6 @@ __device__ __forceinline__ float deriv(const Pairs<ORD> &q, const StepParams &p,
 #ifndef TS_VELOCITY3D_MIN_BLOCKS
 #define TS_VELOCITY3D_MIN_BLOCKS 3
 #endif
-// The stress kernels' interior sweep is compiled only with TS_3D_STRESS_FAST=1
-// (its second copy of the loop changes the register allocation of the first).
-#ifndef TS_3D_STRESS_FAST
-#define TS_3D_STRESS_FAST 0
-#endif
-constexpr bool kStressSweep3 = TS_3D_STRESS_FAST != 0;
 #ifndef TS_STRESS3D_MIN_BLOCKS
 #define TS_STRESS3D_MIN_BLOCKS 4
 #endif
@@ -158,10 +152,6 @@ __device__ __forceinline__ void normal3d_body(const StepParams &p, int bz) {
     const int z = blockIdx.x * kZB3 + (threadIdx.y % kZW3) * kBX3 + threadIdx.x;
     const int y = blockIdx.y * kYB3 + threadIdx.y / kZW3;
     const int x0 = bz * kTX3S;
-    // warps whose chunks lie wholly in the interior (no strips, no region or
-    // bounds tests; decided by all lanes before any returns)
-    const bool fast = kStressSweep3 && p.stress_sweep_3d &&
-                      interior_warp<ORD, kTX3S>(p, y, z, x0, strip_index(p.strip[1], y), strip_index(p.strip[2], z));
     if (y >= p.ny || z >= p.nz || x0 >= p.nx) return;
     const I X = (I)p.plane, Y = (I)p.pitch, yz = (I)y * Y + z, G = (I)p.grid_elems;
     const float *__restrict__ vx = p.v[0];
@@ -211,111 +201,105 @@ __device__ __forceinline__ void normal3d_body(const StepParams &p, int bz) {
             }
         }
     }
-    auto sweep = [&](auto fast_tag) {
-        constexpr bool FAST = decltype(fast_tag)::value;
-        const int syl = FAST ? -1 : sy, szl = FAST ? -1 : sz;
-        float wx[2 * ORD];   // vx planes [x-ORD+1, x+ORD]
-        xwindow<ORD, !FAST>(wx, vx, x0 - ORD + 1, p.nx, X, yz);
-    #pragma unroll
-        for (int t = 0; t < kTX3S; ++t) {
-            const int x = x0 + t;
-            if (!FAST && x >= p.nx) break;
-            if (FAST || (yz_n && x >= ORD - 1 && x < p.nx - ORD)) {
-                const I i = (I)x * X + yz;
-                const int sx = FAST ? -1 : strip_index(p.strip[0], x);
-                const I ix = ((I)sx * p.ny + y) * Y + z;
-                const I iy = ((I)x * p.strip[1].width + syl) * Y + z;
-                const I iz = ((I)x * p.ny + y) * p.strip[2].width + szl;
-                // ---- loads ----
-                const Pairs<ORD> n_y = load_pairs<ORD, false>(vy, i, Y);   // vy[y+c]-vy[y-c-1]
-                const Pairs<ORD> n_z = load_pairs<ORD, false>(vz, i, (I)1);   // vz[z+c]-vz[z-c-1]
-                // palette: the index first, its table entry after every other load
-                // (the entry load waits for the index)
-                const uint16_t pidx = PAL ? __ldg(p.pal_idx + i) : 0;
-                float L = 0.f, M = 0.f, gp = 1.f, gs = 1.f;
-                if constexpr (!PAL) {
-                    L = __ldg(p.lam_dt + i);
-                    M = __ldg(p.mu_dt + i);
-                    if (ZM == 2) {
-                        gp = __ldg(p.g_p + i);
-                        gs = __ldg(p.g_s + i);
-                    }
+    float wx[2 * ORD];   // vx planes [x-ORD+1, x+ORD]
+    xwindow<ORD>(wx, vx, x0 - ORD + 1, p.nx, X, yz);
+#pragma unroll
+    for (int t = 0; t < kTX3S; ++t) {
+        const int x = x0 + t;
+        if (x >= p.nx) break;
+        if (yz_n && x >= ORD - 1 && x < p.nx - ORD) {
+            const I i = (I)x * X + yz;
+            const int sx = strip_index(p.strip[0], x);
+            const I ix = ((I)sx * p.ny + y) * Y + z;
+            const I iy = ((I)x * p.strip[1].width + sy) * Y + z;
+            const I iz = ((I)x * p.ny + y) * p.strip[2].width + sz;
+            // ---- loads ----
+            const Pairs<ORD> n_y = load_pairs<ORD, false>(vy, i, Y);   // vy[y+c]-vy[y-c-1]
+            const Pairs<ORD> n_z = load_pairs<ORD, false>(vz, i, (I)1);   // vz[z+c]-vz[z-c-1]
+            // palette: the index first, its table entry after every other load
+            // (the entry load waits for the index)
+            const uint16_t pidx = PAL ? __ldg(p.pal_idx + i) : 0;
+            float L = 0.f, M = 0.f, gp = 1.f, gs = 1.f;
+            if constexpr (!PAL) {
+                L = __ldg(p.lam_dt + i);
+                M = __ldg(p.mu_dt + i);
+                if (ZM == 2) {
+                    gp = __ldg(p.g_p + i);
+                    gs = __ldg(p.g_s + i);
                 }
-                const float s0 = p.s[0][i], s1 = p.s[1][i], s2 = p.s[2][i];
-                float pz0 = 0.f, pz1 = 0.f, pz2 = 0.f;
-                if (sx >= 0) pz0 = p.psi[0][ix];
-                if (syl >= 0) pz1 = p.psi[1][iy];
-                if (szl >= 0) pz2 = p.psi[2][iz];
-                float r0[R], r1[R], r2[R];
-                if (ZM != 0) {
-    #pragma unroll
-                    for (int l = 0; l < R; ++l)
-                        if (l < n_mech) {
-                            r0[l] = p.r[0][l * G + i];
-                            r1[l] = p.r[1][l * G + i];
-                            r2[l] = p.r[2][l * G + i];
-                        }
-                }
-                if constexpr (PAL) {
-                    const float4 c = __ldg(&p.pal[pidx].normal);
-                    L = c.x;
-                    M = c.y;
-                    if (ZM == 2) {
-                        gp = c.z;
-                        gs = c.w;
-                    }
-                }
-                // ---- update: vx[x+c+1]-vx[x-c] from the window ----
-                float ddx = wderiv<ORD>(wx, p), ddy = deriv(n_y, p, 1), ddz = deriv(n_z, p, 2);
-                float np_;
-                if (sx >= 0) {
-                    ddx = cpml(ddx, pz0, np_, p.tab_h[0][x]);
-                    p.psi[0][ix] = np_;
-                }
-                if (syl >= 0) {
-                    ddy = cpml(ddy, pz1, np_, p.tab_f[1][y]);
-                    p.psi[1][iy] = np_;
-                }
-                if (szl >= 0) {
-                    ddz = cpml(ddz, pz2, np_, p.tab_f[2][z]);
-                    p.psi[2][iz] = np_;
-                }
-                const float L2M = fmaf(2.f, M, L);
-                float ux = fmaf(L2M, ddx, L * (ddy + ddz));
-                float uy = fmaf(L2M, ddy, L * (ddx + ddz));
-                float uz = fmaf(L2M, ddz, L * (ddx + ddy));
-                if (ZM != 0) {
-                    const float div = ddx + ddy + ddz;
-                    const float third = div * (1.f / 3.f);
-                    const float dy_ = ddx - third, dz_ = ddy - third;
-                    float srxx = 0.f, sryy = 0.f, srzz = 0.f;
-    #pragma unroll
-                    for (int l = 0; l < R; ++l)
-                        if (l < n_mech) {
-                            const float a = fmaf(p.zen.Ap[l], r0[l], (p.zen.Bp[l] * gp) * div);
-                            const float b = fmaf(p.zen.As[l], r1[l], (p.zen.Bs[l] * gs) * dy_);
-                            const float c = fmaf(p.zen.As[l], r2[l], (p.zen.Bs[l] * gs) * dz_);
-                            srxx += r0[l] + a;
-                            sryy += r1[l] + b;
-                            srzz += r2[l] + c;
-                            p.r[0][l * G + i] = a;
-                            p.r[1][l * G + i] = b;
-                            p.r[2][l * G + i] = c;
-                        }
-                    const float hl23 = 0.5f * fmaf(2.f / 3.f, M, L);
-                    ux = fmaf(hl23, srxx, fmaf(M, sryy, ux));
-                    uy = fmaf(hl23, srxx, fmaf(M, srzz, uy));
-                    uz = fmaf(0.5f * L2M, srxx, fmaf(-M * (1.f / 3.f), sryy + srzz, uz));
-                }
-                p.s[0][i] = s0 + ux * p.dt;   // (...) dt, wgsl3d:1442-1449
-                p.s[1][i] = s1 + uy * p.dt;
-                p.s[2][i] = s2 + uz * p.dt;
             }
-            if (t + 1 < kTX3S) xshift<ORD, !FAST>(wx, vx, x + ORD + 1, p.nx, X, yz);
+            const float s0 = p.s[0][i], s1 = p.s[1][i], s2 = p.s[2][i];
+            float pz0 = 0.f, pz1 = 0.f, pz2 = 0.f;
+            if (sx >= 0) pz0 = p.psi[0][ix];
+            if (sy >= 0) pz1 = p.psi[1][iy];
+            if (sz >= 0) pz2 = p.psi[2][iz];
+            float r0[R], r1[R], r2[R];
+            if (ZM != 0) {
+#pragma unroll
+                for (int l = 0; l < R; ++l)
+                    if (l < n_mech) {
+                        r0[l] = p.r[0][l * G + i];
+                        r1[l] = p.r[1][l * G + i];
+                        r2[l] = p.r[2][l * G + i];
+                    }
+            }
+            if constexpr (PAL) {
+                const float4 c = __ldg(&p.pal[pidx].normal);
+                L = c.x;
+                M = c.y;
+                if (ZM == 2) {
+                    gp = c.z;
+                    gs = c.w;
+                }
+            }
+            // ---- update: vx[x+c+1]-vx[x-c] from the window ----
+            float ddx = wderiv<ORD>(wx, p), ddy = deriv(n_y, p, 1), ddz = deriv(n_z, p, 2);
+            float np_;
+            if (sx >= 0) {
+                ddx = cpml(ddx, pz0, np_, p.tab_h[0][x]);
+                p.psi[0][ix] = np_;
+            }
+            if (sy >= 0) {
+                ddy = cpml(ddy, pz1, np_, p.tab_f[1][y]);
+                p.psi[1][iy] = np_;
+            }
+            if (sz >= 0) {
+                ddz = cpml(ddz, pz2, np_, p.tab_f[2][z]);
+                p.psi[2][iz] = np_;
+            }
+            const float L2M = fmaf(2.f, M, L);
+            float ux = fmaf(L2M, ddx, L * (ddy + ddz));
+            float uy = fmaf(L2M, ddy, L * (ddx + ddz));
+            float uz = fmaf(L2M, ddz, L * (ddx + ddy));
+            if (ZM != 0) {
+                const float div = ddx + ddy + ddz;
+                const float third = div * (1.f / 3.f);
+                const float dy_ = ddx - third, dz_ = ddy - third;
+                float srxx = 0.f, sryy = 0.f, srzz = 0.f;
+#pragma unroll
+                for (int l = 0; l < R; ++l)
+                    if (l < n_mech) {
+                        const float a = fmaf(p.zen.Ap[l], r0[l], (p.zen.Bp[l] * gp) * div);
+                        const float b = fmaf(p.zen.As[l], r1[l], (p.zen.Bs[l] * gs) * dy_);
+                        const float c = fmaf(p.zen.As[l], r2[l], (p.zen.Bs[l] * gs) * dz_);
+                        srxx += r0[l] + a;
+                        sryy += r1[l] + b;
+                        srzz += r2[l] + c;
+                        p.r[0][l * G + i] = a;
+                        p.r[1][l * G + i] = b;
+                        p.r[2][l * G + i] = c;
+                    }
+                const float hl23 = 0.5f * fmaf(2.f / 3.f, M, L);
+                ux = fmaf(hl23, srxx, fmaf(M, sryy, ux));
+                uy = fmaf(hl23, srxx, fmaf(M, srzz, uy));
+                uz = fmaf(0.5f * L2M, srxx, fmaf(-M * (1.f / 3.f), sryy + srzz, uz));
+            }
+            p.s[0][i] = s0 + ux * p.dt;   // (...) dt, wgsl3d:1442-1449
+            p.s[1][i] = s1 + uy * p.dt;
+            p.s[2][i] = s2 + uz * p.dt;
         }
-    };
-    if (kStressSweep3 && fast) sweep(std::true_type{});
-    else sweep(std::false_type{});
+        if (t + 1 < kTX3S) xshift<ORD>(wx, vx, x + ORD + 1, p.nx, X, yz);
+    }
     pdl_trigger();
 }
 
@@ -327,10 +311,6 @@ __device__ __forceinline__ void shear3d_body(const StepParams &p, int bz) {
     const int z = blockIdx.x * kZB3 + (threadIdx.y % kZW3) * kBX3 + threadIdx.x;
     const int y = blockIdx.y * kYB3 + threadIdx.y / kZW3;
     const int x0 = bz * kTX3S;
-    // warps whose chunks lie wholly in the interior (no strips, no region or
-    // bounds tests; decided by all lanes before any returns)
-    const bool fast = kStressSweep3 && p.stress_sweep_3d &&
-                      interior_warp<ORD, kTX3S>(p, y, z, x0, strip_index(p.strip[1], y), strip_index(p.strip[2], z));
     if (y >= p.ny || z >= p.nz || x0 >= p.nx) return;
     const I X = (I)p.plane, Y = (I)p.pitch, yz = (I)y * Y + z, G = (I)p.grid_elems;
     const float *__restrict__ vx = p.v[0];
@@ -377,151 +357,145 @@ __device__ __forceinline__ void shear3d_body(const StepParams &p, int bz) {
             }
         }
     }
-    auto sweep = [&](auto fast_tag) {
-        constexpr bool FAST = decltype(fast_tag)::value;
-        const int syl = FAST ? -1 : sy, szl = FAST ? -1 : sz;
-        float wy[2 * ORD], wz[2 * ORD];   // vy and vz planes [x-ORD, x+ORD-1]
-        xwindow<ORD, !FAST>(wy, vy, x0 - ORD, p.nx, X, yz);
-        xwindow<ORD, !FAST>(wz, vz, x0 - ORD, p.nx, X, yz);
-    #pragma unroll
-        for (int t = 0; t < kTX3S; ++t) {
-            const int x = x0 + t;
-            if (!FAST && x >= p.nx) break;
-            const bool in_xy = FAST || (yz_s && x >= ORD && x < p.nx - ORD + 1);
-            const bool in_yz = FAST || (yz_s && x >= ORD - 1 && x < p.nx - ORD);
-            if (in_xy || in_yz) {
-                const I i = (I)x * X + yz;
-                const int sx = FAST ? -1 : strip_index(p.strip[0], x);
-                const I ix = ((I)sx * p.ny + y) * Y + z;
-                const I iy = ((I)x * p.strip[1].width + syl) * Y + z;
-                const I iz = ((I)x * p.ny + y) * p.strip[2].width + szl;
-                // ---- loads ----
-                Pairs<ORD> a_vx, b_vx, c_vz, c_vy;
-                float Mxy = 0.f, Mxz = 0.f, Myz = 0.f, s_xy = 0.f, s_xz = 0.f, s_yz = 0.f;
-                float psi[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-                float r3[R], r4[R], r5[R];
-                // palette: the index first, its table entry after every other load
-                const uint16_t pidx = PAL ? __ldg(p.pal_idx + i) : 0;
-                float gs = 1.f;
-                if (!PAL && ZM == 2) gs = __ldg(p.g_s + i);
-                if (in_xy) {
-                    a_vx = load_pairs<ORD, true>(vx, i, Y);   // vx[y+c+1]-vx[y-c]
-                    b_vx = load_pairs<ORD, true>(vx, i, (I)1);   // vx[z+c+1]-vx[z-c]
-                    if (!PAL) {
-                        Mxy = __ldg(p.mus_dt[0] + i);
-                        Mxz = __ldg(p.mus_dt[1] + i);
-                    }
-                    s_xy = p.s[3][i];
-                    s_xz = p.s[4][i];
-                    if (sx >= 0) {
-                        psi[0] = p.psi[3][ix];
-                        psi[2] = p.psi[5][ix];
-                    }
-                    if (syl >= 0) psi[1] = p.psi[4][iy];
-                    if (szl >= 0) psi[3] = p.psi[6][iz];
-                    if (ZM != 0) {
-    #pragma unroll
-                        for (int l = 0; l < R; ++l)
-                            if (l < n_mech) {
-                                r3[l] = p.r[3][l * G + i];
-                                r4[l] = p.r[4][l * G + i];
-                            }
-                    }
+    float wy[2 * ORD], wz[2 * ORD];   // vy and vz planes [x-ORD, x+ORD-1]
+    xwindow<ORD>(wy, vy, x0 - ORD, p.nx, X, yz);
+    xwindow<ORD>(wz, vz, x0 - ORD, p.nx, X, yz);
+#pragma unroll
+    for (int t = 0; t < kTX3S; ++t) {
+        const int x = x0 + t;
+        if (x >= p.nx) break;
+        const bool in_xy = yz_s && x >= ORD && x < p.nx - ORD + 1;
+        const bool in_yz = yz_s && x >= ORD - 1 && x < p.nx - ORD;
+        if (in_xy || in_yz) {
+            const I i = (I)x * X + yz;
+            const int sx = strip_index(p.strip[0], x);
+            const I ix = ((I)sx * p.ny + y) * Y + z;
+            const I iy = ((I)x * p.strip[1].width + sy) * Y + z;
+            const I iz = ((I)x * p.ny + y) * p.strip[2].width + sz;
+            // ---- loads ----
+            Pairs<ORD> a_vx, b_vx, c_vz, c_vy;
+            float Mxy = 0.f, Mxz = 0.f, Myz = 0.f, s_xy = 0.f, s_xz = 0.f, s_yz = 0.f;
+            float psi[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            float r3[R], r4[R], r5[R];
+            // palette: the index first, its table entry after every other load
+            const uint16_t pidx = PAL ? __ldg(p.pal_idx + i) : 0;
+            float gs = 1.f;
+            if (!PAL && ZM == 2) gs = __ldg(p.g_s + i);
+            if (in_xy) {
+                a_vx = load_pairs<ORD, true>(vx, i, Y);   // vx[y+c+1]-vx[y-c]
+                b_vx = load_pairs<ORD, true>(vx, i, (I)1);   // vx[z+c+1]-vx[z-c]
+                if (!PAL) {
+                    Mxy = __ldg(p.mus_dt[0] + i);
+                    Mxz = __ldg(p.mus_dt[1] + i);
                 }
-                if (in_yz) {
-                    c_vz = load_pairs<ORD, true>(vz, i, Y);   // vz[y+c+1]-vz[y-c]
-                    c_vy = load_pairs<ORD, true>(vy, i, (I)1);   // vy[z+c+1]-vy[z-c]
-                    if (!PAL) Myz = __ldg(p.mus_dt[2] + i);
-                    s_yz = p.s[5][i];
-                    if (syl >= 0) psi[4] = p.psi[7][iy];
-                    if (szl >= 0) psi[5] = p.psi[8][iz];
-                    if (ZM != 0) {
-    #pragma unroll
-                        for (int l = 0; l < R; ++l)
-                            if (l < n_mech) r5[l] = p.r[5][l * G + i];
-                    }
+                s_xy = p.s[3][i];
+                s_xz = p.s[4][i];
+                if (sx >= 0) {
+                    psi[0] = p.psi[3][ix];
+                    psi[2] = p.psi[5][ix];
                 }
-                if constexpr (PAL) {
-                    const float4 c = __ldg(&p.pal[pidx].shear);
-                    Mxy = c.x;
-                    Mxz = c.y;
-                    Myz = c.z;
-                    if (ZM == 2) gs = c.w;
-                }
-                float np_;
-                // ---- sigma_xy: vy[x+c]-vy[x-c-1] (window), sigma_xz: vz[x+c]-vz[x-c-1] (window) ----
-                if (in_xy) {
-                    float a1 = wderiv<ORD>(wy, p), a2 = deriv(a_vx, p, 1);
-                    float b1 = wderiv<ORD>(wz, p), b2 = deriv(b_vx, p, 2);
-                    if (sx >= 0) {
-                        a1 = cpml(a1, psi[0], np_, p.tab_f[0][x]);
-                        p.psi[3][ix] = np_;
-                        b1 = cpml(b1, psi[2], np_, p.tab_f[0][x]);
-                        p.psi[5][ix] = np_;
-                    }
-                    if (syl >= 0) {
-                        a2 = cpml(a2, psi[1], np_, p.tab_h[1][y]);
-                        p.psi[4][iy] = np_;
-                    }
-                    if (szl >= 0) {
-                        b2 = cpml(b2, psi[3], np_, p.tab_h[2][z]);
-                        p.psi[6][iz] = np_;
-                    }
-                    const float ea = a1 + a2, eb = b1 + b2;
-                    float u = Mxy * ea, w = Mxz * eb;
-                    if (ZM != 0) {
-                        float sa = 0.f, sb = 0.f;
-    #pragma unroll
-                        for (int l = 0; l < R; ++l)
-                            if (l < n_mech) {
-                                const float na = fmaf(p.zen.As[l], r3[l], (p.zen.Bs[l] * gs) * ea);
-                                const float nb = fmaf(p.zen.As[l], r4[l], (p.zen.Bs[l] * gs) * eb);
-                                sa += r3[l] + na;
-                                sb += r4[l] + nb;
-                                p.r[3][l * G + i] = na;
-                                p.r[4][l * G + i] = nb;
-                            }
-                        u = fmaf(0.5f * Mxy, sa, u);
-                        w = fmaf(0.5f * Mxz, sb, w);
-                    }
-                    p.s[3][i] = s_xy + u * p.dt;
-                    p.s[4][i] = s_xz + w * p.dt;
-                }
-                // ---- sigma_yz ----
-                if (in_yz) {
-                    float a1 = deriv(c_vz, p, 1), a2 = deriv(c_vy, p, 2);
-                    if (syl >= 0) {
-                        a1 = cpml(a1, psi[4], np_, p.tab_h[1][y]);
-                        p.psi[7][iy] = np_;
-                    }
-                    if (szl >= 0) {
-                        a2 = cpml(a2, psi[5], np_, p.tab_h[2][z]);
-                        p.psi[8][iz] = np_;
-                    }
-                    const float e = a1 + a2;
-                    float u = Myz * e;
-                    if (ZM != 0) {
-                        float sr = 0.f;
-    #pragma unroll
-                        for (int l = 0; l < R; ++l)
-                            if (l < n_mech) {
-                                const float n_ = fmaf(p.zen.As[l], r5[l], (p.zen.Bs[l] * gs) * e);
-                                sr += r5[l] + n_;
-                                p.r[5][l * G + i] = n_;
-                            }
-                        u = fmaf(0.5f * Myz, sr, u);
-                    }
-                    p.s[5][i] = s_yz + u * p.dt;
+                if (sy >= 0) psi[1] = p.psi[4][iy];
+                if (sz >= 0) psi[3] = p.psi[6][iz];
+                if (ZM != 0) {
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) {
+                            r3[l] = p.r[3][l * G + i];
+                            r4[l] = p.r[4][l * G + i];
+                        }
                 }
             }
-            if (t + 1 < kTX3S) {
-                xshift<ORD, !FAST>(wy, vy, x + ORD, p.nx, X, yz);
-                xshift<ORD, !FAST>(wz, vz, x + ORD, p.nx, X, yz);
+            if (in_yz) {
+                c_vz = load_pairs<ORD, true>(vz, i, Y);   // vz[y+c+1]-vz[y-c]
+                c_vy = load_pairs<ORD, true>(vy, i, (I)1);   // vy[z+c+1]-vy[z-c]
+                if (!PAL) Myz = __ldg(p.mus_dt[2] + i);
+                s_yz = p.s[5][i];
+                if (sy >= 0) psi[4] = p.psi[7][iy];
+                if (sz >= 0) psi[5] = p.psi[8][iz];
+                if (ZM != 0) {
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) r5[l] = p.r[5][l * G + i];
+                }
+            }
+            if constexpr (PAL) {
+                const float4 c = __ldg(&p.pal[pidx].shear);
+                Mxy = c.x;
+                Mxz = c.y;
+                Myz = c.z;
+                if (ZM == 2) gs = c.w;
+            }
+            float np_;
+            // ---- sigma_xy: vy[x+c]-vy[x-c-1] (window), sigma_xz: vz[x+c]-vz[x-c-1] (window) ----
+            if (in_xy) {
+                float a1 = wderiv<ORD>(wy, p), a2 = deriv(a_vx, p, 1);
+                float b1 = wderiv<ORD>(wz, p), b2 = deriv(b_vx, p, 2);
+                if (sx >= 0) {
+                    a1 = cpml(a1, psi[0], np_, p.tab_f[0][x]);
+                    p.psi[3][ix] = np_;
+                    b1 = cpml(b1, psi[2], np_, p.tab_f[0][x]);
+                    p.psi[5][ix] = np_;
+                }
+                if (sy >= 0) {
+                    a2 = cpml(a2, psi[1], np_, p.tab_h[1][y]);
+                    p.psi[4][iy] = np_;
+                }
+                if (sz >= 0) {
+                    b2 = cpml(b2, psi[3], np_, p.tab_h[2][z]);
+                    p.psi[6][iz] = np_;
+                }
+                const float ea = a1 + a2, eb = b1 + b2;
+                float u = Mxy * ea, w = Mxz * eb;
+                if (ZM != 0) {
+                    float sa = 0.f, sb = 0.f;
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) {
+                            const float na = fmaf(p.zen.As[l], r3[l], (p.zen.Bs[l] * gs) * ea);
+                            const float nb = fmaf(p.zen.As[l], r4[l], (p.zen.Bs[l] * gs) * eb);
+                            sa += r3[l] + na;
+                            sb += r4[l] + nb;
+                            p.r[3][l * G + i] = na;
+                            p.r[4][l * G + i] = nb;
+                        }
+                    u = fmaf(0.5f * Mxy, sa, u);
+                    w = fmaf(0.5f * Mxz, sb, w);
+                }
+                p.s[3][i] = s_xy + u * p.dt;
+                p.s[4][i] = s_xz + w * p.dt;
+            }
+            // ---- sigma_yz ----
+            if (in_yz) {
+                float a1 = deriv(c_vz, p, 1), a2 = deriv(c_vy, p, 2);
+                if (sy >= 0) {
+                    a1 = cpml(a1, psi[4], np_, p.tab_h[1][y]);
+                    p.psi[7][iy] = np_;
+                }
+                if (sz >= 0) {
+                    a2 = cpml(a2, psi[5], np_, p.tab_h[2][z]);
+                    p.psi[8][iz] = np_;
+                }
+                const float e = a1 + a2;
+                float u = Myz * e;
+                if (ZM != 0) {
+                    float sr = 0.f;
+#pragma unroll
+                    for (int l = 0; l < R; ++l)
+                        if (l < n_mech) {
+                            const float n_ = fmaf(p.zen.As[l], r5[l], (p.zen.Bs[l] * gs) * e);
+                            sr += r5[l] + n_;
+                            p.r[5][l * G + i] = n_;
+                        }
+                    u = fmaf(0.5f * Myz, sr, u);
+                }
+                p.s[5][i] = s_yz + u * p.dt;
             }
         }
-    };
-    if (kStressSweep3 && fast) sweep(std::true_type{});
-    else sweep(std::false_type{});
+        if (t + 1 < kTX3S) {
+            xshift<ORD>(wy, vy, x + ORD, p.nx, X, yz);
+            xshift<ORD>(wz, vz, x + ORD, p.nx, X, yz);
+        }
+    }
     pdl_trigger();
 }
 
